@@ -1,0 +1,169 @@
+// Test-only C shim over the reference mvkit NCC matcher, compiled from the
+// reference's own sources (see oracle/Makefile).  It is the parity pin for the
+// oracle restatement in ncc_oracle.cpp and the generator of tests/golden/.
+// Nothing in the product links or loads this file.
+//
+// Entry points mirror the reference internal API:
+//   mv::ncc_matching::create  src/ncc_matching/model.cpp:120
+//   mv::ncc_matching::find    src/ncc_matching/matcher.cpp:1063
+//   normalized_correlation    src/ncc_matching/model.cpp:105
+#include <ncc_matching/model.hpp>
+#include <core/exception.hpp>
+#include <core/image.hpp>
+#include <core/region.hpp>
+
+#include <cstdint>
+#include <cstring>
+#include <exception>
+#include <new>
+#include <string>
+#include <vector>
+
+namespace {
+namespace ncc = mv::ncc_matching;
+
+void set_error(char* err, int len, const char* text) {
+  if (!err || len <= 0) return;
+  std::strncpy(err, text, std::size_t(len - 1));
+  err[len - 1] = 0;
+}
+
+template <class Fn> int guarded(char* err, int len, Fn&& fn) {
+  try {
+    fn();
+    return 0;
+  } catch (const mv::core::Exception& e) {
+    set_error(err, len, std::string(e.message()).c_str());
+    return int(e.status());
+  } catch (const std::bad_alloc&) {
+    set_error(err, len, "out of memory");
+    return -5;
+  } catch (const std::exception& e) {
+    set_error(err, len, e.what());
+    return -1000;
+  }
+}
+
+// Builds a reference Image from a dense pixel buffer; `mask` (w*h bytes,
+// nullable) becomes the image domain through Region::from_runs.
+mv::core::Image make_image(const void* pixels, int type, std::int64_t w, std::int64_t h,
+                           std::int64_t stride, const std::uint8_t* mask) {
+  const auto pt = type == 1 ? mv::core::PixelType::UInt16 : mv::core::PixelType::UInt8;
+  const std::size_t bpp = type == 1 ? 2 : 1;
+  auto image = mv::core::Image::create(std::size_t(w), std::size_t(h), pt);
+  auto* dst = static_cast<std::byte*>(image.mutable_data());
+  const auto* src = static_cast<const std::byte*>(pixels);
+  for (std::int64_t r = 0; r < h; ++r)
+    std::memcpy(dst + r * image.stride(), src + r * stride, std::size_t(w) * bpp);
+  if (!mask) return image;
+  std::vector<mv::core::RegionRun> runs;
+  for (std::int64_t r = 0; r < h; ++r) {
+    std::int64_t c = 0;
+    while (c < w) {
+      while (c < w && !mask[r * w + c]) ++c;
+      if (c >= w) break;
+      const auto begin = c;
+      while (c < w && mask[r * w + c]) ++c;
+      runs.emplace_back(r, begin, c - 1);
+    }
+  }
+  return image.reduce_domain(mv::core::Region::from_runs(runs));
+}
+}  // namespace
+
+extern "C" {
+
+int ref_ncc_create(const void* tmpl, int type, std::int64_t w, std::int64_t h, std::int64_t stride,
+                   const std::uint8_t* mask, int levels, double angle_start, double angle_extent,
+                   double angle_step, int ignore_polarity, void** out, char* err, int errlen) {
+  *out = nullptr;
+  return guarded(err, errlen, [&] {
+    ncc::CreateOptions o;
+    o.levels = levels;
+    o.angle_start = angle_start;
+    o.angle_extent = angle_extent;
+    o.angle_step = angle_step;
+    o.ignore_global_polarity = ignore_polarity != 0;
+    auto model = new ncc::Model(ncc::create(make_image(tmpl, type, w, h, stride, mask), o));
+    *out = model;
+  });
+}
+
+void ref_ncc_free(void* model) { delete static_cast<ncc::Model*>(model); }
+
+// info[0]=levels info[1]=angle_step info[2]=origin_row info[3]=origin_column
+// info[4]=patches per level (level 0)  info[5]=original sample count
+void ref_ncc_model_info(void* model, double* info) {
+  const auto& m = *static_cast<ncc::Model*>(model);
+  info[0] = double(m.levels.size());
+  info[1] = m.options.angle_step;
+  info[2] = m.origin_row;
+  info[3] = m.origin_column;
+  info[4] = double(m.levels.front().patches.size());
+  info[5] = double(m.original.samples.size());
+}
+
+// Level geometry: dims[0]=width dims[1]=height; origin[0..1]=origin row/col.
+void ref_ncc_level(void* model, int level, std::int64_t* dims, double* origin) {
+  const auto& l = static_cast<ncc::Model*>(model)->levels[std::size_t(level)];
+  dims[0] = std::int64_t(l.width);
+  dims[1] = std::int64_t(l.height);
+  origin[0] = l.origin_row;
+  origin[1] = l.origin_column;
+}
+
+// Copies one patch: returns sample count; rows/cols/weights are filled when
+// non-null and capacity allows.  meta = {angle, origin_row, origin_column, weight_sum}.
+std::int64_t ref_ncc_patch(void* model, int level, int index, std::int32_t* rows,
+                           std::int32_t* cols, double* weights, std::int64_t capacity, double* meta) {
+  const auto& m = *static_cast<ncc::Model*>(model);
+  const auto& p = level < 0 ? m.original : m.levels[std::size_t(level)].patches[std::size_t(index)];
+  meta[0] = p.angle;
+  meta[1] = p.origin_row;
+  meta[2] = p.origin_column;
+  meta[3] = p.weight_sum;
+  const auto n = std::int64_t(p.samples.size());
+  if (rows && n <= capacity)
+    for (std::int64_t i = 0; i < n; ++i) {
+      rows[i] = p.samples[std::size_t(i)].row;
+      cols[i] = p.samples[std::size_t(i)].column;
+      weights[i] = p.samples[std::size_t(i)].weight;
+    }
+  return n;
+}
+
+// Runs the reference find; out is capacity x 4 doubles (row, column, angle,
+// score) in the matcher's internal pixel-centre convention.
+int ref_ncc_find(void* model, const void* img, int type, std::int64_t w, std::int64_t h,
+                 std::int64_t stride, const std::uint8_t* domain, double angle_start,
+                 double angle_extent, double min_score, std::int64_t num_matches, double max_overlap,
+                 int subpixel, int highest, int lowest, double* out, std::int64_t capacity,
+                 std::int64_t* count, char* err, int errlen) {
+  *count = 0;
+  return guarded(err, errlen, [&] {
+    ncc::FindOptions o;
+    o.angle_start = angle_start;
+    o.angle_extent = angle_extent;
+    o.min_score = min_score;
+    o.num_matches = std::size_t(num_matches);
+    o.max_overlap = max_overlap;
+    o.subpixel = subpixel != 0;
+    o.highest_level = highest;
+    o.lowest_level = lowest < 1 ? 1 : lowest;
+    const auto found = ncc::find(make_image(img, type, w, h, stride, domain),
+                                 *static_cast<ncc::Model*>(model), o);
+    *count = std::int64_t(found.size());
+    for (std::size_t i = 0; i < found.size() && std::int64_t(i) < capacity; ++i) {
+      out[4 * i + 0] = found[i].row;
+      out[4 * i + 1] = found[i].column;
+      out[4 * i + 2] = found[i].angle;
+      out[4 * i + 3] = found[i].score;
+    }
+  });
+}
+
+double ref_normalized_correlation(const double* a, const double* b, std::int64_t n, int absolute) {
+  return ncc::normalized_correlation({a, std::size_t(n)}, {b, std::size_t(n)}, absolute != 0);
+}
+
+}  // extern "C"
