@@ -1,0 +1,115 @@
+/* GB300 NCC matching: C ABI of libmvkit_gb300.so.
+ *
+ * Drop-in boundary for mvkit's NCC matching operators.  Each entry point
+ * takes plain pointers and scalars: the control tuples of the reference
+ * operators become one scalar each, the output tuples become caller-owned
+ * double arrays.  Status codes are the reference's MvStatus values
+ * (include/mvkit/c/mv_status.h:12-24): 0 ok, -1 invalid argument,
+ * -3 type mismatch, -5 out of memory, -6 unsupported, -7 invalid state,
+ * -103 limit exceeded, -1000 internal error.  On failure the thread-local
+ * message of mvg_last_error() says why (reference: mv_get_last_error,
+ * include/mvkit/c/mv_api.h:75).  No call throws across the ABI.
+ *
+ * Pixel types: 0 = byte (uint8), 1 = uint2 (uint16), one channel.
+ * Search runs on the current CUDA device; results are synchronous. */
+#ifndef MVKIT_GB300_NCC_H
+#define MVKIT_GB300_NCC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define MVG_API __attribute__((visibility("default")))
+#else
+#define MVG_API
+#endif
+
+typedef struct mvg_ncc_model_s* mvg_ncc_model;
+
+#define MVG_PIXEL_BYTE 0
+#define MVG_PIXEL_UINT2 1
+#define MVG_METRIC_USE_POLARITY 0
+#define MVG_METRIC_IGNORE_GLOBAL_POLARITY 1
+#define MVG_MEMORY_HOST 0
+#define MVG_MEMORY_DEVICE 1
+
+/* Replaces mv_create_ncc_model (include/mvkit/c/mv_ncc_matching.h:30-32).
+ * Template: pixels (row_stride bytes apart); domain: width*height bytes,
+ * nonzero = inside the template ROI, NULL = whole image.  num_levels: 0 or
+ * -1 = "auto" (both build as many levels as the template allows, as the
+ * reference does for 0 and "auto"), else 1..16.  angle_step: 0 or negative
+ * = "auto", else (0, pi/16].  metric: MVG_METRIC_*.  *model_id receives an
+ * owned handle; free it with mvg_clear_ncc_model. */
+MVG_API int32_t mvg_create_ncc_model(const void* pixels, int32_t pixel_type, int64_t width, int64_t height,
+                             int64_t row_stride, const uint8_t* domain, int32_t num_levels,
+                             double angle_start, double angle_extent, double angle_step, int32_t metric,
+                             mvg_ncc_model* model_id);
+
+/* Replaces mv_get_ncc_model_params (include/mvkit/c/mv_ncc_matching.h:46-47).
+ * angle_step is 0 for a model without angle range, as the reference reports. */
+MVG_API int32_t mvg_get_ncc_model_params(mvg_ncc_model model_id, int32_t* num_levels, double* angle_start,
+                                 double* angle_extent, double* angle_step, int32_t* metric);
+
+/* Releases a model (the reference frees it with the handle tuple,
+ * mv_destroy_tuple; include/mvkit/c/mv_ncc_matching.h:64-67). */
+MVG_API int32_t mvg_clear_ncc_model(mvg_ncc_model model_id);
+
+/* Replaces mv_find_ncc_model (include/mvkit/c/mv_ncc_matching.h:71-74).
+ * pixels: host memory (location MVG_MEMORY_HOST; copied to the device
+ * inside the call) or device memory (MVG_MEMORY_DEVICE).  Controls as the
+ * reference's tuples: angle_start/angle_extent in radians, min_score and
+ * max_overlap in [0, 1], num_matches >= 0 (0 = all), subpixel 0/1
+ * ("false"/"true"), highest_level >= 0 (0 = all model levels), lowest_level
+ * >= 1 (the reference's [highest, lowest] NumLevels pair; pass 1 for a
+ * single NumLevels value).  Outputs row/column/angle/score (capacity
+ * entries each) in the operator's convention (edge-centred translation,
+ * src/c_api/ncc_matching_api.cpp:171-176); *count receives the number of
+ * matches (entries beyond capacity are dropped).  stream: a cudaStream_t or
+ * NULL for the library's per-thread stream. */
+MVG_API int32_t mvg_find_ncc_model(const void* pixels, int32_t pixel_type, int64_t width, int64_t height,
+                           int64_t row_stride, int32_t location, mvg_ncc_model model_id,
+                           double angle_start, double angle_extent, double min_score, int64_t num_matches,
+                           double max_overlap, int32_t subpixel, int32_t highest_level, int32_t lowest_level,
+                           double* row, double* column, double* angle, double* score, int64_t capacity,
+                           int64_t* count, void* stream);
+
+/* Candidate list of one internal stage of a find, in the matcher's
+ * pixel-centre pose convention (mv::ncc_matching::find,
+ * src/ncc_matching/matcher.cpp:1063): stage 0 = coarse candidates after
+ * non-maximum suppression; k >= 1 = after the k-th coarse-to-fine tracking
+ * step; 100 = scored and sorted full-resolution candidates; -1 = final
+ * matches.  out holds capacity x 4 doubles (row, column, angle, score). */
+MVG_API int32_t mvg_find_ncc_model_stage(const void* pixels, int32_t pixel_type, int64_t width, int64_t height,
+                                 int64_t row_stride, int32_t location, mvg_ncc_model model_id,
+                                 double angle_start, double angle_extent, double min_score,
+                                 int64_t num_matches, double max_overlap, int32_t subpixel,
+                                 int32_t highest_level, int32_t lowest_level, int32_t stage, double* out,
+                                 int64_t capacity, int64_t* count);
+
+/* Search-pyramid level of an image as the matcher holds it: exact integer
+ * sums of 4^level input pixels over the crop the model implies (the
+ * reference's FP64 level value is sum/4^level minus the crop's first pixel).
+ * geom[0..4] = width, height, crop_row, crop_column, first crop pixel. */
+MVG_API int32_t mvg_ncc_pyramid_level(const void* pixels, int32_t pixel_type, int64_t width, int64_t height,
+                              int64_t row_stride, mvg_ncc_model model_id, int32_t highest_level, int32_t level,
+                              float* out, int64_t capacity, double* geom);
+
+/* Thread-local message of the last failed call (empty after success). */
+MVG_API const char* mvg_last_error(void);
+
+/* Page-locked host buffers for zero-staging uploads, and device buffers for
+ * callers without their own allocator. */
+MVG_API int32_t mvg_host_alloc(size_t bytes, void** ptr);
+MVG_API int32_t mvg_host_free(void* ptr);
+MVG_API int32_t mvg_device_alloc(size_t bytes, void** ptr);
+MVG_API int32_t mvg_device_free(void* ptr);
+MVG_API int32_t mvg_copy_to_device(void* dst, const void* src, size_t bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

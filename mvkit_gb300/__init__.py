@@ -1,0 +1,6 @@
+"""GB300-native NCC template matching (mvkit FindNccModel / CreateNccModel)."""
+from .ncc import (MvError, NccModel, DeviceImage, PinnedBuffer, create_ncc_model, find_ncc_model,
+                  find_ncc_model_stage, get_ncc_model_params, load, pyramid_level)
+
+__all__ = ["MvError", "NccModel", "DeviceImage", "PinnedBuffer", "create_ncc_model", "find_ncc_model",
+           "find_ncc_model_stage", "get_ncc_model_params", "load", "pyramid_level"]

@@ -1,0 +1,895 @@
+// Host side of the GB300 NCC find: query planning (crop, patch lists,
+// position ranges) in FP64 exactly as the reference plans it, the kernel
+// sequence on one CUDA stream, and the C ABI of include/mvkit_gb300_ncc.h.
+//   prepare  src/ncc_matching/matcher.cpp:343-851
+//   find     src/ncc_matching/matcher.cpp:1063-1076
+//   C API    src/c_api/ncc_matching_api.cpp:29-203
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/mvkit_gb300_ncc.h"
+#include "ncc_kernels.h"
+#include "ncc_model.h"
+
+namespace mvg {
+namespace {
+
+thread_local std::string g_last_error;
+
+void check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    if (e == cudaErrorMemoryAllocation) raise(kOutOfMemory, std::string(what) + ": " + cudaGetErrorString(e));
+    raise(kInternal, std::string(what) + ": " + cudaGetErrorString(e));
+  }
+}
+
+template <class T> struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void reserve(size_t count) {
+    if (count <= n && p) return;
+    release();
+    check(cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T)), "cudaMalloc");
+    n = std::max<size_t>(count, 1);
+  }
+  void upload(const std::vector<T>& v, cudaStream_t s) {
+    reserve(v.size());
+    if (!v.empty()) check(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s), "upload");
+  }
+};
+
+// ------------------------------------------------------------------ model
+struct DevLevel {
+  std::vector<PatchDesc> desc;      // host copy (model patches + query endpoints)
+  std::vector<double> angles;
+  size_t model_patches = 0;         // trained patches; endpoints follow
+  std::vector<int32_t> offs, runs, runs_end;
+  std::vector<float> w;
+  DevBuf<PatchDesc> d_desc;
+  DevBuf<int32_t> d_offs, d_runs, d_runs_end;
+  DevBuf<float> d_w;
+  void append(const Raster& r) {
+    PatchDesc d{};
+    d.angle = r.angle;
+    d.orow = r.orow;
+    d.ocol = r.ocol;
+    d.rmin = r.rmin;
+    d.rmax = r.rmax;
+    d.cmin = r.cmin;
+    d.cmax = r.cmax;
+    d.n = int32_t(r.size());
+    d.sample_off = int32_t(offs.size());
+    d.nruns = int32_t(r.run_row.size());
+    d.run_off = int32_t(runs.size());
+    for (size_t i = 0; i < r.size(); ++i) {
+      offs.push_back(int32_t((uint32_t(uint16_t(int16_t(r.rows[i]))) << 16) | uint16_t(int16_t(r.cols[i]))));
+      w.push_back(float(r.w[i]));
+    }
+    for (size_t j = 0; j < r.run_row.size(); ++j) {
+      runs.push_back(int32_t((uint32_t(uint16_t(int16_t(r.run_row[j]))) << 16) | uint16_t(int16_t(r.run_begin[j]))));
+      runs_end.push_back(r.run_end[j]);
+    }
+    desc.push_back(d);
+    angles.push_back(r.angle);
+  }
+  // Replaced device tables stay allocated until the model is cleared: finds
+  // on other threads may still be reading them.
+  std::vector<void*> retired;
+  ~DevLevel() {
+    for (void* p : retired) cudaFree(p);
+  }
+  template <class T> void retire(DevBuf<T>& b) {
+    if (b.p) retired.push_back(b.p);
+    b.p = nullptr;
+    b.n = 0;
+  }
+  void upload() {
+    retire(d_desc);
+    retire(d_offs);
+    retire(d_runs);
+    retire(d_runs_end);
+    retire(d_w);
+    d_desc.upload(desc, nullptr);
+    d_offs.upload(offs, nullptr);
+    d_runs.upload(runs, nullptr);
+    d_runs_end.upload(runs_end, nullptr);
+    d_w.upload(w, nullptr);
+    check(cudaDeviceSynchronize(), "model upload");
+  }
+  LevelView view() const {
+    LevelView v;
+    v.patches = d_desc.p;
+    v.offs = d_offs.p;
+    v.w = d_w.p;
+    v.runs = d_runs.p;
+    v.runs_end = d_runs_end.p;
+    v.npatches = int32_t(desc.size());
+    return v;
+  }
+};
+
+struct OrigDev {
+  DevBuf<float> dr, dc, w;
+  int32_t n = 0;
+  void set(const Raster& r, double orow, double ocol) {
+    std::vector<float> a(r.size()), b(r.size()), c(r.size());
+    for (size_t i = 0; i < r.size(); ++i) {
+      a[i] = float(double(r.rows[i]) - orow);
+      b[i] = float(double(r.cols[i]) - ocol);
+      c[i] = float(r.w[i]);
+    }
+    dr.upload(a, nullptr);
+    dc.upload(b, nullptr);
+    w.upload(c, nullptr);
+    n = int32_t(r.size());
+    check(cudaDeviceSynchronize(), "model upload");
+  }
+  OriginalView view() const { return OriginalView{dr.p, dc.p, w.p, n}; }
+};
+
+}  // namespace
+}  // namespace mvg
+
+struct mvg_ncc_model_s {
+  mvg::HostModel host;
+  std::vector<std::unique_ptr<mvg::DevLevel>> levels;
+  mvg::OrigDev original;
+  // unrotated rasters of coarser finest levels (lowest_level > 1), by level
+  std::vector<std::unique_ptr<mvg::OrigDev>> coarse_original;
+  std::mutex mutex;  // guards the endpoint caches
+  int device = 0;
+};
+
+namespace mvg {
+namespace {
+
+// Index of the raster at `angle` on `level` among the query endpoints,
+// building and uploading it on first use.  -1 when degenerate.
+int endpoint_patch(mvg_ncc_model_s& m, size_t level, double angle) {
+  DevLevel& L = *m.levels[level];
+  for (size_t i = L.model_patches; i < L.desc.size(); ++i)
+    if (L.angles[i] == angle) return int(i);
+  Raster r = rotate_level(m.host.levels[level], angle);
+  if (r.w.empty()) return -1;
+  L.append(r);
+  L.upload();
+  return int(L.desc.size() - 1);
+}
+
+const OrigDev& coarse_original(mvg_ncc_model_s& m, size_t level) {
+  if (m.coarse_original.size() <= level) m.coarse_original.resize(level + 1);
+  if (!m.coarse_original[level]) {
+    Raster r = rotate_level(m.host.levels[level], 0.);
+    auto o = std::make_unique<OrigDev>();
+    o->set(r, m.host.levels[level].orow, m.host.levels[level].ocol);
+    m.coarse_original[level] = std::move(o);
+  }
+  return *m.coarse_original[level];
+}
+
+// ------------------------------------------------------------- query plan
+struct FindParams {
+  double angle_start = 0, angle_extent = 0, min_score = .8, max_overlap = .5;
+  int64_t num_matches = 1;
+  bool subpixel = true;
+  int highest = 0, lowest = 1;
+};
+
+// Largest/smallest integer r in [lo, hi) with pred(r) true, for predicates
+// monotone over r.  Returns an empty range when none holds.
+template <class Pred> void clip_increasing(int& lo, int& hi, Pred below_min) {
+  // below_min(r) true for small r, false from some r on (monotone).
+  int a = lo, b = hi;
+  while (a < b) {
+    const int mid = a + (b - a) / 2;
+    if (below_min(mid)) a = mid + 1;
+    else b = mid;
+  }
+  lo = a;
+}
+template <class Pred> void clip_decreasing(int& lo, int& hi, Pred above_max) {
+  // above_max(r) false for small r, true from some r on.
+  int a = lo, b = hi;
+  while (a < b) {
+    const int mid = a + (b - a) / 2;
+    if (above_max(mid)) b = mid;
+    else a = mid + 1;
+  }
+  hi = a;
+}
+
+// Position interval on a level where the pose lies in the search domain as
+// the reference tests it (may_contain, matcher.cpp:507-534; full image
+// domain) and, optionally, inside [base_lo, base_hi).
+void pose_interval(int& lo, int& hi, double crop, double step, double o, double off, double extent_max) {
+  auto pose = [&](int r) { return crop + step * (r + o) + off; };
+  if (step == 1) {
+    // domain_contains: 0 <= floor(pose + .5) <= extent_max
+    clip_increasing(lo, hi, [&](int r) { return std::floor(pose(r) + .5) < 0; });
+    clip_decreasing(lo, hi, [&](int r) { return std::floor(pose(r) + .5) > extent_max; });
+  } else {
+    const double margin = 2 * step;
+    clip_increasing(lo, hi, [&](int r) { return pose(r) < 0 - margin; });
+    clip_decreasing(lo, hi, [&](int r) { return pose(r) > extent_max + margin; });
+  }
+  if (hi < lo) hi = lo;
+}
+
+struct LevelPlan {
+  std::vector<int32_t> plist;  // query patch order
+  std::vector<PosRange> ranges;
+};
+
+// ------------------------------------------------------------- workspace
+struct Workspace {
+  int device = -1;
+  cudaStream_t own_stream = nullptr;
+  DevBuf<uint8_t> image;
+  DevBuf<float> lev_v[kMaxLevels];
+  DevBuf<longlong2> lev_p[kMaxLevels];
+  DevBuf<float> planes;
+  DevBuf<Cand> cand_a, cand_b, tmp, sorted, accepted;
+  DevBuf<int> table;
+  DevBuf<Refined> refined;
+  DevBuf<int32_t> refined_flag, batch;
+  DevBuf<QueryState> state;
+  DevBuf<uint8_t> tables;            // query patch lists and ranges, one upload
+  uint8_t* h_tables = nullptr;       // pinned staging of the same
+  size_t h_tables_size = 0;
+  QueryState* h_state = nullptr;
+  int32_t* h_error = nullptr;
+  size_t smem_optin = 0;
+  ~Workspace() {
+    if (h_tables) cudaFreeHost(h_tables);
+    if (h_state) cudaFreeHost(h_state);
+    if (own_stream) cudaStreamDestroy(own_stream);
+  }
+  void init() {
+    int dev = 0;
+    check(cudaGetDevice(&dev), "cudaGetDevice");
+    if (device == dev) return;
+    device = dev;
+    check(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    check(cudaMallocHost(&h_state, sizeof(QueryState)), "cudaMallocHost");
+    int optin = 0;
+    check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "attribute");
+    smem_optin = size_t(optin);
+    cand_a.reserve(kMaxCandidates);
+    cand_b.reserve(kMaxCandidates);
+    tmp.reserve(kMaxCandidates);
+    sorted.reserve(kMaxCandidates);
+    accepted.reserve(kMaxCandidates);
+    table.reserve(kHashSlots);
+    refined.reserve(kMaxCandidates);
+    refined_flag.reserve(kMaxCandidates);
+    batch.reserve(64);
+    state.reserve(1);
+  }
+  // Stages `bytes` of query tables; returns the pinned host pointer.
+  uint8_t* stage_tables(size_t bytes) {
+    if (bytes > h_tables_size) {
+      if (h_tables) cudaFreeHost(h_tables);
+      h_tables = nullptr;
+      h_tables_size = 0;
+      check(cudaMallocHost(&h_tables, bytes), "cudaMallocHost");
+      h_tables_size = bytes;
+    }
+    tables.reserve(bytes);
+    return h_tables;
+  }
+};
+
+thread_local std::unique_ptr<Workspace> t_workspace;
+
+Workspace& workspace() {
+  if (!t_workspace) t_workspace = std::make_unique<Workspace>();
+  t_workspace->init();
+  return *t_workspace;
+}
+
+struct Match {
+  double row, col, angle, score;
+};
+
+struct FindOutput {
+  std::vector<Match> matches;
+  std::vector<Match> stage;   // requested stage dump
+};
+
+constexpr double kMissing = -std::numeric_limits<double>::infinity();
+
+void fetch_stage(Workspace& ws, cudaStream_t s, const Cand* src, int slot, FindOutput& out) {
+  check(cudaMemcpyAsync(ws.h_state, ws.state.p, sizeof(QueryState), cudaMemcpyDeviceToHost, s), "state");
+  check(cudaStreamSynchronize(s), "sync");
+  const int n = slot < 0 ? ws.h_state->sorted_count : std::min(ws.h_state->count[slot], kMaxCandidates);
+  std::vector<Cand> h(size_t(std::max(n, 0)));
+  if (n > 0) check(cudaMemcpyAsync(h.data(), src, size_t(n) * sizeof(Cand), cudaMemcpyDeviceToHost, s), "stage");
+  check(cudaStreamSynchronize(s), "sync");
+  for (const Cand& c : h) out.stage.push_back({c.row, c.col, c.angle, c.score});
+}
+
+// One find on the current device.  stage >= 0 stops after that stage and
+// returns its candidate list.
+FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W, int64_t H, int64_t stride,
+                    int location, const FindParams& req, cudaStream_t user_stream, int stage) {
+  FindOutput out;
+  const HostModel& hm = m.host;
+  // src/ncc_matching/matcher.cpp:349-374 (validation and range clipping)
+  if (type != 0 && type != 1) raise(kTypeMismatch, "one byte or uint2 channel required");
+  if (!pixels) raise(kInvalidArgument, "image pixels must not be null");
+  if (hm.levels.empty()) raise(kInvalidState, "model is empty");
+  if (req.highest < 0 || req.lowest < 1) raise(kInvalidArgument, "invalid pyramid levels");
+  const size_t level_count = req.highest ? std::min(hm.levels.size(), size_t(req.highest)) : hm.levels.size();
+  const size_t finest = std::min(size_t(req.lowest), level_count) - 1;
+  FindParams opt = req;
+  if (!std::isfinite(opt.angle_start) || !std::isfinite(opt.angle_extent) || opt.angle_extent < 0 ||
+      !std::isfinite(opt.min_score) || opt.min_score < 0 || opt.min_score > 1 || !std::isfinite(opt.max_overlap) ||
+      opt.max_overlap < 0 || opt.max_overlap > 1 || opt.num_matches < 0)
+    raise(kInvalidArgument, "invalid query range, score, overlap or candidate budget");
+  const double angle_end = opt.angle_start + opt.angle_extent;  // unclipped, as the reference
+  if (!std::isfinite(angle_end)) raise(kInvalidArgument, "query angle range must be finite");
+  const double cs = std::max(opt.angle_start, hm.params.angle_start);
+  const double ce = std::min(angle_end, hm.params.angle_start + hm.params.angle_extent);
+  if (cs > ce + 1e-12) return out;
+  opt.angle_start = cs;
+  opt.angle_extent = std::max(0., ce - cs);
+  if (W <= 0 || H <= 0 || W > std::numeric_limits<int>::max() || H > std::numeric_limits<int>::max() ||
+      H > 32000000 / W)
+    raise(kLimitExceeded, "search image exceeds pixel budget");
+  const int64_t bpp = type == 1 ? 2 : 1;
+  if (stride < W * bpp || stride % bpp) raise(kInvalidArgument, "invalid row stride");
+
+  // crop with halo on the pyramid lattice (matcher.cpp:383-393), full domain
+  const ModelLevel& base = hm.levels.front();
+  const double radius = std::hypot(std::max(base.orow, double(base.height - 1) - base.orow),
+                                   std::max(base.ocol, double(base.width - 1) - base.ocol));
+  const int64_t lattice = int64_t(size_t{1} << (level_count - 1));
+  const int64_t halo = int64_t(std::ceil(radius)) + 4 * lattice;
+  const int64_t crop_row = std::max<int64_t>(0, 0 - halo) / lattice * lattice;
+  const int64_t crop_col = std::max<int64_t>(0, 0 - halo) / lattice * lattice;
+  const int64_t crop_bottom = std::min<int64_t>(H, ((H - 1 + halo) / lattice + 1) * lattice);
+  const int64_t crop_right = std::min<int64_t>(W, ((W - 1 + halo) / lattice + 1) * lattice);
+
+  Workspace& ws = workspace();
+  cudaStream_t s = user_stream ? user_stream : ws.own_stream;
+  // Planning reads (and may extend) the model's endpoint rasters: serialise
+  // it per model and snapshot the device views used by this find.
+  std::unique_lock<std::mutex> lock(m.mutex);
+  LevelView views[kMaxLevels];
+
+  // query patch lists (matcher.cpp:463-482)
+  std::vector<LevelPlan> plan(level_count);
+  for (size_t li = 0; li < level_count; ++li) {
+    DevLevel& L = *m.levels[li];
+    auto& list = plan[li].plist;
+    for (size_t p = 0; p < L.model_patches; ++p)
+      if (L.angles[p] >= opt.angle_start - 1e-12 && L.angles[p] <= angle_end + 1e-12) list.push_back(int32_t(p));
+    for (const double a : {opt.angle_start, angle_end}) {
+      bool found = false;
+      for (int32_t p : list)
+        if (std::abs(L.angles[size_t(p)] - a) < 1e-12) found = true;
+      if (found) continue;
+      const int e = endpoint_patch(m, li, a);
+      if (e >= 0) list.push_back(e);
+    }
+  }
+  const size_t top = level_count - 1;
+  const double coarse_radius = .5 * std::hypot(double(hm.levels[top].width), double(hm.levels[top].height));
+  const size_t angle_stride = std::max<size_t>(1, size_t(std::min(double(plan[top].plist.size()),
+      std::ceil(.5 / std::max(1e-20, coarse_radius * hm.params.angle_step)))));
+  {
+    auto& ca = plan[top].plist;
+    const DevLevel& L = *m.levels[top];
+    std::sort(ca.begin(), ca.end(), [&](int32_t x, int32_t y) { return L.angles[size_t(x)] < L.angles[size_t(y)]; });
+    size_t kept = 0;
+    for (size_t i = 0; i < ca.size(); ++i)
+      if (i % angle_stride == 0 || i + 1 == ca.size()) ca[kept++] = ca[i];
+    ca.resize(kept);
+  }
+  // level geometry of the crop
+  int lw[kMaxLevels], lh[kMaxLevels];
+  lw[0] = int(crop_right - crop_col);
+  lh[0] = int(crop_bottom - crop_row);
+  for (size_t l = 1; l < level_count; ++l) {
+    lw[l] = std::max(1, lw[l - 1] / 2);
+    lh[l] = std::max(1, lh[l - 1] / 2);
+  }
+  // position ranges per level and patch
+  const double Hd = double(H), Wd = double(W);
+  for (size_t li = 0; li < level_count; ++li) {
+    const DevLevel& L = *m.levels[li];
+    const double step = std::ldexp(1., int(li)), off = (step - 1) * .5;
+    for (int32_t p : plan[li].plist) {
+      const PatchDesc& d = L.desc[size_t(p)];
+      PosRange rg;
+      rg.r0 = std::max(0, -d.rmin);
+      rg.r1 = lh[li] - d.rmax;
+      rg.c0 = std::max(0, -d.cmin);
+      rg.c1 = lw[li] - d.cmax;
+      if (li == top) {
+        // coarse scan bounds (matcher.cpp:549-553)
+        const double margin = step == 1 ? .5 : 2 * step;
+        rg.r0 = std::max(rg.r0, int(std::ceil((0 - margin - double(crop_row) - off) / step - d.orow)));
+        rg.r1 = std::min(rg.r1, int(std::floor((Hd - 1 + margin - double(crop_row) - off) / step - d.orow)) + 1);
+        rg.c0 = std::max(rg.c0, int(std::ceil((0 - margin - double(crop_col) - off) / step - d.ocol)));
+        rg.c1 = std::min(rg.c1, int(std::floor((Wd - 1 + margin - double(crop_col) - off) / step - d.ocol)) + 1);
+      }
+      if (rg.r1 < rg.r0) rg.r1 = rg.r0;
+      if (rg.c1 < rg.c0) rg.c1 = rg.c0;
+      pose_interval(rg.r0, rg.r1, double(crop_row), step, d.orow, off, Hd - 1);
+      pose_interval(rg.c0, rg.c1, double(crop_col), step, d.ocol, off, Wd - 1);
+      plan[li].ranges.push_back(rg);
+    }
+  }
+
+  const size_t finest_level = finest;
+  const OriginalView orig = finest_level ? coarse_original(m, finest_level).view() : m.original.view();
+  for (size_t li = 0; li < level_count; ++li) views[li] = m.levels[li]->view();
+  std::vector<PatchDesc> top_desc(m.levels[top]->desc);
+  lock.unlock();
+
+  // upload image and query tables (one pinned copy for the tables)
+  const void* dev_pixels = pixels;
+  int64_t pitch_elems = stride / bpp;
+  if (location == MVG_MEMORY_HOST) {
+    const size_t bytes = size_t(stride) * size_t(H - 1) + size_t(W * bpp);
+    ws.image.reserve(bytes);
+    check(cudaMemcpyAsync(ws.image.p, pixels, bytes, cudaMemcpyHostToDevice, s), "image upload");
+    dev_pixels = ws.image.p;
+  }
+  const int32_t* d_plist[kMaxLevels];
+  const PosRange* d_ranges[kMaxLevels];
+  {
+    size_t total = 0;
+    std::vector<size_t> at(2 * level_count);
+    for (size_t li = 0; li < level_count; ++li) {
+      at[2 * li] = total;
+      total += (plan[li].plist.size() * sizeof(int32_t) + 15) & ~size_t(15);
+      at[2 * li + 1] = total;
+      total += (plan[li].ranges.size() * sizeof(PosRange) + 15) & ~size_t(15);
+    }
+    uint8_t* h = ws.stage_tables(std::max<size_t>(total, 16));
+    for (size_t li = 0; li < level_count; ++li) {
+      std::memcpy(h + at[2 * li], plan[li].plist.data(), plan[li].plist.size() * sizeof(int32_t));
+      std::memcpy(h + at[2 * li + 1], plan[li].ranges.data(), plan[li].ranges.size() * sizeof(PosRange));
+      d_plist[li] = reinterpret_cast<const int32_t*>(ws.tables.p + at[2 * li]);
+      d_ranges[li] = reinterpret_cast<const PosRange*>(ws.tables.p + at[2 * li + 1]);
+    }
+    check(cudaMemcpyAsync(ws.tables.p, h, total, cudaMemcpyHostToDevice, s), "tables");
+  }
+  check(cudaMemsetAsync(ws.state.p, 0, sizeof(QueryState), s), "memset");
+
+  // pyramid (levels finest..top as needed; level 0 always feeds the rest)
+  LevelImage lev[kMaxLevels];
+  for (size_t l = 0; l < level_count; ++l) {
+    ws.lev_v[l].reserve(size_t(lw[l]) * size_t(lh[l]));
+    lev[l].v = ws.lev_v[l].p;
+    lev[l].w = lw[l];
+    lev[l].h = lh[l];
+  }
+  QueryState* st = ws.state.p;
+  int32_t* err_flag = &st->error;
+  check(launch_pyramid0(dev_pixels, type, pitch_elems, int(crop_row), int(crop_col), lev[0], err_flag, s), "pyramid0");
+  for (size_t l = 1; l < level_count; ++l) check(launch_pyramid(lev[l - 1], lev[l], err_flag, s), "pyramid");
+  const size_t first_target = std::max(finest, size_t(opt.subpixel ? 1 : 0));
+  for (size_t l = 0; l < level_count; ++l) {
+    const bool need = l == top || (l + 1 <= top && l >= first_target);
+    if (!need) continue;
+    ws.lev_p[l].reserve(size_t(lw[l] + 1) * size_t(lh[l]));
+    lev[l].prefix = ws.lev_p[l].p;
+    check(launch_prefix(lev[l], s), "prefix");
+  }
+
+  // coarse scan + NMS
+  const double scale = std::ldexp(1., int(top)), phase = (scale - 1) * .5;
+  const int nplist = int(plan[top].plist.size());
+  int max_bh = 0, max_bw = 0;
+  for (int32_t p : plan[top].plist) {
+    max_bh = std::max(max_bh, top_desc[size_t(p)].rmax - top_desc[size_t(p)].rmin);
+    max_bw = std::max(max_bw, top_desc[size_t(p)].cmax - top_desc[size_t(p)].cmin);
+  }
+  ws.planes.reserve(size_t(std::max(nplist, 1)) * size_t(lw[top]) * size_t(lh[top]));
+  if (nplist > 0) {
+    CoarseArgs ca;
+    ca.lev = lev[top];
+    ca.view = views[top];
+    ca.plist = d_plist[top];
+    ca.ranges = d_ranges[top];
+    ca.nplist = nplist;
+    ca.planes = ws.planes.p;
+    ca.absolute = hm.params.ignore_polarity;
+    const cudaError_t e = launch_coarse(ca, max_bh, max_bw, s, ws.smem_optin);
+    if (e == cudaErrorInvalidConfiguration) raise(kUnsupported, "coarse template raster exceeds on-chip tile");
+    check(e, "coarse");
+    NmsArgs na;
+    na.planes = ws.planes.p;
+    na.nplist = nplist;
+    na.w = lw[top];
+    na.h = lh[top];
+    na.plist = d_plist[top];
+    na.view = views[top];
+    na.crop_row = double(crop_row);
+    na.crop_col = double(crop_col);
+    na.scale = scale;
+    na.phase = phase;
+    na.threshold = opt.min_score * .4;
+    na.out = ws.cand_a.p;
+    na.state = st;
+    na.max_candidates = kMaxCandidates;
+    check(launch_nms(na, s), "nms");
+  }
+  if (stage == 0) {
+    fetch_stage(ws, s, ws.cand_a.p, 0, out);
+    if (ws.h_state->overflow) raise(kLimitExceeded, "coarse candidate budget exceeded");
+    return out;
+  }
+
+  // coarse-to-fine tracking (matcher.cpp:630-761)
+  Cand* cur = ws.cand_a.p;
+  Cand* nxt = ws.cand_b.p;
+  int slot = 0, step_no = 0;
+  for (size_t l = top; l > finest; --l) {
+    const bool snap = l == 1 && opt.subpixel;
+    if (!snap) {
+      const size_t t = l - 1;
+      TrackArgs ta;
+      ta.lev = lev[t];
+      ta.view = views[t];
+      ta.plist = d_plist[t];
+      ta.ranges = d_ranges[t];
+      ta.nplist = int(plan[t].plist.size());
+      ta.in = cur;
+      ta.out = ws.tmp.p;
+      ta.state = st;
+      ta.in_slot = slot;
+      ta.crop_row = double(crop_row);
+      ta.crop_col = double(crop_col);
+      ta.step = std::ldexp(1., int(t));
+      ta.offset = (ta.step - 1) * .5;
+      ta.angle_limit = hm.params.angle_step * double(l == top ? angle_stride : 1) * 1.01;
+      ta.absolute = hm.params.ignore_polarity;
+      check(launch_track(ta, kMaxCandidates, s), "track");
+    }
+    check(cudaMemsetAsync(ws.table.p, 0xff, sizeof(int) * kHashSlots, s), "memset");
+    DedupArgs da;
+    da.in = snap ? cur : ws.tmp.p;
+    da.out = nxt;
+    da.table = ws.table.p;
+    da.state = st;
+    da.in_slot = slot;
+    da.out_slot = slot + 1;
+    da.threshold = snap ? kMissing : opt.min_score * .4;
+    da.snap = snap;
+    da.height = Hd;
+    da.width = Wd;
+    check(launch_dedup(da, kMaxCandidates, s), "dedup");
+    std::swap(cur, nxt);
+    ++slot;
+    ++step_no;
+    if (stage == step_no) {
+      fetch_stage(ws, s, cur, slot, out);
+      return out;
+    }
+    if (snap) break;
+  }
+
+  // full-resolution score (matcher.cpp:813-822) and sort (824-827)
+  const double fscale = std::ldexp(1., int(finest)), fphase = (fscale - 1) * .5;
+  ImageView fine{lev[finest].v, lw[finest], lh[finest]};
+  {
+    ScoreArgs sa;
+    sa.img = fine;
+    sa.orig = orig;
+    sa.cand = cur;
+    sa.state = st;
+    sa.slot = slot;
+    sa.crop_row = double(crop_row);
+    sa.crop_col = double(crop_col);
+    sa.scale = fscale;
+    sa.phase = fphase;
+    sa.absolute = hm.params.ignore_polarity;
+    check(launch_score(sa, kMaxCandidates, s), "score");
+    SortArgs so;
+    so.in = cur;
+    so.out = ws.sorted.p;
+    so.state = st;
+    so.slot = slot;
+    check(launch_sort(so, s), "sort");
+  }
+  if (stage == 100) {
+    fetch_stage(ws, s, ws.sorted.p, -1, out);
+    return out;
+  }
+
+  // greedy selection with refinement (matcher.cpp:1063-1076)
+  check(cudaMemsetAsync(ws.refined_flag.p, 0, sizeof(int32_t) * kMaxCandidates, s), "memset");
+  const int batch_limit = int(std::min<int64_t>(64, opt.num_matches > 0 ? opt.num_matches + 4 : 32));
+  SelectArgs se;
+  se.sorted = ws.sorted.p;
+  se.refined = ws.refined.p;
+  se.refined_flag = ws.refined_flag.p;
+  se.batch = ws.batch.p;
+  se.accepted = ws.accepted.p;
+  se.state = st;
+  se.batch_limit = batch_limit;
+  se.num_matches = opt.num_matches;
+  se.max_overlap = opt.max_overlap;
+  se.tmpl_w = double(base.width);
+  se.tmpl_h = double(base.height);
+  se.tmpl_orow = base.orow;
+  se.tmpl_ocol = base.ocol;
+  RefineArgs ra;
+  ra.img = fine;
+  ra.orig = orig;
+  ra.lev0 = lev[0];
+  ra.view0 = views[0];
+  ra.plist0 = d_plist[0];
+  ra.ranges0 = d_ranges[0];
+  ra.nplist0 = int(plan[0].plist.size());
+  ra.sorted = ws.sorted.p;
+  ra.refined = ws.refined.p;
+  ra.refined_flag = ws.refined_flag.p;
+  ra.batch = ws.batch.p;
+  ra.state = st;
+  ra.crop_row = double(crop_row);
+  ra.crop_col = double(crop_col);
+  ra.scale = fscale;
+  ra.phase = fphase;
+  ra.angle_start = opt.angle_start;
+  ra.angle_end = opt.angle_start + opt.angle_extent;
+  ra.angle_step = hm.params.angle_step;
+  ra.min_score = opt.min_score;
+  ra.rotate = opt.angle_extent > 0;
+  ra.subpixel = opt.subpixel;
+  ra.absolute = hm.params.ignore_polarity;
+  ra.top = int(top);
+  ra.finest = int(finest);
+  ra.height = Hd;
+  ra.width = Wd;
+  check(launch_select(se, s), "select");
+  for (int round = 0; round < 100000; ++round) {
+    check(launch_refine(ra, batch_limit, s), "refine");
+    check(launch_select(se, s), "select");
+    check(cudaMemcpyAsync(ws.h_state, st, sizeof(QueryState), cudaMemcpyDeviceToHost, s), "state");
+    check(cudaStreamSynchronize(s), "find");
+    if (ws.h_state->done || !ws.h_state->need) break;
+  }
+  const QueryState hs = *ws.h_state;
+  if (hs.overflow) raise(kLimitExceeded, "coarse candidate budget exceeded");
+  if (hs.error) raise(hs.error, "pyramid sums exceed the exact float range");
+  std::vector<Cand> acc(size_t(hs.accepted));
+  if (hs.accepted > 0) {
+    check(cudaMemcpyAsync(acc.data(), ws.accepted.p, acc.size() * sizeof(Cand), cudaMemcpyDeviceToHost, s), "result");
+    check(cudaStreamSynchronize(s), "result");
+  }
+  for (const Cand& c : acc) out.matches.push_back({c.row, c.col, c.angle, c.score});
+  if (stage == -1) out.stage = out.matches;
+  return out;
+}
+
+template <class Fn> int32_t guarded(Fn&& fn) {
+  try {
+    fn();
+    g_last_error.clear();
+    return kOk;
+  } catch (const Error& e) {
+    g_last_error = e.what();
+    return e.status;
+  } catch (const std::bad_alloc&) {
+    g_last_error = "out of memory";
+    return kOutOfMemory;
+  } catch (const std::exception& e) {
+    g_last_error = e.what();
+    return kInternal;
+  } catch (...) {
+    g_last_error = "unknown failure";
+    return kInternal;
+  }
+}
+
+FindParams make_params(double angle_start, double angle_extent, double min_score, int64_t num_matches,
+                       double max_overlap, int32_t subpixel, int32_t highest, int32_t lowest) {
+  FindParams p;
+  p.angle_start = angle_start;
+  p.angle_extent = angle_extent;
+  p.min_score = min_score;
+  p.num_matches = num_matches;
+  p.max_overlap = max_overlap;
+  p.subpixel = subpixel != 0;
+  p.highest = highest;
+  p.lowest = std::max<int32_t>(1, lowest);
+  return p;
+}
+
+}  // namespace
+}  // namespace mvg
+
+using namespace mvg;
+
+extern "C" {
+
+int32_t mvg_create_ncc_model(const void* pixels, int32_t pixel_type, int64_t width, int64_t height, int64_t row_stride,
+                             const uint8_t* domain, int32_t num_levels, double angle_start, double angle_extent,
+                             double angle_step, int32_t metric, mvg_ncc_model* model_id) {
+  return guarded([&] {
+    if (!model_id) raise(kInvalidArgument, "ModelID must not be null");
+    *model_id = nullptr;
+    if (metric != MVG_METRIC_USE_POLARITY && metric != MVG_METRIC_IGNORE_GLOBAL_POLARITY)
+      raise(kInvalidArgument, "unsupported NCC metric");
+    if (num_levels > 16) raise(kInvalidArgument, "levels must be 0..16 or auto");
+    if (angle_step > 3.14159265358979323846 / 16) raise(kInvalidArgument, "angle step must be in [0,pi/16] or auto");
+    CreateParams p;
+    p.levels = std::max(0, num_levels);
+    p.ignore_polarity = metric == MVG_METRIC_IGNORE_GLOBAL_POLARITY;
+    p.angle_start = angle_start;
+    p.angle_extent = angle_extent;
+    p.angle_step = angle_step > 0 ? angle_step : 0.;
+    auto m = std::make_unique<mvg_ncc_model_s>();
+    m->host = create_model(pixels, pixel_type, width, height, row_stride, domain, p);
+    check(cudaGetDevice(&m->device), "cudaGetDevice");
+    for (const ModelLevel& L : m->host.levels) {
+      auto d = std::make_unique<DevLevel>();
+      for (const Raster& r : L.patches) d->append(r);
+      d->model_patches = d->desc.size();
+      d->upload();
+      m->levels.push_back(std::move(d));
+    }
+    m->original.set(m->host.original, m->host.levels.front().orow, m->host.levels.front().ocol);
+    *model_id = m.release();
+  });
+}
+
+int32_t mvg_get_ncc_model_params(mvg_ncc_model model_id, int32_t* num_levels, double* angle_start,
+                                 double* angle_extent, double* angle_step, int32_t* metric) {
+  return guarded([&] {
+    if (!model_id) raise(kInvalidArgument, "control handle is not an NCC model");
+    const HostModel& h = model_id->host;
+    if (num_levels) *num_levels = int32_t(h.levels.size());
+    if (angle_start) *angle_start = h.params.angle_start;
+    if (angle_extent) *angle_extent = h.params.angle_extent;
+    if (angle_step) *angle_step = h.params.angle_extent == 0 ? 0. : h.params.angle_step;
+    if (metric) *metric = h.params.ignore_polarity ? MVG_METRIC_IGNORE_GLOBAL_POLARITY : MVG_METRIC_USE_POLARITY;
+  });
+}
+
+int32_t mvg_clear_ncc_model(mvg_ncc_model model_id) {
+  return guarded([&] { delete model_id; });
+}
+
+int32_t mvg_find_ncc_model(const void* pixels, int32_t pixel_type, int64_t width, int64_t height, int64_t row_stride,
+                           int32_t location, mvg_ncc_model model_id, double angle_start, double angle_extent,
+                           double min_score, int64_t num_matches, double max_overlap, int32_t subpixel,
+                           int32_t highest_level, int32_t lowest_level, double* row, double* column, double* angle,
+                           double* score, int64_t capacity, int64_t* count, void* stream) {
+  return guarded([&] {
+    if (!model_id) raise(kInvalidArgument, "control handle is not an NCC model");
+    if (!count) raise(kInvalidArgument, "count must not be null");
+    *count = 0;
+    const auto p = make_params(angle_start, angle_extent, min_score, num_matches, max_overlap, subpixel,
+                               highest_level, lowest_level);
+    const FindOutput r = run_find(*model_id, pixels, pixel_type, width, height, row_stride, location, p,
+                                  static_cast<cudaStream_t>(stream), -2);
+    *count = int64_t(r.matches.size());
+    for (size_t i = 0; i < r.matches.size() && int64_t(i) < capacity; ++i) {
+      // edge-centred pose convention (src/c_api/ncc_matching_api.cpp:171-176)
+      const Match& mt = r.matches[i];
+      const double c = std::cos(mt.angle), s = std::sin(mt.angle);
+      if (row) row[i] = mt.row + .5 * (1 - c + s);
+      if (column) column[i] = mt.col + .5 * (1 - c - s);
+      if (angle) angle[i] = mt.angle;
+      if (score) score[i] = mt.score;
+    }
+  });
+}
+
+int32_t mvg_find_ncc_model_stage(const void* pixels, int32_t pixel_type, int64_t width, int64_t height,
+                                 int64_t row_stride, int32_t location, mvg_ncc_model model_id, double angle_start,
+                                 double angle_extent, double min_score, int64_t num_matches, double max_overlap,
+                                 int32_t subpixel, int32_t highest_level, int32_t lowest_level, int32_t stage,
+                                 double* out, int64_t capacity, int64_t* count) {
+  return guarded([&] {
+    if (!model_id) raise(kInvalidArgument, "control handle is not an NCC model");
+    if (!count) raise(kInvalidArgument, "count must not be null");
+    *count = 0;
+    const auto p = make_params(angle_start, angle_extent, min_score, num_matches, max_overlap, subpixel,
+                               highest_level, lowest_level);
+    const FindOutput r = run_find(*model_id, pixels, pixel_type, width, height, row_stride, location, p, nullptr,
+                                  stage);
+    *count = int64_t(r.stage.size());
+    for (size_t i = 0; i < r.stage.size() && int64_t(i) < capacity; ++i) {
+      out[4 * i + 0] = r.stage[i].row;
+      out[4 * i + 1] = r.stage[i].col;
+      out[4 * i + 2] = r.stage[i].angle;
+      out[4 * i + 3] = r.stage[i].score;
+    }
+  });
+}
+
+int32_t mvg_ncc_pyramid_level(const void* pixels, int32_t pixel_type, int64_t width, int64_t height,
+                              int64_t row_stride, mvg_ncc_model model_id, int32_t highest_level, int32_t level,
+                              float* out, int64_t capacity, double* geom) {
+  return guarded([&] {
+    if (!model_id) raise(kInvalidArgument, "control handle is not an NCC model");
+    if (pixel_type != 0 && pixel_type != 1) raise(kTypeMismatch, "one byte or uint2 channel required");
+    const HostModel& hm = model_id->host;
+    const size_t level_count = highest_level ? std::min(hm.levels.size(), size_t(highest_level)) : hm.levels.size();
+    if (level < 0 || size_t(level) >= level_count) raise(kInvalidArgument, "level out of range");
+    const ModelLevel& base = hm.levels.front();
+    const double radius = std::hypot(std::max(base.orow, double(base.height - 1) - base.orow),
+                                     std::max(base.ocol, double(base.width - 1) - base.ocol));
+    const int64_t lattice = int64_t(size_t{1} << (level_count - 1));
+    const int64_t halo = int64_t(std::ceil(radius)) + 4 * lattice;
+    const int64_t crop_bottom = std::min<int64_t>(height, ((height - 1 + halo) / lattice + 1) * lattice);
+    const int64_t crop_right = std::min<int64_t>(width, ((width - 1 + halo) / lattice + 1) * lattice);
+    Workspace& ws = workspace();
+    cudaStream_t s = ws.own_stream;
+    const int64_t bpp = pixel_type == 1 ? 2 : 1;
+    const size_t bytes = size_t(row_stride) * size_t(height - 1) + size_t(width * bpp);
+    ws.image.reserve(bytes);
+    check(cudaMemcpyAsync(ws.image.p, pixels, bytes, cudaMemcpyHostToDevice, s), "image upload");
+    check(cudaMemsetAsync(ws.state.p, 0, sizeof(QueryState), s), "memset");
+    LevelImage lev[kMaxLevels];
+    int w = int(crop_right), h = int(crop_bottom);
+    for (int l = 0; l <= level; ++l) {
+      if (l) {
+        w = std::max(1, w / 2);
+        h = std::max(1, h / 2);
+      }
+      ws.lev_v[l].reserve(size_t(w) * size_t(h));
+      lev[l].v = ws.lev_v[l].p;
+      lev[l].w = w;
+      lev[l].h = h;
+      if (l == 0)
+        check(launch_pyramid0(ws.image.p, pixel_type, row_stride / bpp, 0, 0, lev[0], &ws.state.p->error, s), "pyramid0");
+      else
+        check(launch_pyramid(lev[l - 1], lev[l], &ws.state.p->error, s), "pyramid");
+    }
+    if (int64_t(w) * h > capacity) raise(kInvalidArgument, "output capacity too small");
+    check(cudaMemcpyAsync(out, lev[level].v, size_t(w) * size_t(h) * sizeof(float), cudaMemcpyDeviceToHost, s), "copy");
+    check(cudaStreamSynchronize(s), "sync");
+    const uint8_t* px = static_cast<const uint8_t*>(pixels);
+    geom[0] = w;
+    geom[1] = h;
+    geom[2] = 0;
+    geom[3] = 0;
+    geom[4] = pixel_type == 1 ? double(*reinterpret_cast<const uint16_t*>(px)) : double(px[0]);
+  });
+}
+
+const char* mvg_last_error(void) { return g_last_error.c_str(); }
+
+int32_t mvg_host_alloc(size_t bytes, void** ptr) {
+  return guarded([&] { check(cudaMallocHost(ptr, bytes), "cudaMallocHost"); });
+}
+int32_t mvg_host_free(void* ptr) {
+  return guarded([&] { check(cudaFreeHost(ptr), "cudaFreeHost"); });
+}
+int32_t mvg_device_alloc(size_t bytes, void** ptr) {
+  return guarded([&] { check(cudaMalloc(ptr, bytes), "cudaMalloc"); });
+}
+int32_t mvg_device_free(void* ptr) {
+  return guarded([&] { check(cudaFree(ptr), "cudaFree"); });
+}
+int32_t mvg_copy_to_device(void* dst, const void* src, size_t bytes) {
+  return guarded([&] { check(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice), "cudaMemcpy"); });
+}
+
+}  // extern "C"

@@ -1,0 +1,1215 @@
+// CUDA kernels of the GB300 NCC find path (sm_103a).
+//
+// Numerics.  Every pyramid value is an integer sum of 4^k input pixels, held
+// exactly in float.  Window moments (sum S, sum S^2) come from int64 row
+// prefix sums, so the variance numerator n*sum(S^2) - (sum S)^2 is exact and
+// the "variance <= 0 -> no score" rule of the reference is decided exactly.
+// The template dot product sum(w * (S - S_first)) runs in FP32 on the CUDA
+// cores; the full-resolution score and the Gauss-Newton moments accumulate in
+// FP32 per thread and combine in FP64.  Poses are FP64 with the reference's
+// expressions (no contraction: __dadd_rn/__dmul_rn).
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+
+#include "ncc_kernels.h"
+
+namespace mvg {
+namespace {
+
+__device__ __forceinline__ int off_row(int32_t o) { return o >> 16; }
+__device__ __forceinline__ int off_col(int32_t o) { return int(int16_t(o & 0xffff)); }
+__device__ __forceinline__ int run_row(int32_t o) { return o >> 16; }
+__device__ __forceinline__ int run_begin(int32_t o) { return int(int16_t(o & 0xffff)); }
+
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+
+// pose coordinate of integer position r on a level: crop + step*(r + o) + off
+// (src/ncc_matching/matcher.cpp:558,592,687)
+__device__ __forceinline__ double lattice_pose(double crop, double step, int r, double o, double off) {
+  return dadd(dadd(crop, dmul(step, dadd(double(r), o))), off);
+}
+
+// Score of one window from the FP32 template dot and exact integer moments.
+// D = sum w (S - S0) relates to the reference's sum w q by a 4^k factor that
+// cancels against the variance, giving score = D / sqrt(V / n) with
+// V = n sum S^2 - (sum S)^2 (src/ncc_matching/matcher.cpp:97-105).
+__device__ __forceinline__ float window_score(float dot, long long s1, long long s2, int n, int absolute) {
+  const __int128 v = (__int128)n * s2 - (__int128)s1 * s1;
+  if (v <= 0) return -INFINITY;
+  const float vn = float((double)(long long)v) / float(n);
+  float s = dot * rsqrtf(vn);
+  s = fminf(1.f, fmaxf(-1.f, s));
+  return absolute ? fabsf(s) : s;
+}
+
+__device__ __forceinline__ void window_moments(const longlong2* __restrict__ P, int pitch, int r, int c,
+                                               const int32_t* __restrict__ runs, const int32_t* __restrict__ ends,
+                                               int nruns, long long& s1, long long& s2) {
+  s1 = 0;
+  s2 = 0;
+  for (int j = 0; j < nruns; ++j) {
+    const int32_t rb = __ldg(runs + j);
+    const int e = __ldg(ends + j);
+    const size_t base = size_t(r + run_row(rb)) * pitch + c;
+    const longlong2 hi = P[base + e + 1];
+    const longlong2 lo = P[base + run_begin(rb)];
+    s1 += hi.x - lo.x;
+    s2 += hi.y - lo.y;
+  }
+}
+
+// ------------------------------------------------------------------ pyramid
+template <class T>
+__global__ void pyramid0_kernel(const T* __restrict__ src, int64_t pitch, int crop_row, int crop_col, LevelImage dst) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.y * blockDim.y + threadIdx.y;
+  if (c >= dst.w || r >= dst.h) return;
+  dst.v[size_t(r) * dst.w + c] = float(src[(int64_t(crop_row) + r) * pitch + crop_col + c]);
+}
+
+// level k+1 from level k: 2x2 sums with the reference's clamped neighbours
+// (src/ncc_matching/matcher.cpp:436-453)
+__global__ void pyramid_kernel(LevelImage src, LevelImage dst, int32_t* error_flag) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.y * blockDim.y + threadIdx.y;
+  if (c >= dst.w || r >= dst.h) return;
+  const int r0 = 2 * r, r1 = min(r0 + 1, src.h - 1), c0 = 2 * c, c1 = min(c0 + 1, src.w - 1);
+  const float a = src.v[size_t(r0) * src.w + c0], b = src.v[size_t(r0) * src.w + c1];
+  const float d = src.v[size_t(r1) * src.w + c0], e = src.v[size_t(r1) * src.w + c1];
+  const float s = ((a + b) + d) + e;
+  if (s >= 16777216.f) atomicExch(error_flag, int32_t(kUnsupported));
+  dst.v[size_t(r) * dst.w + c] = s;
+}
+
+// row prefix sums {sum S, sum S^2}, one warp per row
+__global__ void prefix_kernel(LevelImage lev) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= lev.h) return;
+  const float* row = lev.v + size_t(warp) * lev.w;
+  longlong2* out = lev.prefix + size_t(warp) * (lev.w + 1);
+  if (lane == 0) out[0] = make_longlong2(0, 0);
+  long long c1 = 0, c2 = 0;
+  for (int base = 0; base < lev.w; base += 32) {
+    const int c = base + lane;
+    const long long s = c < lev.w ? (long long)row[c] : 0;
+    long long a = s, b = s * s;
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long ua = __shfl_up_sync(0xffffffffu, a, o);
+      const long long ub = __shfl_up_sync(0xffffffffu, b, o);
+      if (lane >= o) {
+        a += ua;
+        b += ub;
+      }
+    }
+    if (c < lev.w) out[c + 1] = make_longlong2(c1 + a, c2 + b);
+    c1 += __shfl_sync(0xffffffffu, a, 31);
+    c2 += __shfl_sync(0xffffffffu, b, 31);
+  }
+}
+
+// ---------------------------------------------------------------- coarse scan
+// Dense score planes of the top level for the kept coarse patches
+// (src/ncc_matching/matcher.cpp:542-579).  Block = 32x8 positions of one
+// patch; the image tile with the patch's reach is staged in shared memory.
+constexpr int kTileW = 32, kTileH = 8;
+
+__global__ void __launch_bounds__(256) coarse_kernel(CoarseArgs a) {
+  extern __shared__ float tile[];
+  const int p = blockIdx.z;
+  const PatchDesc pd = a.view.patches[a.plist[p]];
+  const PosRange rg = a.ranges[p];
+  const int R0 = blockIdx.y * kTileH, C0 = blockIdx.x * kTileW;
+  const int TW = kTileW + pd.cmax - pd.cmin, TH = kTileH + pd.rmax - pd.rmin;
+  const int tid = threadIdx.y * kTileW + threadIdx.x;
+  const int w = a.lev.w, h = a.lev.h;
+  // skip tiles with no valid position (still write -inf)
+  const bool any = R0 < rg.r1 && R0 + kTileH > rg.r0 && C0 < rg.c1 && C0 + kTileW > rg.c0;
+  if (any) {
+    for (int i = tid; i < TW * TH; i += 256) {
+      const int gr = R0 + pd.rmin + i / TW, gc = C0 + pd.cmin + i % TW;
+      tile[i] = (gr >= 0 && gc >= 0 && gr < h && gc < w) ? a.lev.v[size_t(gr) * w + gc] : 0.f;
+    }
+  }
+  __syncthreads();
+  const int r = R0 + threadIdx.y, c = C0 + threadIdx.x;
+  if (r >= h || c >= w) return;
+  float score = -INFINITY;
+  if (any && r >= rg.r0 && r < rg.r1 && c >= rg.c0 && c < rg.c1) {
+    const int32_t* offs = a.view.offs + pd.sample_off;
+    const float* wt = a.view.w + pd.sample_off;
+    const float* base = tile + (threadIdx.y - pd.rmin) * TW + (threadIdx.x - pd.cmin);
+    const int32_t o0 = __ldg(offs);
+    const float s0 = base[off_row(o0) * TW + off_col(o0)];
+    float acc0 = 0.f, acc1 = 0.f;
+    int i = 0;
+    for (; i + 1 < pd.n; i += 2) {
+      const int32_t oa = __ldg(offs + i), ob = __ldg(offs + i + 1);
+      acc0 = fmaf(__ldg(wt + i), base[off_row(oa) * TW + off_col(oa)] - s0, acc0);
+      acc1 = fmaf(__ldg(wt + i + 1), base[off_row(ob) * TW + off_col(ob)] - s0, acc1);
+    }
+    if (i < pd.n) {
+      const int32_t oa = __ldg(offs + i);
+      acc0 = fmaf(__ldg(wt + i), base[off_row(oa) * TW + off_col(oa)] - s0, acc0);
+    }
+    long long s1, s2;
+    window_moments(a.lev.prefix, w + 1, r, c, a.view.runs + pd.run_off, a.view.runs_end + pd.run_off, pd.nruns, s1, s2);
+    score = window_score(acc0 + acc1, s1, s2, pd.n, a.absolute);
+  }
+  a.planes[(size_t(p) * h + r) * w + c] = score;
+}
+
+// 3x3 local maxima >= 0.4*MinScore with the reference's tie rule, compacted
+// into the candidate list (src/ncc_matching/matcher.cpp:581-593).
+__global__ void nms_kernel(NmsArgs a) {
+  const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t plane = int64_t(a.w) * a.h;
+  if (idx >= plane * a.nplist) return;
+  const int p = int(idx / plane);
+  const int rem = int(idx % plane);
+  const int r = rem / a.w, c = rem % a.w;
+  const float* s = a.planes + size_t(p) * plane;
+  const float v = s[rem];
+  if (!(double(v) >= a.threshold) || !isfinite(v)) return;
+  for (int dr = -1; dr <= 1; ++dr)
+    for (int dc = -1; dc <= 1; ++dc) {
+      const int rr = r + dr, cc = c + dc;
+      if (rr < 0 || cc < 0 || rr >= a.h || cc >= a.w || (!dr && !dc)) continue;
+      const float o = s[rr * a.w + cc];
+      if (o > v || (o == v && (dr < 0 || (!dr && dc < 0)))) return;
+    }
+  const int k = atomicAdd(&a.state->count[0], 1);
+  if (k >= a.max_candidates) {
+    atomicExch(&a.state->overflow, 1);
+    return;
+  }
+  const PatchDesc pd = a.view.patches[a.plist[p]];
+  Cand out;
+  out.row = lattice_pose(a.crop_row, a.scale, r, pd.orow, a.phase);
+  out.col = lattice_pose(a.crop_col, a.scale, c, pd.ocol, a.phase);
+  out.angle = pd.angle;
+  out.score = double(v);
+  a.out[k] = out;
+}
+
+// ------------------------------------------------------------------ tracking
+// One block per candidate: every query patch of the target level within the
+// angle window, 5x5 positions each; the first strict maximum in (patch order,
+// dr, dc) wins (src/ncc_matching/matcher.cpp:670-757).
+__device__ __forceinline__ bool better(float s, int o, float bs, int bo) {
+  return s > bs || (s == bs && o < bo);
+}
+
+__global__ void __launch_bounds__(256) track_kernel(TrackArgs a) {
+  const int i = blockIdx.x;
+  if (i >= a.state->count[a.in_slot]) return;
+  __shared__ int sel[256];
+  __shared__ int nsel;
+  __shared__ float wscore[8];
+  __shared__ int worder[8];
+  const Cand cd = a.in[i];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) nsel = 0;
+  __syncthreads();
+  // ordered selection of the patches inside the angle window (warp 0)
+  if (warp == 0) {
+    int count = 0;
+    for (int base = 0; base < a.nplist; base += 32) {
+      const int j = base + lane;
+      bool hit = false;
+      if (j < a.nplist) {
+        const double ang = a.view.patches[a.plist[j]].angle;
+        hit = !(fabs(dsub(ang, cd.angle)) > a.angle_limit);
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, hit);
+      if (hit) {
+        const int pos = count + __popc(m & ((1u << lane) - 1));
+        if (pos < 256) sel[pos] = j;
+      }
+      count += __popc(m);
+    }
+    if (lane == 0) nsel = min(count, 256);
+  }
+  __syncthreads();
+  float best = -INFINITY;
+  int border = INT32_MAX;
+  const int dr = lane / 5 - 2, dc = lane % 5 - 2;
+  for (int k = warp; k < nsel; k += 8) {
+    const int j = sel[k];
+    const PatchDesc pd = a.view.patches[a.plist[j]];
+    const PosRange rg = a.ranges[j];
+    const int row = int(round(dsub(dsub(dsub(cd.row, a.crop_row), a.offset) / a.step, pd.orow)));
+    const int col = int(round(dsub(dsub(dsub(cd.col, a.crop_col), a.offset) / a.step, pd.ocol)));
+    const int r = row + dr, c = col + dc;
+    if (lane < 25 && r >= rg.r0 && r < rg.r1 && c >= rg.c0 && c < rg.c1) {
+      const int32_t* offs = a.view.offs + pd.sample_off;
+      const float* wt = a.view.w + pd.sample_off;
+      const int pitch = a.lev.w;
+      const float* base = a.lev.v + size_t(r) * pitch + c;
+      const int32_t o0 = __ldg(offs);
+      const float s0 = __ldg(base + off_row(o0) * pitch + off_col(o0));
+      float acc0 = 0.f, acc1 = 0.f;
+      int s = 0;
+      for (; s + 1 < pd.n; s += 2) {
+        const int32_t oa = __ldg(offs + s), ob = __ldg(offs + s + 1);
+        acc0 = fmaf(__ldg(wt + s), __ldg(base + off_row(oa) * pitch + off_col(oa)) - s0, acc0);
+        acc1 = fmaf(__ldg(wt + s + 1), __ldg(base + off_row(ob) * pitch + off_col(ob)) - s0, acc1);
+      }
+      if (s < pd.n) {
+        const int32_t oa = __ldg(offs + s);
+        acc0 = fmaf(__ldg(wt + s), __ldg(base + off_row(oa) * pitch + off_col(oa)) - s0, acc0);
+      }
+      long long s1, s2;
+      window_moments(a.lev.prefix, pitch + 1, r, c, a.view.runs + pd.run_off, a.view.runs_end + pd.run_off,
+                     pd.nruns, s1, s2);
+      const float sc = window_score(acc0 + acc1, s1, s2, pd.n, a.absolute);
+      const int order = k * 25 + lane;
+      if (better(sc, order, best, border)) {
+        best = sc;
+        border = order;
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const float ob = __shfl_down_sync(0xffffffffu, best, o);
+    const int oo = __shfl_down_sync(0xffffffffu, border, o);
+    if (better(ob, oo, best, border)) {
+      best = ob;
+      border = oo;
+    }
+  }
+  if (lane == 0) {
+    wscore[warp] = best;
+    worder[warp] = border;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float bs = -INFINITY;
+    int bo = INT32_MAX;
+    for (int w = 0; w < 8; ++w)
+      if (better(wscore[w], worder[w], bs, bo)) {
+        bs = wscore[w];
+        bo = worder[w];
+      }
+    Cand out = cd;
+    out.score = -INFINITY;
+    if (bo != INT32_MAX && bs > -INFINITY) {
+      const int k = bo / 25, l = bo % 25;
+      const PatchDesc pd = a.view.patches[a.plist[sel[k]]];
+      const int row = int(round(dsub(dsub(dsub(cd.row, a.crop_row), a.offset) / a.step, pd.orow)));
+      const int col = int(round(dsub(dsub(dsub(cd.col, a.crop_col), a.offset) / a.step, pd.ocol)));
+      out.row = lattice_pose(a.crop_row, a.step, row + l / 5 - 2, pd.orow, a.offset);
+      out.col = lattice_pose(a.crop_col, a.step, col + l % 5 - 2, pd.ocol, a.offset);
+      out.angle = pd.angle;
+      out.score = double(bs);
+    }
+    a.out[i] = out;
+  }
+}
+
+// ------------------------------------------------------------ merge_identical
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
+  x ^= x >> 33;
+  x *= 0xff51afd7ed558ccdULL;
+  x ^= x >> 33;
+  x *= 0xc4ceb9fe1a85ec53ULL;
+  x ^= x >> 33;
+  return x;
+}
+
+// Snap poses outside the image to the nearest in-image pixel within 4 rows
+// and columns (full-image domain; src/ncc_matching/matcher.cpp:633-643).
+__device__ void snap_pose(Cand& p, double height, double width) {
+  const double rr = floor(p.row + .5), cc = floor(p.col + .5);
+  if (rr >= 0 && cc >= 0 && rr < height && cc < width) return;
+  double best = INFINITY, nr = p.row, nc = p.col;
+  const double first = fmax(0., ceil(p.row - 4));
+  for (double r = first; r <= p.row + 4 && r < height; r += 1) {
+    const double c = fmin(fmax(round(p.col), 0.), width - 1);
+    if (fabs(c - p.col) > 4) continue;
+    const double dist = hypot(r - p.row, c - p.col);
+    if (dist < best) {
+      best = dist;
+      nr = r;
+      nc = c;
+    }
+  }
+  if (isfinite(best)) {
+    p.row = nr;
+    p.col = nc;
+  } else {
+    p.score = -INFINITY;
+  }
+}
+
+__global__ void snap_kernel(Cand* c, const QueryState* state, int slot, double height, double width) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= state->count[slot]) return;
+  Cand p = c[i];
+  snap_pose(p, height, width);
+  c[i] = p;
+}
+
+// merge_identical + threshold (src/ncc_matching/matcher.cpp:241-248,758-760):
+// keep one candidate per exact (row, column, angle), drop non-finite scores
+// and scores below the threshold; order is irrelevant downstream.
+__global__ void dedup_kernel(DedupArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.state->count[a.in_slot]) return;
+  const Cand p = a.in[i];
+  if (!isfinite(p.score) || p.score < a.threshold) return;
+  const unsigned long long kr = __double_as_longlong(p.row), kc = __double_as_longlong(p.col),
+                           ka = __double_as_longlong(p.angle);
+  unsigned slot = unsigned(mix64(kr ^ mix64(kc ^ mix64(ka)))) & (kHashSlots - 1);
+  for (int probe = 0; probe < kHashSlots; ++probe) {
+    const int prev = atomicCAS(a.table + slot, -1, i);
+    if (prev == -1) {
+      const int k = atomicAdd(&a.state->count[a.out_slot], 1);
+      a.out[k] = p;
+      return;
+    }
+    const Cand q = a.in[prev];
+    if (q.row == p.row && q.col == p.col && q.angle == p.angle) return;
+    slot = (slot + 1) & (kHashSlots - 1);
+  }
+}
+
+// -------------------------------------------------- full-resolution scoring
+// Cross-thread sums use FP32 (hi, lo) pairs (Knuth two-sum): per-thread FP32
+// partials combine with ~2^-44 relative error without FP64 instructions (the
+// FP64 pipe of sm_103 is narrow).  Thread 0 finishes each pass in FP64 and
+// broadcasts through shared memory.
+struct F2 {
+  float hi, lo;
+};
+__device__ __forceinline__ F2 f2_add(F2 x, F2 y) {
+  const float s = x.hi + y.hi;
+  const float bb = s - x.hi;
+  const float e = ((x.hi - (s - bb)) + (y.hi - bb)) + (x.lo + y.lo);
+  const float h = s + e;
+  return F2{h, e - (h - s)};
+}
+
+// Totals of K per-thread values; valid on thread 0 only.  scratch: K*64 floats.
+template <int K>
+__device__ void block_total(const float (&v)[K], double (&out)[K], float* scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  F2 x[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) x[k] = F2{v[k], 0.f};
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+    for (int o = 16; o > 0; o >>= 1) {
+      const F2 y{__shfl_down_sync(0xffffffffu, x[k].hi, o), __shfl_down_sync(0xffffffffu, x[k].lo, o)};
+      x[k] = f2_add(x[k], y);
+    }
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      scratch[(k * 32 + warp) * 2] = x[k].hi;
+      scratch[(k * 32 + warp) * 2 + 1] = x[k].lo;
+    }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      F2 y = lane < nw ? F2{scratch[(k * 32 + lane) * 2], scratch[(k * 32 + lane) * 2 + 1]} : F2{0.f, 0.f};
+      for (int o = 16; o > 0; o >>= 1) {
+        const F2 z{__shfl_down_sync(0xffffffffu, y.hi, o), __shfl_down_sync(0xffffffffu, y.lo, o)};
+        y = f2_add(y, z);
+      }
+      out[k] = double(y.hi) + double(y.lo);
+    }
+  }
+  __syncthreads();
+}
+
+// Pose in the frame of an integer anchor: FP64 only here (thread 0).
+struct LocalPose {
+  int R0, C0;        // integer anchor
+  float fr, fc;      // fractional part of the pose relative to the anchor
+  float ca, sa;
+};
+
+__device__ __forceinline__ LocalPose make_local(double row, double col, double angle) {
+  LocalPose l;
+  const double fr = floor(row), fc = floor(col);
+  l.R0 = int(fr);
+  l.C0 = int(fc);
+  l.fr = float(row - fr);
+  l.fc = float(col - fc);
+  double s, c;
+  sincos(angle, &s, &c);
+  l.ca = float(c);
+  l.sa = float(s);
+  return l;
+}
+
+// Shared state of a block working on one pose at a time.
+struct PoseShared {
+  LocalPose lp;
+  double score;       // result of the last continuous pass
+  int ok;             // result flag of the last Gauss-Newton pass
+  double gscore;      // score seen by the last Gauss-Newton pass (-inf if none)
+  double delta[3];
+  float scratch[19 * 64];
+};
+
+__device__ __forceinline__ float bilinear_at(const ImageView& img, int r, int c, float fy, float fx, int r1, int c1) {
+  const float* v = img.v;
+  return (1 - fy) * ((1 - fx) * __ldg(v + size_t(r) * img.w + c) + fx * __ldg(v + size_t(r) * img.w + c1)) +
+         fy * ((1 - fx) * __ldg(v + size_t(r1) * img.w + c) + fx * __ldg(v + size_t(r1) * img.w + c1));
+}
+
+// continuous() of src/ncc_matching/matcher.cpp:144-156 at a level-local pose;
+// every thread of the block calls it; sh.score holds the result afterwards.
+__device__ void continuous_pass(const ImageView& img, const OriginalView& orig, double row, double col, double angle,
+                                int absolute, PoseShared& sh) {
+  if (threadIdx.x == 0) sh.lp = make_local(row, col, angle);
+  __syncthreads();
+  const LocalPose L = sh.lp;
+  const float hmax = float(img.h - 1 - L.R0), wmax = float(img.w - 1 - L.C0);
+  const float hmin = float(-L.R0), wmin = float(-L.C0);
+  float offset = 0.f;
+  {
+    const float dr = orig.dr[0], dc = orig.dc[0];
+    const float y = L.fr + (L.ca * dr - L.sa * dc), x = L.fc + (L.sa * dr + L.ca * dc);
+    if (y >= hmin && x >= wmin && y <= hmax && x <= wmax) {
+      const float fy0 = floorf(y), fx0 = floorf(x);
+      const int r = L.R0 + int(fy0), c = L.C0 + int(fx0);
+      offset = bilinear_at(img, r, c, y - fy0, x - fx0, min(r + 1, img.h - 1), min(c + 1, img.w - 1));
+    }
+  }
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};  // sum q, sum q^2, sum w q, out-of-image flag
+  for (int s = threadIdx.x; s < orig.n; s += blockDim.x) {
+    const float dr = __ldg(orig.dr + s), dc = __ldg(orig.dc + s), w = __ldg(orig.w + s);
+    const float y = L.fr + (L.ca * dr - L.sa * dc), x = L.fc + (L.sa * dr + L.ca * dc);
+    if (!(y >= hmin && x >= wmin && y <= hmax && x <= wmax)) {
+      acc[3] = 1.f;
+      continue;
+    }
+    const float fy0 = floorf(y), fx0 = floorf(x);
+    const int r = L.R0 + int(fy0), c = L.C0 + int(fx0);
+    const float q = bilinear_at(img, r, c, y - fy0, x - fx0, min(r + 1, img.h - 1), min(c + 1, img.w - 1)) - offset;
+    acc[0] += q;
+    acc[1] = fmaf(q, q, acc[1]);
+    acc[2] = fmaf(w, q, acc[2]);
+  }
+  double t[4];
+  block_total<4>(acc, t, sh.scratch);
+  if (threadIdx.x == 0) {
+    double sc = -INFINITY;
+    if (!(t[3] > 0)) {
+      const double var = t[1] - t[0] * t[0] / double(orig.n);
+      if (var > 0) {
+        sc = fmin(1., fmax(-1., t[2] / sqrt(var)));
+        if (absolute) sc = fabs(sc);
+      }
+    }
+    sh.score = sc;
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(128) score_kernel(ScoreArgs a) {
+  __shared__ PoseShared sh;
+  const int i = blockIdx.x;
+  if (i >= a.state->count[a.slot]) return;
+  const Cand c = a.cand[i];
+  if (!isfinite(c.score)) return;
+  const double row = (c.row - a.crop_row - a.phase) / a.scale;
+  const double col = (c.col - a.crop_col - a.phase) / a.scale;
+  continuous_pass(a.img, a.orig, row, col, c.angle, a.absolute, sh);
+  if (threadIdx.x == 0) a.cand[i].score = sh.score;
+}
+
+// --------------------------------------------------------------------- sort
+// Candidates by score (descending), then row, column, angle ascending
+// (src/ncc_matching/matcher.cpp:824-827).  One block, bitonic on indices.
+__device__ __forceinline__ bool before(const Cand* c, const double* key, const int* idx, int a, int b) {
+  const int ia = idx[a], ib = idx[b];
+  if (ia < 0) return false;
+  if (ib < 0) return true;
+  const double ka = key[a], kb = key[b];
+  if (ka != kb) return ka > kb;
+  const Cand x = c[ia], y = c[ib];
+  if (x.row != y.row) return x.row < y.row;
+  if (x.col != y.col) return x.col < y.col;
+  return x.angle < y.angle;
+}
+
+__global__ void __launch_bounds__(1024) sort_kernel(SortArgs a) {
+  extern __shared__ unsigned char smem[];
+  const int n = a.state->count[a.slot];
+  int P = 1;
+  while (P < n) P <<= 1;
+  double* key = reinterpret_cast<double*>(smem);
+  int* idx = reinterpret_cast<int*>(key + P);
+  for (int t = threadIdx.x; t < P; t += blockDim.x) {
+    idx[t] = t < n ? t : -1;
+    key[t] = t < n ? a.in[t].score : -INFINITY;
+  }
+  __syncthreads();
+  for (int k = 2; k <= P; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int t = threadIdx.x; t < P; t += blockDim.x) {
+        const int l = t ^ j;
+        if (l > t) {
+          const bool up = (t & k) == 0;
+          const bool swap = up ? before(a.in, key, idx, l, t) : before(a.in, key, idx, t, l);
+          if (swap) {
+            const double tk = key[t];
+            key[t] = key[l];
+            key[l] = tk;
+            const int ti = idx[t];
+            idx[t] = idx[l];
+            idx[l] = ti;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  __shared__ int finite_count;
+  if (threadIdx.x == 0) finite_count = 0;
+  __syncthreads();
+  int local = 0;
+  for (int t = threadIdx.x; t < n; t += blockDim.x) {
+    const Cand c = a.in[idx[t]];
+    a.out[t] = c;
+    local += isfinite(c.score) ? 1 : 0;
+  }
+  atomicAdd(&finite_count, local);
+  __syncthreads();
+  if (threadIdx.x == 0) a.state->sorted_count = finite_count;
+}
+
+// ----------------------------------------------------------------- overlap
+// Intersection area of two rotated template rectangles over the template
+// area (src/ncc_matching/matcher.cpp:252-277).  a is the candidate, b the
+// accepted match.
+struct Pt { double x, y; };
+
+__device__ void rect_corners(const Cand& m, const Cand& a, const SelectArgs& s, Pt out[4]) {
+  double sa, ca;
+  sincos(m.angle, &sa, &ca);
+  const double left = -s.tmpl_ocol - .5, right = s.tmpl_w - s.tmpl_ocol - .5;
+  const double top = -s.tmpl_orow - .5, bottom = s.tmpl_h - s.tmpl_orow - .5;
+  const Pt in[4] = {{left, top}, {right, top}, {right, bottom}, {left, bottom}};
+  for (int i = 0; i < 4; ++i) {
+    out[i].x = dadd(dadd(dsub(m.col, a.col), dmul(ca, in[i].x)), dmul(sa, in[i].y));
+    out[i].y = dadd(dsub(dsub(m.row, a.row), dmul(sa, in[i].x)), dmul(ca, in[i].y));
+  }
+}
+
+__device__ double overlap_ratio(const Cand& a, const Cand& b, const SelectArgs& s) {
+  Pt clip[4], poly[16], next[16];
+  rect_corners(b, a, s, clip);
+  rect_corners(a, a, s, poly);
+  // axis-aligned boxes disjoint -> empty intersection
+  double ax0 = poly[0].x, ax1 = ax0, ay0 = poly[0].y, ay1 = ay0, bx0 = clip[0].x, bx1 = bx0, by0 = clip[0].y, by1 = by0;
+  for (int i = 1; i < 4; ++i) {
+    ax0 = fmin(ax0, poly[i].x); ax1 = fmax(ax1, poly[i].x); ay0 = fmin(ay0, poly[i].y); ay1 = fmax(ay1, poly[i].y);
+    bx0 = fmin(bx0, clip[i].x); bx1 = fmax(bx1, clip[i].x); by0 = fmin(by0, clip[i].y); by1 = fmax(by1, clip[i].y);
+  }
+  if (ax1 < bx0 || bx1 < ax0 || ay1 < by0 || by1 < ay0) return 0.;
+  int count = 4;
+  for (int edge = 0; edge < 4 && count; ++edge) {
+    const Pt p = clip[edge], q = clip[(edge + 1) & 3];
+    int out = 0;
+    for (int i = 0; i < count; ++i) {
+      const Pt u = poly[i], v = poly[(i + 1) % count];
+      const double du = dsub(dmul(dsub(q.x, p.x), dsub(u.y, p.y)), dmul(dsub(q.y, p.y), dsub(u.x, p.x)));
+      const double dv = dsub(dmul(dsub(q.x, p.x), dsub(v.y, p.y)), dmul(dsub(q.y, p.y), dsub(v.x, p.x)));
+      if (du >= 0 && out < 16) next[out++] = u;
+      if ((du >= 0) != (dv >= 0) && out < 16) {
+        const double t = du / dsub(du, dv);
+        next[out++] = Pt{dadd(u.x, dmul(t, dsub(v.x, u.x))), dadd(u.y, dmul(t, dsub(v.y, u.y)))};
+      }
+    }
+    for (int i = 0; i < out; ++i) poly[i] = next[i];
+    count = out;
+  }
+  double area = 0;
+  for (int i = 0; i < count; ++i)
+    area = dadd(area, dsub(dmul(poly[i].x, poly[(i + 1) % count].y), dmul(poly[(i + 1) % count].x, poly[i].y)));
+  return fabs(area) * .5 / (s.tmpl_w * s.tmpl_h);
+}
+
+// Greedy MaxOverlap selection over the sorted candidates
+// (src/ncc_matching/matcher.cpp:1063-1076).  Refinement results come from
+// refine_kernel; when the next candidate has none, the kernel queues a batch
+// of candidates that the current accepted set does not suppress and returns
+// with state->need = 1.
+__device__ bool suppressed_by(const Cand& c, const Cand* list, int n, const SelectArgs& s) {
+  __shared__ int hit;
+  if (threadIdx.x == 0) hit = 0;
+  __syncthreads();
+  for (int j = threadIdx.x; j < n; j += blockDim.x)
+    if (overlap_ratio(c, list[j], s) > s.max_overlap + 1e-12) hit = 1;
+  __syncthreads();
+  const bool r = hit != 0;
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(256) select_kernel(SelectArgs a) {
+  __shared__ Cand batch_poses[64];
+  QueryState* st = a.state;
+  if (st->done) return;
+  const int total = st->sorted_count;
+  if (threadIdx.x == 0) st->need = 0;
+  while (true) {
+    const int i = st->next;
+    const int accepted = st->accepted;
+    __syncthreads();
+    if (i >= total || (a.num_matches && accepted >= a.num_matches)) break;
+    const Cand c = a.sorted[i];
+    if (suppressed_by(c, a.accepted, accepted, a)) {
+      __syncthreads();
+      if (threadIdx.x == 0) st->next = i + 1;
+      __syncthreads();
+      continue;
+    }
+    if (a.refined_flag[i] != 2) {
+      // queue a refinement batch starting at i
+      int nb = 0;
+      for (int k = i; k < total && nb < a.batch_limit && nb < 64; ++k) {
+        if (a.refined_flag[k] == 2) continue;
+        const Cand ck = a.sorted[k];
+        if (k != i && suppressed_by(ck, a.accepted, accepted, a)) continue;
+        if (k != i && suppressed_by(ck, batch_poses, nb, a)) continue;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          batch_poses[nb] = ck;
+          a.batch[nb] = k;
+          a.refined_flag[k] = 1;
+        }
+        ++nb;
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) {
+        st->batch_count = nb;
+        st->need = 1;
+      }
+      return;
+    }
+    const Refined r = a.refined[i];
+    bool keep = r.ok != 0;
+    Cand rc;
+    rc.row = r.row;
+    rc.col = r.col;
+    rc.angle = r.angle;
+    rc.score = r.score;
+    if (keep && suppressed_by(rc, a.accepted, accepted, a)) keep = false;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      if (keep) {
+        a.accepted[accepted] = rc;
+        st->accepted = accepted + 1;
+      }
+      st->next = i + 1;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    // final order: score desc, row, column, angle (src/ncc_matching/matcher.cpp:1072-1075)
+    const int n = st->accepted;
+    for (int x = 1; x < n; ++x) {
+      const Cand v = a.accepted[x];
+      int y = x - 1;
+      while (y >= 0) {
+        const Cand u = a.accepted[y];
+        const bool after = u.score != v.score ? u.score < v.score
+                           : u.row != v.row   ? u.row > v.row
+                           : u.col != v.col   ? u.col > v.col
+                                              : u.angle > v.angle;
+        if (!after) break;
+        a.accepted[y + 1] = u;
+        --y;
+      }
+      a.accepted[y + 1] = v;
+    }
+    st->done = 1;
+  }
+}
+
+// --------------------------------------------------------------- refinement
+// refinement_step of src/ncc_matching/matcher.cpp:170-240 at a level-local
+// pose: bilinear samples with the analytic gradient, FP32 per thread, two-sum
+// combination, FP64 normal equations and Gauss-Jordan solve on thread 0.
+// Afterwards sh.ok / sh.gscore / sh.delta hold the result for every thread.
+__device__ void gn_pass(const ImageView& img, const OriginalView& orig, double row, double col, double angle,
+                        int absolute, int rotate, bool use_minimum, double minimum, PoseShared& sh) {
+  if (threadIdx.x == 0) sh.lp = make_local(row, col, angle);
+  __syncthreads();
+  const LocalPose L = sh.lp;
+  const float hmax = float(img.h - 1 - L.R0), wmax = float(img.w - 1 - L.C0);
+  const float hmin = float(-L.R0), wmin = float(-L.C0);
+  float offset = 0.f;
+  {
+    const float dr = orig.dr[0], dc = orig.dc[0];
+    const float y = L.fr + (L.ca * dr - L.sa * dc), x = L.fc + (L.sa * dr + L.ca * dc);
+    if (y >= hmin && x >= wmin && y < hmax && x < wmax) {
+      const float fy0 = floorf(y), fx0 = floorf(x);
+      const int r = L.R0 + int(fy0), c = L.C0 + int(fx0);
+      offset = bilinear_at(img, r, c, y - fy0, x - fx0, r + 1, c + 1);
+    }
+  }
+  // 0 sum q, 1 sum q^2, 2 sum wq, 3..5 gs, 6..8 qg, 9..11 wg, 12..17 gg (00,10,11,20,21,22), 18 out
+  float acc[19];
+#pragma unroll
+  for (int k = 0; k < 19; ++k) acc[k] = 0.f;
+  for (int s = threadIdx.x; s < orig.n; s += blockDim.x) {
+    const float dr = __ldg(orig.dr + s), dc = __ldg(orig.dc + s), w = __ldg(orig.w + s);
+    const float y = L.fr + (L.ca * dr - L.sa * dc), x = L.fc + (L.sa * dr + L.ca * dc);
+    if (!(y >= hmin && x >= wmin && y < hmax && x < wmax)) {
+      acc[18] = 1.f;
+      continue;
+    }
+    const float fy0 = floorf(y), fx0 = floorf(x);
+    const float fy = y - fy0, fx = x - fx0;
+    const float* v = img.v + size_t(L.R0 + int(fy0)) * img.w + (L.C0 + int(fx0));
+    const float va = __ldg(v), vb = __ldg(v + 1), vd = __ldg(v + img.w), ve = __ldg(v + img.w + 1);
+    const float q = (1 - fy) * ((1 - fx) * va + fx * vb) + fy * ((1 - fx) * vd + fx * ve) - offset;
+    const float gy = (1 - fx) * (vd - va) + fx * (ve - vb), gx = (1 - fy) * (vb - va) + fy * (ve - vd);
+    const float g2 = gy * (-L.sa * dr - L.ca * dc) + gx * (L.ca * dr - L.sa * dc);
+    acc[0] += q;
+    acc[1] = fmaf(q, q, acc[1]);
+    acc[2] = fmaf(w, q, acc[2]);
+    acc[3] += gy;
+    acc[4] += gx;
+    acc[5] += g2;
+    acc[6] = fmaf(q, gy, acc[6]);
+    acc[7] = fmaf(q, gx, acc[7]);
+    acc[8] = fmaf(q, g2, acc[8]);
+    acc[9] = fmaf(w, gy, acc[9]);
+    acc[10] = fmaf(w, gx, acc[10]);
+    acc[11] = fmaf(w, g2, acc[11]);
+    acc[12] = fmaf(gy, gy, acc[12]);
+    acc[13] = fmaf(gx, gy, acc[13]);
+    acc[14] = fmaf(gx, gx, acc[14]);
+    acc[15] = fmaf(g2, gy, acc[15]);
+    acc[16] = fmaf(g2, gx, acc[16]);
+    acc[17] = fmaf(g2, g2, acc[17]);
+  }
+  double t[19];
+  block_total<19>(acc, t, sh.scratch);
+  if (threadIdx.x == 0) {
+    sh.ok = 0;
+    sh.gscore = -INFINITY;
+    sh.delta[0] = sh.delta[1] = sh.delta[2] = 0;
+    const double n = double(orig.n);
+    const double sum = t[0], dot = t[2];
+    const double energy = t[1] - sum * sum / n;
+    if (!(t[18] > 0) && energy > 0) {
+      const double sign = absolute && dot < 0 ? -1 : 1, score = sign * dot / sqrt(energy);
+      sh.gscore = fmin(1., fmax(-1., score));
+      if (!(use_minimum && sh.gscore <= minimum)) {
+        const int axes = rotate ? 3 : 2;
+        double gs[3] = {t[3], t[4], t[5]}, qg[3] = {t[6], t[7], t[8]}, wg[3] = {t[9], t[10], t[11]};
+        const double gg[3][3] = {{t[12], t[13], t[15]}, {t[13], t[14], t[16]}, {t[15], t[16], t[17]}};
+        double m[3][4];
+        for (int i = 0; i < axes; ++i) qg[i] -= sum * gs[i] / n;
+        for (int i = 0; i < axes; ++i) {
+          for (int j = 0; j < axes; ++j) m[i][j] = (gg[i][j] - gs[i] * gs[j] / n - qg[i] * qg[j] / energy) / energy;
+          m[i][axes] = sign * wg[i] / sqrt(energy) - score * qg[i] / energy;
+        }
+        bool good = true;
+        for (int i = 0; i < axes && good; ++i) {
+          int pivot = i;
+          for (int j = i + 1; j < axes; ++j)
+            if (fabs(m[j][i]) > fabs(m[pivot][i])) pivot = j;
+          if (fabs(m[pivot][i]) < 1e-14) {
+            good = false;
+            break;
+          }
+          for (int k = i; k <= axes; ++k) {
+            const double tmp = m[i][k];
+            m[i][k] = m[pivot][k];
+            m[pivot][k] = tmp;
+          }
+          const double div = m[i][i];
+          for (int k = i; k <= axes; ++k) m[i][k] /= div;
+          for (int j = 0; j < axes; ++j)
+            if (j != i) {
+              const double f = m[j][i];
+              for (int k = i; k <= axes; ++k) m[j][k] -= f * m[i][k];
+            }
+        }
+        if (good) {
+          for (int i = 0; i < axes; ++i) sh.delta[i] = m[i][axes];
+          if (!rotate) sh.delta[2] = 0;
+          sh.ok = isfinite(sh.delta[0]) && isfinite(sh.delta[1]) && isfinite(sh.delta[2]);
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ bool inside_image(double row, double col, double height, double width) {
+  const double r = floor(row + .5), c = floor(col + .5);
+  return r >= 0 && c >= 0 && r < height && c < width;
+}
+
+// Per-block fit state; scalar decisions are made by thread 0 and read by all
+// threads after a barrier.
+struct FitShared {
+  PoseShared ps;
+  Cand c, imp, best, seed;
+  double next_delta[3], delta[3], factor;
+  int cached, accepted, next_valid, flag;
+  float wbest[8];
+  int word[8];
+};
+
+__device__ __forceinline__ double local_row(const RefineArgs& a, double row) { return (row - a.crop_row - a.phase) / a.scale; }
+__device__ __forceinline__ double local_col(const RefineArgs& a, double col) { return (col - a.crop_col - a.phase) / a.scale; }
+
+__device__ void score_pose(const RefineArgs& a, FitShared& f, const Cand& p) {
+  continuous_pass(a.img, a.orig, local_row(a, p.row), local_col(a, p.col), p.angle, a.absolute, f.ps);
+}
+
+__device__ __forceinline__ double step_factor(const double d[3], int rotate, double angle_step) {
+  double fct = fmin(1., fmin(.75 / fmax(1e-20, fabs(d[0])), .75 / fmax(1e-20, fabs(d[1]))));
+  if (rotate) fct = fmin(fct, angle_step / fmax(1e-20, fabs(d[2])));
+  return fct;
+}
+
+// fit() of src/ncc_matching/matcher.cpp:903-982 for the candidate in f.c
+// (single-model query: no memo, no background guard).
+__device__ void fit_full(const RefineArgs& a, FitShared& f) {
+  if (!a.subpixel) return;
+  if (threadIdx.x == 0) f.cached = 0;
+  __syncthreads();
+  for (int it = 0; it < 6; ++it) {
+    if (!f.cached) {
+      gn_pass(a.img, a.orig, local_row(a, f.c.row), local_col(a, f.c.col), f.c.angle, a.absolute, a.rotate, false, 0.,
+              f.ps);
+      if (!f.ps.ok) break;
+      if (threadIdx.x == 0)
+        for (int k = 0; k < 3; ++k) f.delta[k] = f.ps.delta[k];
+    } else if (threadIdx.x == 0) {
+      for (int k = 0; k < 3; ++k) f.delta[k] = f.next_delta[k];
+    }
+    if (threadIdx.x == 0) {
+      f.cached = 0;
+      f.factor = step_factor(f.delta, a.rotate, a.angle_step);
+      f.accepted = 0;
+    }
+    __syncthreads();
+    for (int bt = 0; bt < 4; ++bt) {
+      if (threadIdx.x == 0) {
+        const double st = ldexp(f.factor, -bt);
+        Cand imp = f.c;
+        imp.row = dadd(imp.row, dmul(st, f.delta[0]));
+        imp.col = dadd(imp.col, dmul(st, f.delta[1]));
+        imp.angle = fmin(fmax(dadd(imp.angle, dmul(st, f.delta[2])), a.angle_start), a.angle_end);
+        f.imp = imp;
+        f.flag = inside_image(imp.row, imp.col, a.height, a.width);
+        f.next_valid = 0;
+      }
+      __syncthreads();
+      if (!f.flag) continue;
+      if (bt == 0 && it + 1 < 6) {
+        gn_pass(a.img, a.orig, local_row(a, f.imp.row), local_col(a, f.imp.col), f.imp.angle, a.absolute, a.rotate,
+                true, f.c.score, f.ps);
+        if (threadIdx.x == 0) {
+          f.imp.score = f.ps.gscore;
+          f.next_valid = f.ps.ok;
+          for (int k = 0; k < 3; ++k) f.next_delta[k] = f.ps.delta[k];
+        }
+        __syncthreads();
+        if (!isfinite(f.imp.score)) {
+          score_pose(a, f, f.imp);
+          if (threadIdx.x == 0) f.imp.score = f.ps.score;
+        }
+      } else {
+        score_pose(a, f, f.imp);
+        if (threadIdx.x == 0) f.imp.score = f.ps.score;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0 && f.imp.score > f.c.score) {
+        f.c = f.imp;
+        f.accepted = 1;
+        f.cached = f.next_valid;
+      }
+      __syncthreads();
+      if (f.accepted) break;
+    }
+    if (threadIdx.x == 0)
+      f.flag = !f.accepted || (hypot(f.delta[0], f.delta[1]) < 1e-4 && fabs(f.delta[2]) < 1e-5);
+    __syncthreads();
+    if (f.flag) break;
+  }
+  __syncthreads();
+}
+
+// refine_coarse_candidate of src/ncc_matching/matcher.cpp:853-877
+__device__ void fit_coarse(const RefineArgs& a, FitShared& f) {
+  if (!a.subpixel) return;
+  for (int it = 0; it < 6; ++it) {
+    gn_pass(a.img, a.orig, local_row(a, f.c.row), local_col(a, f.c.col), f.c.angle, a.absolute, a.rotate, false, 0.,
+            f.ps);
+    if (!f.ps.ok) break;
+    if (threadIdx.x == 0) {
+      for (int k = 0; k < 3; ++k) f.delta[k] = f.ps.delta[k];
+      f.factor = step_factor(f.delta, a.rotate, a.angle_step);
+      f.accepted = 0;
+    }
+    __syncthreads();
+    for (int bt = 0; bt < 4; ++bt) {
+      if (threadIdx.x == 0) {
+        const double st = ldexp(f.factor, -bt);
+        Cand nx = f.c;
+        nx.row = dadd(nx.row, dmul(dmul(a.scale, st), f.delta[0]));
+        nx.col = dadd(nx.col, dmul(dmul(a.scale, st), f.delta[1]));
+        nx.angle = fmin(fmax(dadd(nx.angle, dmul(st, f.delta[2])), a.angle_start), a.angle_end);
+        f.imp = nx;
+        f.flag = inside_image(nx.row, nx.col, a.height, a.width);
+      }
+      __syncthreads();
+      if (!f.flag) continue;
+      score_pose(a, f, f.imp);
+      if (threadIdx.x == 0) {
+        f.imp.score = f.ps.score;
+        if (f.imp.score > f.c.score) {
+          f.c = f.imp;
+          f.accepted = 1;
+        }
+      }
+      __syncthreads();
+      if (f.accepted) break;
+    }
+    if (!f.accepted) break;
+  }
+  __syncthreads();
+}
+
+// Discrete level-0 search around the seed (matcher.cpp:986-1059): one warp per
+// (patch, position), exact integer moments in the loop.  Leaves the first
+// strict maximum over (patch order, dr, dc) in f.best (score -inf if none).
+__device__ void recovery_search(const RefineArgs& a, FitShared& f) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const Cand seed = f.seed;
+  float best = -INFINITY;
+  int border = INT32_MAX;
+  int k = 0;
+  for (int j = 0; j < a.nplist0; ++j) {
+    const PatchDesc pd = a.view0.patches[a.plist0[j]];
+    if (fabs(pd.angle - seed.angle) > a.angle_step * 1.01) continue;
+    const PosRange rg = a.ranges0[j];
+    const int r0 = int(round(seed.row - a.crop_row - pd.orow)), c0 = int(round(seed.col - a.crop_col - pd.ocol));
+    for (int pos = warp; pos < 25; pos += nw) {
+      const int r = r0 + pos / 5 - 2, c = c0 + pos % 5 - 2;
+      if (r < rg.r0 || r >= rg.r1 || c < rg.c0 || c >= rg.c1) continue;
+      const int32_t* offs = a.view0.offs + pd.sample_off;
+      const float* wt = a.view0.w + pd.sample_off;
+      const float* base = a.lev0.v + size_t(r) * a.lev0.w + c;
+      const int32_t o0 = __ldg(offs);
+      const float s0 = base[off_row(o0) * a.lev0.w + off_col(o0)];
+      float dot = 0.f;
+      long long s1 = 0, s2 = 0;
+      for (int s = lane; s < pd.n; s += 32) {
+        const int32_t o = __ldg(offs + s);
+        const float x = base[off_row(o) * a.lev0.w + off_col(o)] - s0;
+        dot = fmaf(__ldg(wt + s), x, dot);
+        const long long xi = (long long)x;
+        s1 += xi;
+        s2 += xi * xi;
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        dot += __shfl_down_sync(0xffffffffu, dot, o);
+        s1 += __shfl_down_sync(0xffffffffu, s1, o);
+        s2 += __shfl_down_sync(0xffffffffu, s2, o);
+      }
+      if (lane == 0) {
+        const float sc = window_score(dot, s1, s2, pd.n, a.absolute);
+        const int order = k * 25 + pos;
+        if (better(sc, order, best, border)) {
+          best = sc;
+          border = order;
+        }
+      }
+    }
+    ++k;
+  }
+  if (lane == 0) {
+    f.wbest[warp] = best;
+    f.word[warp] = border;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float bs = -INFINITY;
+    int bo = INT32_MAX;
+    for (int w = 0; w < nw; ++w)
+      if (better(f.wbest[w], f.word[w], bs, bo)) {
+        bs = f.wbest[w];
+        bo = f.word[w];
+      }
+    Cand out = seed;
+    out.score = -INFINITY;
+    if (bo != INT32_MAX && bs > -INFINITY) {
+      int kk = 0;
+      for (int j = 0; j < a.nplist0; ++j) {
+        const PatchDesc pd = a.view0.patches[a.plist0[j]];
+        if (fabs(pd.angle - seed.angle) > a.angle_step * 1.01) continue;
+        if (kk == bo / 25) {
+          const int r0 = int(round(seed.row - a.crop_row - pd.orow)), c0 = int(round(seed.col - a.crop_col - pd.ocol));
+          out.row = double((long long)a.crop_row + r0 + (bo % 25) / 5 - 2) + pd.orow;
+          out.col = double((long long)a.crop_col + c0 + (bo % 25) % 5 - 2) + pd.ocol;
+          out.angle = pd.angle;
+          out.score = double(bs);
+          break;
+        }
+        ++kk;
+      }
+    }
+    f.best = out;
+  }
+  __syncthreads();
+}
+
+// refine_candidate (src/ncc_matching/matcher.cpp:878-1061) for one queued
+// candidate per block.
+__global__ void __launch_bounds__(256) refine_kernel(RefineArgs a) {
+  __shared__ FitShared f;
+  const int b = blockIdx.x;
+  if (b >= a.state->batch_count) return;
+  const int i = a.batch[b];
+  if (threadIdx.x == 0) {
+    f.c = a.sorted[i];
+    f.seed = f.c;
+  }
+  __syncthreads();
+  if (a.finest) {
+    fit_coarse(a, f);
+  } else {
+    fit_full(a, f);
+    if (a.subpixel && a.top > 0 && f.c.score < a.min_score) {
+      recovery_search(a, f);
+      // the search starts from the fitted candidate: only a strictly higher
+      // discrete score moves it
+      if (threadIdx.x == 0) {
+        if (!(f.best.score > f.c.score)) f.best = f.c;
+        f.flag = f.best.row != f.c.row || f.best.col != f.c.col || f.best.angle != f.c.angle;
+      }
+      __syncthreads();
+      if (f.flag) {
+        score_pose(a, f, f.best);
+        if (threadIdx.x == 0) {
+          f.best.score = f.ps.score;
+          f.seed = f.c;      // keep the fitted candidate
+          f.c = f.best;
+        }
+        __syncthreads();
+        fit_full(a, f);
+        if (threadIdx.x == 0 && !(f.c.score > f.seed.score)) f.c = f.seed;
+        __syncthreads();
+      }
+    }
+  }
+  if (threadIdx.x == 0) {
+    Refined r;
+    r.row = f.c.row;
+    r.col = f.c.col;
+    r.angle = f.c.angle;
+    r.score = f.c.score;
+    r.ok = (f.c.score >= a.min_score) && inside_image(f.c.row, f.c.col, a.height, a.width);
+    r.pad = 0;
+    a.refined[i] = r;
+    __threadfence();
+    a.refined_flag[i] = 2;
+  }
+}
+
+}  // namespace
+
+// --------------------------------------------------------------- launchers
+cudaError_t launch_pyramid0(const void* src, int type, int64_t pitch_elems, int crop_row, int crop_col, LevelImage dst,
+                            int32_t* error_flag, cudaStream_t s) {
+  (void)error_flag;
+  const dim3 block(32, 8), grid((dst.w + 31) / 32, (dst.h + 7) / 8);
+  if (type == 1)
+    pyramid0_kernel<uint16_t><<<grid, block, 0, s>>>(static_cast<const uint16_t*>(src), pitch_elems, crop_row, crop_col, dst);
+  else
+    pyramid0_kernel<uint8_t><<<grid, block, 0, s>>>(static_cast<const uint8_t*>(src), pitch_elems, crop_row, crop_col, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pyramid(const LevelImage& src, LevelImage dst, int32_t* error_flag, cudaStream_t s) {
+  const dim3 block(32, 8), grid((dst.w + 31) / 32, (dst.h + 7) / 8);
+  pyramid_kernel<<<grid, block, 0, s>>>(src, dst, error_flag);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prefix(const LevelImage& lev, cudaStream_t s) {
+  const int warps = lev.h, threads = 256;
+  const int blocks = (warps * 32 + threads - 1) / threads;
+  prefix_kernel<<<blocks, threads, 0, s>>>(lev);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_coarse(const CoarseArgs& a, int max_bh, int max_bw, cudaStream_t s, size_t smem_limit) {
+  const size_t smem = size_t(kTileH + max_bh) * size_t(kTileW + max_bw) * sizeof(float);
+  if (smem > smem_limit) return cudaErrorInvalidConfiguration;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(coarse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_limit));
+    attr = true;
+  }
+  const dim3 block(kTileW, kTileH), grid((a.lev.w + kTileW - 1) / kTileW, (a.lev.h + kTileH - 1) / kTileH, a.nplist);
+  coarse_kernel<<<grid, block, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_nms(const NmsArgs& a, cudaStream_t s) {
+  const int64_t n = int64_t(a.w) * a.h * a.nplist;
+  nms_kernel<<<unsigned((n + 255) / 256), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_track(const TrackArgs& a, int max_candidates, cudaStream_t s) {
+  track_kernel<<<max_candidates, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dedup(const DedupArgs& a, int max_candidates, cudaStream_t s) {
+  const unsigned blocks = unsigned((max_candidates + 255) / 256);
+  if (a.snap) snap_kernel<<<blocks, 256, 0, s>>>(const_cast<Cand*>(a.in), a.state, a.in_slot, a.height, a.width);
+  dedup_kernel<<<blocks, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_score(const ScoreArgs& a, int max_candidates, cudaStream_t s) {
+  score_kernel<<<max_candidates, 128, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sort(const SortArgs& a, cudaStream_t s) {
+  const size_t smem = 16384 * (sizeof(double) + sizeof(int));
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    attr = true;
+  }
+  sort_kernel<<<1, 1024, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_select(const SelectArgs& a, cudaStream_t s) {
+  select_kernel<<<1, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_refine(const RefineArgs& a, int batch_limit, cudaStream_t s) {
+  refine_kernel<<<batch_limit, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace mvg

@@ -1,0 +1,63 @@
+// Host-side NCC model (CreateNccModel).  The model is built once on the host
+// in FP64, exactly as the reference builds it, then uploaded to HBM as flat
+// sample/run tables that the find kernels read.
+#pragma once
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "ncc_types.h"
+
+namespace mvg {
+
+struct Error : std::runtime_error {
+  int32_t status;
+  Error(int32_t s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+[[noreturn]] inline void raise(int32_t status, const std::string& message) { throw Error(status, message); }
+
+struct CreateParams {
+  int levels = 0;               // 0 = automatic (up to 16)
+  bool ignore_polarity = false; // Metric "ignore_global_polarity"
+  double angle_start = 0, angle_extent = 0, angle_step = 0;  // step 0 = automatic
+};
+
+// One template raster: samples in raster order with FP64 unit-energy weights.
+struct Raster {
+  double angle = 0, orow = 0, ocol = 0;
+  int32_t rmin = 0, rmax = 0, cmin = 0, cmax = 0;
+  std::vector<int32_t> rows, cols;
+  std::vector<double> w;
+  double wsum = 0;
+  std::vector<int32_t> run_row, run_begin, run_end;
+  size_t size() const { return w.size(); }
+};
+
+struct ModelLevel {
+  size_t width = 0, height = 0;
+  double orow = 0, ocol = 0;
+  std::vector<double> gray;
+  std::vector<uint8_t> mask;
+  std::vector<Raster> patches;
+};
+
+struct HostModel {
+  CreateParams params;          // params.angle_step holds the resolved step
+  size_t sample_count = 0;
+  double origin_row = 0, origin_col = 0;
+  Raster original;              // unrotated level-0 raster (row/col absolute)
+  std::vector<ModelLevel> levels;
+};
+
+// CreateNccModel on a byte (type 0) or uint16 (type 1) template.  `mask`
+// (width*height bytes, nonzero = inside) is the template domain; NULL means
+// the whole image.  Throws Error with an MvStatus code.
+HostModel create_model(const void* pixels, int type, int64_t width, int64_t height, int64_t stride_bytes,
+                       const uint8_t* mask, const CreateParams& params);
+
+// Raster of `level` rotated by `angle` (used for query-range endpoints that
+// fall between trained angles).  Empty when the rotation is degenerate.
+Raster rotate_level(const ModelLevel& level, double angle);
+
+}  // namespace mvg

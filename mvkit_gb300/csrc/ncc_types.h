@@ -1,0 +1,82 @@
+// Shared host/device layouts of the GB300 NCC matcher.
+#pragma once
+#include <cstdint>
+
+namespace mvg {
+
+constexpr int kMaxLevels = 16;
+constexpr int kMaxCandidates = 10000;        // FindOptions::max_candidates (src/ncc_matching/model.hpp:21)
+constexpr int kHashSlots = 32768;            // >= 3 x kMaxCandidates, power of two
+
+// Status codes (MvStatus, include/mvkit/c/mv_status.h:12-24 in the reference).
+enum Status : int32_t {
+  kOk = 0,
+  kInvalidArgument = -1,
+  kTypeMismatch = -3,
+  kOutOfMemory = -5,
+  kUnsupported = -6,
+  kInvalidState = -7,
+  kLimitExceeded = -103,
+  kInternal = -1000,
+};
+
+// One rotated template raster on the device.  Sample offsets are relative to
+// the patch reference point (the level origin for rotated patches, the level's
+// top-left corner for the unrotated one, src/ncc_matching/model.cpp:66-98).
+struct PatchDesc {
+  double angle;
+  double orow, ocol;            // added to the integer position to get the pose
+  int32_t rmin, rmax, cmin, cmax;
+  int32_t n;                    // samples
+  int32_t sample_off;           // into the level's sample arrays
+  int32_t nruns;                // contiguous row spans
+  int32_t run_off;
+};
+
+// Device view of one model level (its patches and their samples).
+struct LevelView {
+  const PatchDesc* patches;
+  const int32_t* offs;          // packed (row << 16) | (col & 0xffff), int16 each
+  const float* w;               // sample weights (float of the FP64 model weight)
+  const int32_t* runs;          // packed row(16) | begin; end in runs_end
+  const int32_t* runs_end;
+  int32_t npatches;
+};
+
+// Unrotated full-resolution template used for continuous scoring and the
+// Gauss-Newton fit (Model::original, src/ncc_matching/model.cpp:182-204).
+struct OriginalView {
+  const float* dr;              // sample row - level origin row
+  const float* dc;              // sample column - level origin column
+  const float* w;
+  int32_t n;
+};
+
+// A candidate pose carried between stages.  (row, column, angle) follow the
+// reference's FP64 expressions exactly; score is the stage's score.
+struct Cand {
+  double row, col, angle;
+  double score;
+};
+
+// Result of refining one candidate (src/ncc_matching/matcher.cpp:878-1061).
+struct Refined {
+  double row, col, angle, score;
+  int32_t ok;                   // score >= MinScore and inside the domain
+  int32_t pad;
+};
+
+// Per-query device state that kernels read and write.
+struct QueryState {
+  int32_t count[kMaxLevels + 2];   // candidates per stage
+  int32_t overflow;                // coarse candidate budget exceeded
+  int32_t error;                   // kernel-side failure code
+  int32_t sorted_count;            // finite full-resolution candidates
+  int32_t accepted;                // matches accepted by the greedy selection
+  int32_t next;                    // next candidate index to examine
+  int32_t need;                    // 1: refinement results missing for `next`
+  int32_t done;
+  int32_t batch_count;             // entries in the refinement batch
+};
+
+}  // namespace mvg

@@ -1,0 +1,347 @@
+"""Python mirror of mvkit's NCC matching operators over libmvkit_gb300.so.
+
+Names, argument meaning and error behaviour follow the reference C API
+(src/c_api/ncc_matching_api.cpp): each control accepts one value (a scalar
+or a one-element sequence), strings are checked as the reference checks them
+("auto", "true"/"false", metric names), and failures raise MvError carrying
+the reference's MvStatus code.  The search itself runs on the GPU through
+the C ABI declared in include/mvkit_gb300_ncc.h; there is no host fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from pathlib import Path
+from typing import Sequence
+
+import numpy as np
+
+from . import build as _build
+
+# MvStatus (include/mvkit/c/mv_status.h:12-24)
+MV_STATUS_OK = 0
+MV_STATUS_INVALID_ARGUMENT = -1
+MV_STATUS_TYPE_MISMATCH = -3
+MV_STATUS_OUT_OF_MEMORY = -5
+MV_STATUS_UNSUPPORTED = -6
+MV_STATUS_INVALID_STATE = -7
+MV_STATUS_LIMIT_EXCEEDED = -103
+MV_STATUS_INTERNAL_ERROR = -1000
+
+_dp = C.POINTER(C.c_double)
+_fp = C.POINTER(C.c_float)
+_i64p = C.POINTER(C.c_int64)
+_i32p = C.POINTER(C.c_int32)
+_u8p = C.POINTER(C.c_uint8)
+
+
+class MvError(RuntimeError):
+    def __init__(self, status: int, message: str, operator: str = ""):
+        super().__init__(f"{operator}: status {status}: {message}" if operator else f"status {status}: {message}")
+        self.status = status
+        self.message = message
+
+
+_LIB = None
+
+
+def library_path() -> Path:
+    return _build.LIB
+
+
+def load() -> C.CDLL:
+    """Loads the in-tree CUDA library; raises when it has not been built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not path.exists():
+        raise MvError(MV_STATUS_INTERNAL_ERROR, f"CUDA extension missing: {path} (run mvkit_gb300.build.build())")
+    lib = C.CDLL(str(path))
+    lib.mvg_create_ncc_model.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_int64, _u8p, C.c_int32,
+                                         C.c_double, C.c_double, C.c_double, C.c_int32, C.POINTER(C.c_void_p)]
+    lib.mvg_get_ncc_model_params.argtypes = [C.c_void_p, _i32p, _dp, _dp, _dp, _i32p]
+    lib.mvg_clear_ncc_model.argtypes = [C.c_void_p]
+    lib.mvg_find_ncc_model.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int32, C.c_void_p,
+                                       C.c_double, C.c_double, C.c_double, C.c_int64, C.c_double, C.c_int32,
+                                       C.c_int32, C.c_int32, _dp, _dp, _dp, _dp, C.c_int64, _i64p, C.c_void_p]
+    lib.mvg_find_ncc_model_stage.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int32,
+                                             C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int64, C.c_double,
+                                             C.c_int32, C.c_int32, C.c_int32, C.c_int32, _dp, C.c_int64, _i64p]
+    lib.mvg_ncc_pyramid_level.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_void_p,
+                                          C.c_int32, C.c_int32, _fp, C.c_int64, _dp]
+    lib.mvg_last_error.restype = C.c_char_p
+    lib.mvg_host_alloc.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
+    lib.mvg_host_free.argtypes = [C.c_void_p]
+    lib.mvg_device_alloc.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
+    lib.mvg_device_free.argtypes = [C.c_void_p]
+    lib.mvg_copy_to_device.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
+    for name in ("mvg_create_ncc_model", "mvg_get_ncc_model_params", "mvg_clear_ncc_model", "mvg_find_ncc_model",
+                 "mvg_find_ncc_model_stage", "mvg_ncc_pyramid_level", "mvg_host_alloc", "mvg_host_free",
+                 "mvg_device_alloc", "mvg_device_free", "mvg_copy_to_device"):
+        getattr(lib, name).restype = C.c_int32
+    _LIB = lib
+    return lib
+
+
+def _check(status: int, op: str) -> None:
+    if status != 0:
+        msg = (load().mvg_last_error() or b"").decode(errors="replace")
+        raise MvError(status, msg, op)
+
+
+# ---------------------------------------------------------------- controls
+def _values(x, op: str, name: str) -> list:
+    if isinstance(x, (list, tuple, np.ndarray)):
+        return list(x)
+    return [x]
+
+
+def _one(x, op: str, name: str):
+    v = _values(x, op, name)
+    if len(v) != 1:
+        raise MvError(MV_STATUS_INVALID_ARGUMENT, f"{name}: exactly one value required", op)
+    return v[0]
+
+
+def _number(v, op: str, name: str) -> float:
+    if isinstance(v, (bool, np.bool_)) or not isinstance(v, (int, float, np.integer, np.floating)):
+        raise MvError(MV_STATUS_TYPE_MISMATCH, f"{name}: numeric control value required", op)
+    return float(v)
+
+
+def _integer(v, op: str, name: str) -> int:
+    if isinstance(v, (bool, np.bool_)):
+        raise MvError(MV_STATUS_TYPE_MISMATCH, f"{name}: integer control value required", op)
+    if isinstance(v, (int, np.integer)):
+        return int(v)
+    if isinstance(v, (float, np.floating)):
+        if math.isfinite(v) and float(v).is_integer():
+            return int(v)
+        raise MvError(MV_STATUS_INVALID_ARGUMENT, f"{name}: integer-valued control required", op)
+    raise MvError(MV_STATUS_TYPE_MISMATCH, f"{name}: integer control value required", op)
+
+
+def _image(img, op: str, name: str):
+    a = np.asarray(img)
+    if a.ndim != 2 or a.dtype not in (np.uint8, np.uint16):
+        raise MvError(MV_STATUS_TYPE_MISMATCH, f"{name}: one byte or uint2 channel required", op)
+    if a.strides[1] != a.itemsize:
+        a = np.ascontiguousarray(a)
+    return a, (1 if a.dtype == np.uint16 else 0)
+
+
+class NccModel:
+    """Handle of a model on the GPU (the reference's NCC model handle)."""
+
+    def __init__(self, handle: C.c_void_p):
+        self.handle = handle
+
+    def __del__(self):
+        try:
+            self.clear()
+        except Exception:
+            pass
+
+    def clear(self):
+        if self.handle:
+            load().mvg_clear_ncc_model(self.handle)
+            self.handle = None
+
+
+def create_ncc_model(template, num_levels="auto", angle_start=0.0, angle_extent=0.0, angle_step="auto",
+                     metric="use_polarity", domain=None) -> NccModel:
+    """CreateNccModel (src/c_api/ncc_matching_api.cpp:29-66)."""
+    op = "create_ncc_model"
+    t, typ = _image(template, op, "Template")
+    lv = _one(num_levels, op, "NumLevels")
+    if isinstance(lv, str):
+        if lv != "auto":
+            raise MvError(MV_STATUS_INVALID_ARGUMENT, "NumLevels: expected auto", op)
+        levels = 0
+    else:
+        levels = _integer(lv, op, "NumLevels")
+        if levels < 0 or levels > 16:
+            raise MvError(MV_STATUS_INVALID_ARGUMENT, "levels must be 0..16 or auto", op)
+    start = _number(_one(angle_start, op, "AngleStart"), op, "AngleStart")
+    extent = _number(_one(angle_extent, op, "AngleExtent"), op, "AngleExtent")
+    if not math.isfinite(start) or not math.isfinite(extent):
+        raise MvError(MV_STATUS_INVALID_ARGUMENT, "finite control value required", op)
+    st = _one(angle_step, op, "AngleStep")
+    if isinstance(st, str):
+        if st != "auto":
+            raise MvError(MV_STATUS_INVALID_ARGUMENT, "AngleStep: expected auto", op)
+        step = 0.0
+    else:
+        step = _number(st, op, "AngleStep")
+        if not math.isfinite(step):
+            raise MvError(MV_STATUS_INVALID_ARGUMENT, "finite control value required", op)
+        if step < 0 or step > math.pi / 16:
+            raise MvError(MV_STATUS_INVALID_ARGUMENT, "angle step must be in [0,pi/16] or auto", op)
+    m = _one(metric, op, "Metric")
+    if not isinstance(m, str):
+        raise MvError(MV_STATUS_TYPE_MISMATCH, "Metric: string control value required", op)
+    if m == "ignore_global_polarity":
+        metric_id = 1
+    elif m == "use_polarity":
+        metric_id = 0
+    else:
+        raise MvError(MV_STATUS_INVALID_ARGUMENT, "unsupported NCC metric", op)
+    d = None
+    if domain is not None:
+        d = np.ascontiguousarray(np.asarray(domain) != 0, dtype=np.uint8)
+        if d.shape != t.shape:
+            raise MvError(MV_STATUS_INVALID_ARGUMENT, "domain must match the template size", op)
+    h = C.c_void_p()
+    lib = load()
+    _check(lib.mvg_create_ncc_model(t.ctypes.data, typ, t.shape[1], t.shape[0], t.strides[0],
+                                    d.ctypes.data_as(_u8p) if d is not None else None, levels, start, extent, step,
+                                    metric_id, C.byref(h)), op)
+    return NccModel(h)
+
+
+def get_ncc_model_params(model: NccModel):
+    """GetNccModelParams (src/c_api/ncc_matching_api.cpp:85-96)."""
+    lv = C.c_int32()
+    a0, a1, a2 = C.c_double(), C.c_double(), C.c_double()
+    mt = C.c_int32()
+    _check(load().mvg_get_ncc_model_params(model.handle, C.byref(lv), C.byref(a0), C.byref(a1), C.byref(a2),
+                                           C.byref(mt)), "get_ncc_model_params")
+    return (lv.value, a0.value, a1.value, a2.value, "ignore_global_polarity" if mt.value else "use_polarity")
+
+
+def _find_controls(op, angle_start, angle_extent, min_score, num_matches, max_overlap, subpixel, num_levels):
+    """Single-model NccControls (src/c_api/ncc_matching_api.cpp:126-162)."""
+    vals = {}
+    for name, x in (("AngleStart", angle_start), ("AngleExtent", angle_extent), ("MinScore", min_score),
+                    ("NumMatches", num_matches), ("MaxOverlap", max_overlap), ("SubPixel", subpixel)):
+        vals[name] = _one(x, op, name)
+
+    def number(name, lo, hi):
+        v = _number(vals[name], op, name)
+        if not math.isfinite(v) or v < lo or v > hi:
+            raise MvError(MV_STATUS_INVALID_ARGUMENT, f"{name}: numeric control outside allowed range", op)
+        return v
+
+    start = number("AngleStart", -1.7976931348623157e308, 1.7976931348623157e308)
+    extent = number("AngleExtent", 0.0, 6.28318530717958647692)
+    score = number("MinScore", 0.0, 1.0)
+    overlap = number("MaxOverlap", 0.0, 1.0)
+    quota = _integer(vals["NumMatches"], op, "NumMatches")
+    if quota < 0:
+        raise MvError(MV_STATUS_INVALID_ARGUMENT, "match count must be nonnegative", op)
+    mode = vals["SubPixel"]
+    if not isinstance(mode, str):
+        raise MvError(MV_STATUS_TYPE_MISMATCH, "SubPixel: string control value required", op)
+    if mode not in ("true", "false"):
+        raise MvError(MV_STATUS_INVALID_ARGUMENT, "expected true or false", op)
+    lv = _values(num_levels, op, "NumLevels")
+    if len(lv) not in (1, 2):
+        raise MvError(MV_STATUS_INVALID_ARGUMENT, "highest level or shared/per-model level pairs required", op)
+    highest = _integer(lv[0], op, "NumLevels")
+    lowest = _integer(lv[1], op, "NumLevels") if len(lv) == 2 else 1
+    if highest < 0 or highest > 2**31 - 1 or lowest < 0 or lowest > 2**31 - 1:
+        raise MvError(MV_STATUS_INVALID_ARGUMENT, "invalid highest/lowest level pair", op)
+    return start, extent, score, quota, overlap, 1 if mode == "true" else 0, highest, max(1, lowest)
+
+
+class DeviceImage:
+    """An image already resident in device memory (uint8/uint16, dense rows)."""
+
+    def __init__(self, array: np.ndarray):
+        a, typ = _image(array, "device_image", "Image")
+        self.shape = a.shape
+        self.dtype = a.dtype
+        self.type = typ
+        self.stride = a.strides[0]
+        self.nbytes = a.nbytes
+        p = C.c_void_p()
+        _check(load().mvg_device_alloc(a.nbytes, C.byref(p)), "device_image")
+        self.ptr = p
+        _check(load().mvg_copy_to_device(p, a.ctypes.data, a.nbytes), "device_image")
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                load().mvg_device_free(self.ptr)
+                self.ptr = None
+        except Exception:
+            pass
+
+
+def find_ncc_model(image, model: NccModel, angle_start, angle_extent, min_score, num_matches, max_overlap,
+                   subpixel, num_levels, stream=None):
+    """FindNccModel (src/c_api/ncc_matching_api.cpp:178-190).
+
+    image: 2-D uint8/uint16 array in host memory, or a DeviceImage.
+    Returns (Row, Column, Angle, Score) as float64 arrays in the operator's
+    edge-centred convention.  An empty image returns empty outputs."""
+    op = "find_ncc_model"
+    ctl = _find_controls(op, angle_start, angle_extent, min_score, num_matches, max_overlap, subpixel, num_levels)
+    if not isinstance(model, NccModel) or not model.handle:
+        raise MvError(MV_STATUS_TYPE_MISMATCH, "ModelID: NCC model handle required", op)
+    if isinstance(image, DeviceImage):
+        ptr, typ, (h, w), stride, loc = image.ptr, image.type, image.shape, image.stride, 1
+    else:
+        a, typ = _image(image, op, "Image")
+        if a.size == 0:
+            e = np.zeros(0)
+            return e, e.copy(), e.copy(), e.copy()
+        ptr, (h, w), stride, loc = a.ctypes.data, a.shape, a.strides[0], 0
+    cap = 64 if ctl[3] == 0 else int(ctl[3])
+    lib = load()
+    while True:
+        out = [np.zeros(cap) for _ in range(4)]
+        cnt = C.c_int64()
+        _check(lib.mvg_find_ncc_model(ptr, typ, w, h, stride, loc, model.handle, *ctl,
+                                      *[o.ctypes.data_as(_dp) for o in out], cap, C.byref(cnt),
+                                      C.c_void_p(stream) if stream else None), op)
+        if cnt.value <= cap:
+            return tuple(o[: cnt.value] for o in out)
+        cap = int(cnt.value)
+
+
+def find_ncc_model_stage(image, model: NccModel, angle_start, angle_extent, min_score, num_matches, max_overlap,
+                         subpixel, num_levels, stage: int) -> np.ndarray:
+    """Candidate list of an internal stage (n x 4: row, column, angle, score;
+    pixel-centre convention of mv::ncc_matching::find)."""
+    op = "find_ncc_model"
+    ctl = _find_controls(op, angle_start, angle_extent, min_score, num_matches, max_overlap, subpixel, num_levels)
+    a, typ = _image(image, op, "Image")
+    cap = 20000
+    out = np.zeros((cap, 4))
+    cnt = C.c_int64()
+    _check(load().mvg_find_ncc_model_stage(a.ctypes.data, typ, a.shape[1], a.shape[0], a.strides[0], 0, model.handle,
+                                           *ctl, int(stage), out.ctypes.data_as(_dp), cap, C.byref(cnt)), op)
+    return out[: min(cnt.value, cap)].copy()
+
+
+def pyramid_level(image, model: NccModel, highest_level: int, level: int):
+    """Integer pyramid level (sums of 4^level pixels) and geometry."""
+    a, typ = _image(image, "pyramid", "Image")
+    out = np.zeros(a.size + 16, dtype=np.float32)
+    geom = np.zeros(5)
+    _check(load().mvg_ncc_pyramid_level(a.ctypes.data, typ, a.shape[1], a.shape[0], a.strides[0], model.handle,
+                                        int(highest_level), int(level), out.ctypes.data_as(_fp), out.size,
+                                        geom.ctypes.data_as(_dp)), "pyramid")
+    w, h = int(geom[0]), int(geom[1])
+    return out[: w * h].reshape(h, w).copy(), geom
+
+
+class PinnedBuffer:
+    """Page-locked host buffer (for host-to-device uploads at full DMA speed)."""
+
+    def __init__(self, shape, dtype):
+        self.nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        p = C.c_void_p()
+        _check(load().mvg_host_alloc(self.nbytes, C.byref(p)), "host_alloc")
+        self.ptr = p
+        self.array = np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_uint8)), shape=(self.nbytes,)).view(dtype).reshape(shape)
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                load().mvg_host_free(self.ptr)
+                self.ptr = None
+        except Exception:
+            pass

@@ -155,12 +155,14 @@ def _finish(img: np.ndarray, rng: np.random.Generator, noise_sigma: int, maxval:
 
 def make_workload(seed: int, height: int, width: int, tsize: int, n_poses: int,
                   angle_range: tuple = (0.0, 0.0), noise_sigma: int = 3, shapes: int = 40,
-                  maxval: int = 255, contrast: float = 0.0, subpixel: bool = True) -> Workload:
+                  maxval: int = 255, contrast: float = 0.0, subpixel: bool = True,
+                  invert_odd: bool = False, border: float | None = None) -> Workload:
     """One search scene with `n_poses` pastes of one square template of side `tsize`.
 
-    angle_range is in radians; contrast > 0 scales each paste by U[1-c, 1+c].
-    Pastes are kept apart by at least the template diagonal plus a margin,
-    and away from the image border, so every pose is findable.
+    angle_range is in radians; contrast > 0 scales each paste by U[1-c, 1+c];
+    invert_odd pastes every second pose with inverted contrast.  Pastes are
+    kept apart by at least the template diagonal, and `border` pixels (default
+    half the diagonal + 8) away from the image edge.
     """
     dtype = np.uint8 if maxval <= 255 else np.uint16
     rng = np.random.default_rng([seed, 1])
@@ -172,7 +174,7 @@ def make_workload(seed: int, height: int, width: int, tsize: int, n_poses: int,
     tmpl_i = np.clip(tmpl_i + _gauss_int(rng, tmpl_i.shape, noise_sigma), 0, maxval)
     img = scene(seed, height, width, shapes=shapes, maxval=maxval)
     diag = math.hypot(tsize, tsize)
-    margin = diag / 2.0 + 8
+    margin = diag / 2.0 + 8 if border is None else float(border)
     poses: list[Pose] = []
     tries = 0
     while len(poses) < n_poses:
@@ -188,6 +190,8 @@ def make_workload(seed: int, height: int, width: int, tsize: int, n_poses: int,
         c = 1.0
         if contrast > 0:
             c = 1.0 - contrast + 2 * contrast * float(rng.integers(0, 1 << 20)) / (1 << 20)
+        if invert_odd and len(poses) % 2 == 1:
+            c = -c
         if all(math.hypot(row - p.row, col - p.column) > diag + 4 for p in poses):
             poses.append(Pose(row, col, ang, c))
     t_f = tmpl_i.astype(np.float64)

@@ -736,6 +736,9 @@ std::unique_ptr<Query> prepare(const T* px, std::int64_t W, std::int64_t H, std:
           else p.score = kMissing;
         }
       merge_identical(cand);
+      q->stages.push_back(cand);
+      ++stage;
+      if (stop_stage == stage) return q;
       break;
     }
     const Level& L = model.levels[l - 1];

@@ -1,0 +1,95 @@
+"""Seeded parity cases shared by the golden-fixture generator and the tests.
+
+Each case regenerates its image and template from mvkit_gb300.workloads
+(platform-deterministic), builds a model and runs one find.  The fixture
+file golden.json stores, per case, the input digest and the reference's
+final matches (matcher-internal pixel-centre convention)."""
+from __future__ import annotations
+
+import math
+
+from mvkit_gb300 import workloads as W
+
+D = math.radians
+
+# name: generator kwargs, create kwargs, find kwargs, optional template mask kind
+CASES = {
+    "cfg1_s1": dict(gen=dict(seed=1, height=480, width=640, tsize=64, n_poses=1),
+                    create=dict(levels=3, angle_start=0.0, angle_extent=0.0),
+                    find=dict(angle_start=0.0, angle_extent=0.0, min_score=0.8, num_matches=1, max_overlap=0.5,
+                              subpixel=True, highest=3, lowest=1)),
+    "cfg1_s2": dict(gen=dict(seed=2, height=480, width=640, tsize=64, n_poses=1),
+                    create=dict(levels=3, angle_start=0.0, angle_extent=0.0),
+                    find=dict(angle_start=0.0, angle_extent=0.0, min_score=0.8, num_matches=1, max_overlap=0.5,
+                              subpixel=True, highest=3, lowest=1)),
+    "cfg1_s3": dict(gen=dict(seed=3, height=480, width=640, tsize=64, n_poses=1),
+                    create=dict(levels=3, angle_start=0.0, angle_extent=0.0),
+                    find=dict(angle_start=0.0, angle_extent=0.0, min_score=0.8, num_matches=1, max_overlap=0.5,
+                              subpixel=True, highest=3, lowest=1)),
+    "rot3_all": dict(gen=dict(seed=11, height=600, width=800, tsize=64, n_poses=3, angle_range=(-D(30), D(30))),
+                     create=dict(levels=3, angle_start=-D(30), angle_extent=D(60)),
+                     find=dict(angle_start=-D(30), angle_extent=D(60), min_score=0.7, num_matches=0,
+                               max_overlap=0.5, subpixel=True, highest=3, lowest=1)),
+    "rot_l4_2": dict(gen=dict(seed=12, height=768, width=1024, tsize=96, n_poses=2, angle_range=(-D(20), D(20))),
+                     create=dict(levels=4, angle_start=-D(20), angle_extent=D(40)),
+                     find=dict(angle_start=-D(20), angle_extent=D(40), min_score=0.7, num_matches=2,
+                               max_overlap=0.5, subpixel=True, highest=4, lowest=1)),
+    "u16_rot": dict(gen=dict(seed=13, height=480, width=640, tsize=64, n_poses=2, angle_range=(-D(20), D(20)),
+                             maxval=4095, noise_sigma=20),
+                    create=dict(levels=3, angle_start=-D(20), angle_extent=D(40)),
+                    find=dict(angle_start=-D(20), angle_extent=D(40), min_score=0.7, num_matches=2,
+                              max_overlap=0.5, subpixel=True, highest=3, lowest=1)),
+    "polarity": dict(gen=dict(seed=14, height=480, width=640, tsize=64, n_poses=2, invert_odd=True),
+                     create=dict(levels=3, angle_start=0.0, angle_extent=0.0, ignore_polarity=True),
+                     find=dict(angle_start=0.0, angle_extent=0.0, min_score=0.7, num_matches=0, max_overlap=0.5,
+                               subpixel=True, highest=3, lowest=1)),
+    "no_subpixel": dict(gen=dict(seed=15, height=480, width=640, tsize=48, n_poses=2, angle_range=(-D(10), D(10))),
+                        create=dict(levels=3, angle_start=-D(10), angle_extent=D(20)),
+                        find=dict(angle_start=-D(10), angle_extent=D(20), min_score=0.7, num_matches=2,
+                                  max_overlap=0.5, subpixel=False, highest=3, lowest=1)),
+    "lowest2": dict(gen=dict(seed=16, height=480, width=640, tsize=64, n_poses=2, angle_range=(-D(10), D(10))),
+                    create=dict(levels=3, angle_start=-D(10), angle_extent=D(20)),
+                    find=dict(angle_start=-D(10), angle_extent=D(20), min_score=0.6, num_matches=2,
+                              max_overlap=0.5, subpixel=True, highest=3, lowest=2)),
+    "endpoints": dict(gen=dict(seed=17, height=480, width=640, tsize=64, n_poses=2, angle_range=(-D(8), D(12))),
+                      create=dict(levels=3, angle_start=-D(30), angle_extent=D(60)),
+                      find=dict(angle_start=-0.2, angle_extent=0.45, min_score=0.7, num_matches=2, max_overlap=0.5,
+                                subpixel=True, highest=3, lowest=1)),
+    "border": dict(gen=dict(seed=18, height=400, width=500, tsize=64, n_poses=2, border=34.0),
+                   create=dict(levels=3, angle_start=0.0, angle_extent=0.0),
+                   find=dict(angle_start=0.0, angle_extent=0.0, min_score=0.7, num_matches=2, max_overlap=0.5,
+                             subpixel=True, highest=3, lowest=1)),
+    "no_match": dict(gen=dict(seed=19, height=480, width=640, tsize=64, n_poses=1, noise_sigma=12),
+                     create=dict(levels=3, angle_start=0.0, angle_extent=0.0),
+                     find=dict(angle_start=0.0, angle_extent=0.0, min_score=0.99, num_matches=1, max_overlap=0.5,
+                               subpixel=True, highest=3, lowest=1)),
+    "mask_disc": dict(gen=dict(seed=20, height=480, width=640, tsize=64, n_poses=2, angle_range=(-D(15), D(15))),
+                      create=dict(levels=3, angle_start=-D(15), angle_extent=D(30)),
+                      find=dict(angle_start=-D(15), angle_extent=D(30), min_score=0.7, num_matches=2,
+                                max_overlap=0.5, subpixel=True, highest=3, lowest=1),
+                      mask="disc"),
+    "overlap_tight": dict(gen=dict(seed=21, height=600, width=800, tsize=48, n_poses=4, angle_range=(-D(5), D(5))),
+                          create=dict(levels=3, angle_start=-D(5), angle_extent=D(10)),
+                          find=dict(angle_start=-D(5), angle_extent=D(10), min_score=0.5, num_matches=0,
+                                    max_overlap=0.0, subpixel=True, highest=3, lowest=1)),
+}
+
+# Large single-GPU throughput case, checked against the oracle at full size.
+LARGE = {
+    "cfg2_s1": dict(gen=dict(seed=1, height=2048, width=2048, tsize=128, n_poses=5, angle_range=(-D(30), D(30))),
+                    create=dict(levels=4, angle_start=-D(30), angle_extent=D(60)),
+                    find=dict(angle_start=-D(30), angle_extent=D(60), min_score=0.7, num_matches=5,
+                              max_overlap=0.5, subpixel=True, highest=4, lowest=1)),
+}
+
+
+def make_inputs(case: dict):
+    wl = W.make_workload(**case["gen"])
+    mask = None
+    if case.get("mask") == "disc":
+        import numpy as np
+        t = wl.template.shape[0]
+        yy, xx = np.mgrid[0:t, 0:t]
+        c = (t - 1) / 2.0
+        mask = ((yy - c) ** 2 + (xx - c) ** 2 <= (t / 2.0) ** 2).astype(np.uint8)
+    return wl, mask

@@ -1,0 +1,196 @@
+"""GPU parity: the CUDA find path against the reference's golden matches and the
+oracle restatement, through the C ABI (ctypes) of libmvkit_gb300.so.
+
+Tolerances (final matches): identical count and order, |drow|,|dcol| <= 0.05 px,
+|dangle| <= 0.05 deg, |dscore| <= 1e-4.  Pyramid levels are compared bit-exact.
+Candidate stages are compared as sets of poses (exact FP64 equality of
+row/column/angle): the CUDA path scores windows in FP32 from exact integer
+moments, so a stage may differ from the FP64 oracle only by near-ties."""
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle_lib
+from golden.cases import CASES, LARGE, make_inputs
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = json.loads((Path(__file__).parent / "golden" / "golden.json").read_text())["cases"]
+TOL_PX = 0.05
+TOL_ANGLE = math.radians(0.05)
+TOL_SCORE = 1e-4
+
+
+@pytest.fixture(scope="module")
+def mg():
+    import mvkit_gb300
+    from mvkit_gb300 import build
+    build.build()
+    mvkit_gb300.load()
+    return mvkit_gb300
+
+
+@pytest.fixture(scope="module")
+def orc():
+    return oracle_lib.oracle()
+
+
+def gpu_model(mg, case, wl, mask):
+    c = case["create"]
+    return mg.create_ncc_model(wl.template, c["levels"], c["angle_start"], c["angle_extent"],
+                               c.get("angle_step", "auto") or "auto",
+                               "ignore_global_polarity" if c.get("ignore_polarity") else "use_polarity", domain=mask)
+
+
+def gpu_find(mg, model, image, case, **over):
+    f = dict(case["find"])
+    f.update(over)
+    return mg.find_ncc_model(image, model, f["angle_start"], f["angle_extent"], f["min_score"], f["num_matches"],
+                             f["max_overlap"], "true" if f["subpixel"] else "false", [f["highest"], f["lowest"]])
+
+
+def assert_same_matches(got, want_internal, label=""):
+    want = oracle_lib.to_halcon(np.array(want_internal).reshape(-1, 4))
+    g = np.stack(got, axis=1) if len(got[0]) else np.zeros((0, 4))
+    assert g.shape == want.shape, f"{label}: {len(g)} matches vs reference {len(want)}\n{g}\n{want}"
+    if len(g):
+        d = np.abs(g - want)
+        assert d[:, 0].max() <= TOL_PX and d[:, 1].max() <= TOL_PX, f"{label} position\n{g}\n{want}"
+        assert d[:, 2].max() <= TOL_ANGLE, f"{label} angle\n{g}\n{want}"
+        assert d[:, 3].max() <= TOL_SCORE, f"{label} score\n{g}\n{want}"
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_find_matches_reference(mg, name):
+    case = CASES[name]
+    wl, mask = make_inputs(case)
+    assert wl.digest() == GOLDEN[name]["digest"]
+    model = gpu_model(mg, case, wl, mask)
+    got = gpu_find(mg, model, wl.image, case)
+    assert_same_matches(got, GOLDEN[name]["matches"], name)
+
+
+def test_find_matches_reference_2048(mg):
+    case = LARGE["cfg2_s1"]
+    wl, mask = make_inputs(case)
+    assert wl.digest() == GOLDEN["cfg2_s1"]["digest"]
+    model = gpu_model(mg, case, wl, mask)
+    got = gpu_find(mg, model, wl.image, case)
+    assert_same_matches(got, GOLDEN["cfg2_s1"]["matches"], "cfg2_s1")
+
+
+@pytest.mark.parametrize("seed", [31, 32, 33])
+def test_find_matches_oracle_fresh_seeds(mg, orc, seed):
+    case = dict(gen=dict(seed=seed, height=600, width=800, tsize=64, n_poses=3,
+                         angle_range=(-math.radians(25), math.radians(25))),
+                create=dict(levels=3, angle_start=-math.radians(25), angle_extent=math.radians(50)),
+                find=dict(angle_start=-math.radians(25), angle_extent=math.radians(50), min_score=0.7,
+                          num_matches=3, max_overlap=0.5, subpixel=True, highest=3, lowest=1))
+    wl, mask = make_inputs(case)
+    c, f = case["create"], case["find"]
+    om = orc.create(wl.template, levels=c["levels"], angle_start=c["angle_start"], angle_extent=c["angle_extent"])
+    want = orc.find(om, wl.image, f["angle_start"], f["angle_extent"], f["min_score"], f["num_matches"],
+                    f["max_overlap"], True, 3, 1)
+    got = gpu_find(mg, gpu_model(mg, case, wl, mask), wl.image, case)
+    assert_same_matches(got, want, f"seed {seed}")
+
+
+def test_pyramid_levels_bit_exact(mg, orc):
+    case = CASES["rot_l4_2"]
+    wl, mask = make_inputs(case)
+    model = gpu_model(mg, case, wl, mask)
+    om = orc.create(wl.template, levels=4, angle_start=case["create"]["angle_start"],
+                    angle_extent=case["create"]["angle_extent"])
+    for level in range(4):
+        sums, geom = mg.pyramid_level(wl.image, model, 4, level)
+        ref, rgeom = orc.pyramid(om, wl.image, 4, level)
+        assert sums.shape == ref.shape
+        # the reference's FP64 level value is sum / 4^level - dc, exactly
+        np.testing.assert_array_equal(sums.astype(np.float64) / float(4 ** level) - rgeom[4], ref)
+
+
+def pose_set(a):
+    return {(float(r[0]), float(r[1]), float(r[2])) for r in np.asarray(a).reshape(-1, 4)}
+
+
+@pytest.mark.parametrize("name", ["cfg1_s1", "rot3_all", "rot_l4_2", "u16_rot", "polarity"])
+def test_candidate_stages_match_oracle(mg, orc, name):
+    case = CASES[name]
+    wl, mask = make_inputs(case)
+    c, f = case["create"], case["find"]
+    om = orc.create(wl.template, levels=c["levels"], angle_start=c["angle_start"], angle_extent=c["angle_extent"],
+                    ignore_polarity=c.get("ignore_polarity", False), mask=mask)
+    model = gpu_model(mg, case, wl, mask)
+    ctl = (f["angle_start"], f["angle_extent"], f["min_score"], f["num_matches"], f["max_overlap"],
+           "true" if f["subpixel"] else "false", [f["highest"], f["lowest"]])
+    steps = [0] + list(range(1, f["highest"]))
+    for stage in steps:
+        want = orc.find(om, wl.image, f["angle_start"], f["angle_extent"], f["min_score"], f["num_matches"],
+                        f["max_overlap"], f["subpixel"], f["highest"], f["lowest"], stage=stage)
+        got = mg.find_ncc_model_stage(wl.image, model, *ctl, stage=stage)
+        a, b = pose_set(got), pose_set(want)
+        sym = len(a ^ b)
+        assert sym <= max(2, len(b) // 100), f"{name} stage {stage}: {len(a)} vs {len(b)} candidates, {sym} differ"
+        # scores of the common candidates agree to FP32 precision
+        ws = {(r[0], r[1], r[2]): r[3] for r in want}
+        for r in got:
+            k = (r[0], r[1], r[2])
+            if k in ws:
+                assert abs(r[3] - ws[k]) < 2e-5, f"{name} stage {stage} score {r[3]} vs {ws[k]}"
+    # full-resolution scores of the sorted candidate list
+    want = orc.find(om, wl.image, f["angle_start"], f["angle_extent"], f["min_score"], f["num_matches"],
+                    f["max_overlap"], f["subpixel"], f["highest"], f["lowest"], stage=100)
+    got = mg.find_ncc_model_stage(wl.image, model, *ctl, stage=100)
+    want = want[np.isfinite(want[:, 3])]   # the find loop skips unscorable candidates
+    ws = {(r[0], r[1], r[2]): r[3] for r in want}
+    common = [r for r in got if (r[0], r[1], r[2]) in ws]
+    assert len(common) >= 0.98 * len(want)
+    assert np.all(np.diff(got[:, 3]) <= 0), "sorted by score"
+    for r in common:
+        assert abs(r[3] - ws[(r[0], r[1], r[2])]) < 1e-4
+
+
+def test_device_resident_input_and_repeat_calls(mg):
+    case = CASES["rot3_all"]
+    wl, mask = make_inputs(case)
+    model = gpu_model(mg, case, wl, mask)
+    a = gpu_find(mg, model, wl.image, case)
+    b = gpu_find(mg, model, mg.DeviceImage(wl.image), case)
+    c = gpu_find(mg, model, wl.image, case)
+    for x, y in ((a, b), (a, c)):
+        for u, v in zip(x, y):
+            np.testing.assert_array_equal(u, v)
+
+
+def test_empty_and_errors(mg):
+    case = CASES["cfg1_s1"]
+    wl, mask = make_inputs(case)
+    model = gpu_model(mg, case, wl, mask)
+    r = mg.find_ncc_model(np.zeros((0, 0), np.uint8), model, 0.0, 0.0, 0.8, 1, 0.5, "true", 3)
+    assert all(len(x) == 0 for x in r)
+    with pytest.raises(mg.MvError) as e:
+        mg.find_ncc_model(np.zeros((8001, 4001), np.uint8), model, 0.0, 0.0, 0.8, 1, 0.5, "true", 3)
+    assert e.value.status == -103
+    with pytest.raises(mg.MvError) as e:
+        mg.create_ncc_model(np.full((32, 32), 9, np.uint8))
+    assert e.value.status == -1
+    with pytest.raises(mg.MvError) as e:
+        mg.create_ncc_model(wl.template, num_levels=9)
+    assert e.value.status == -1
+    # query range outside the trained range: no matches, no error
+    r = mg.find_ncc_model(wl.image, model, 1.0, 0.5, 0.8, 1, 0.5, "true", 3)
+    assert all(len(x) == 0 for x in r)
+
+
+def test_model_params(mg):
+    case = CASES["rot3_all"]
+    wl, mask = make_inputs(case)
+    model = gpu_model(mg, case, wl, mask)
+    lv, a0, a1, step, metric = mg.get_ncc_model_params(model)
+    assert lv == GOLDEN["rot3_all"]["levels"]
+    assert a0 == case["create"]["angle_start"] and a1 == case["create"]["angle_extent"]
+    assert step == GOLDEN["rot3_all"]["angle_step"]
+    assert metric == "use_polarity"
