@@ -1,0 +1,323 @@
+"""FindNccModel throughput on one GB300 (or N replicas under torchrun).
+
+Workload "find_2048_t128_5x": 2048x2048 uint8 scenes, one 128x128 template
+pasted at 5 poses each (rotation U[-30 deg, 30 deg], sub-pixel shifts), model
+AngleStart -30 deg, AngleExtent 60 deg, automatic angle step, NumLevels 4;
+FindNccModel MinScore 0.7, NumMatches 5, MaxOverlap 0.5, SubPixel true.
+A step is one find on each of `--batch` distinct scenes.
+
+value: images/s with the scenes resident in HBM (CUDA events on the find
+stream, L2 flushed between steps).  e2e: the same through the C ABI with
+page-locked host buffers (upload and result read-back inside the timed
+region).  roofline: the kernel with the largest event-time share, its
+algorithmic multiply-adds over its live event time.  cpu_baseline: the FP64
+oracle restatement of the reference on this host's cores (one scene per
+thread).
+
+--impl reference: the reference's CPU implementation of the path (the oracle
+port here; the reference itself when it was compiled on this machine), all
+host threads, one scene per thread per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "tests"))
+
+D = math.radians
+WORKLOAD = "find_2048_t128_5x"
+GEN = dict(height=2048, width=2048, tsize=128, n_poses=5, angle_range=(-D(30), D(30)))
+CREATE = dict(num_levels=4, angle_start=-D(30), angle_extent=D(60), angle_step="auto", metric="use_polarity")
+FIND = dict(angle_start=-D(30), angle_extent=D(60), min_score=0.7, num_matches=5, max_overlap=0.5, subpixel="true",
+            num_levels=4)
+METRIC = "FindNccModel images/s at <=0.05px/0.05deg pose error; tensor-core vs plain GPU"
+
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return dict(hbm=d["hbm_gbs"], tflops=d["bf16_tflops"], tflops_sustained=d["bf16_tflops_sustained"],
+                    source="measured")
+    return dict(hbm=6800.0, tflops=1900.0, tflops_sustained=1700.0, source="fallback")
+
+
+def scenes(n: int, template_seed: int = 1):
+    from mvkit_gb300 import workloads as W
+    return [W.make_workload(1000 + i, template_seed=template_seed, **GEN) for i in range(n)]
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while running (200 ms period)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def traffic_from_profiles(kernel: str):
+    """DRAM bytes per launch recorded by the committed ncu summary, if any."""
+    for p in sorted((ROOT / "profiles").glob(f"{kernel}*.md")):
+        m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", p.read_text())
+        if m:
+            return float(m.group(1))
+    return None
+
+
+def cpu_baseline(images, threads: int) -> dict:
+    import oracle_lib
+    orc = oracle_lib.oracle()
+    wl = images[0]
+    model = orc.create(wl.template, levels=CREATE["num_levels"], angle_start=CREATE["angle_start"],
+                       angle_extent=CREATE["angle_extent"])
+    sample = [images[i % len(images)].image for i in range(threads)]
+    t0 = time.perf_counter()
+    n = orc.find_many(model, sample, threads, FIND["angle_start"], FIND["angle_extent"], FIND["min_score"],
+                      FIND["num_matches"], FIND["max_overlap"], True, 4, 1)
+    dt = time.perf_counter() - t0
+    return {"value": len(sample) / dt, "unit": "images/s", "cores": threads, "kind": "port",
+            "sample": f"{len(sample)} scenes of {WORKLOAD}, one per thread, FP64 oracle restatement "
+                      f"of the reference scalar path ({n} matches)", "seconds": dt}
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    images = scenes(min(threads, 8))
+    import oracle_lib
+    orc = oracle_lib.oracle()
+    model = orc.create(images[0].template, levels=4, angle_start=CREATE["angle_start"],
+                       angle_extent=CREATE["angle_extent"])
+    sample = [images[i % len(images)].image for i in range(threads)]
+
+    def step():
+        return orc.find_many(model, sample, threads, FIND["angle_start"], FIND["angle_extent"], FIND["min_score"],
+                             FIND["num_matches"], FIND["max_overlap"], True, 4, 1)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    value = args.steps * len(sample) / dt
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "images/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "scenes_per_step": len(sample), "threads": threads},
+            "cpu_baseline": {"value": value, "unit": "images/s", "cores": threads, "kind": "port",
+                             "sample": f"{len(sample)} scenes per step, one per host thread"},
+            "e2e": {"value": value, "unit": "images/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=8, help="scenes per step")
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    args.warmup = max(args.warmup, 3)
+
+    import torch
+    import mvkit_gb300 as mg
+    from mvkit_gb300 import build
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    build.build()
+    mg.load()
+
+    wls = scenes(args.batch)
+    model = mg.create_ncc_model(wls[0].template, **CREATE)
+    ctl = (FIND["angle_start"], FIND["angle_extent"], FIND["min_score"], FIND["num_matches"], FIND["max_overlap"],
+           FIND["subpixel"], FIND["num_levels"])
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    dev = [mg.DeviceImage(w.image) for w in wls]
+    pinned = []
+    for w in wls:
+        pb = mg.PinnedBuffer(w.image.shape, np.uint8)
+        pb.array[...] = w.image
+        pinned.append(pb)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
+    found = []
+
+    def one_step(images, location_host: bool):
+        out = []
+        for im in images:
+            if location_host:
+                out.append(mg.find_ncc_model(im.array, model, *ctl, stream=sp))
+            else:
+                out.append(mg.find_ncc_model(im, model, *ctl, stream=sp))
+        return out
+
+    def timed(images, host: bool, steps: int):
+        total = 0.0
+        with torch.cuda.stream(stream):
+            for _ in range(steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                if world > 1:
+                    torch.distributed.barrier()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                found[:] = one_step(images, host)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                total += e0.elapsed_time(e1)
+        return total
+
+    for _ in range(args.warmup):
+        one_step(dev, False)
+        one_step(pinned, True)
+    torch.cuda.synchronize()
+
+    mg.profile_reset()
+    mg.profile_enable(True)
+    with ClockSampler(local) as clocks:
+        dev_ms = timed(dev, False, args.steps)
+    mg.profile_enable(False)
+    prof = mg.profile_read()
+    host_ms = timed(pinned, True, args.steps)
+
+    def maxed(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    dev_ms, host_ms = maxed(dev_ms), maxed(host_ms)
+    images = args.steps * args.batch * world
+    value = images / (dev_ms / 1e3)
+    e2e = images / (host_ms / 1e3)
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    stages = {k: v for k, v in prof.items() if k != "finds"}
+    dominant = max(stages, key=lambda k: stages[k]["ms"])
+    d = stages[dominant]
+    pk = peaks()
+    launches_total = sum(v["launches"] for v in stages.values())
+    kernel_names = {"track": "track_kernel", "coarse": "coarse_kernel", "score": "score_kernel",
+                    "refine": "refine_kernel", "sort": "sort_kernel", "select": "select_kernel"}
+    if dominant in ("track", "coarse") and d["launches"]:
+        flops = 2.0 * d["work"] / d["launches"]
+        per_launch_s = d["ms"] / 1e3 / d["launches"]
+        achieved = flops / per_launch_s / 1e12
+        roof = {"bound": "tensor", "achieved": achieved, "peak": pk["tflops_sustained"], "unit": "TFLOP/s",
+                "frac": achieved / pk["tflops_sustained"],
+                "traffic": traffic_from_profiles(kernel_names.get(dominant, dominant)),
+                "kernel": kernel_names.get(dominant, dominant),
+                "note": f"algorithmic correlation FLOPs (2 x MACs) per launch over the launch's event time; peak = "
+                        f"{pk['source']} dense bf16 sustained (no INT8 peak is measured on this pool); the kernel "
+                        f"runs on FP32 CUDA cores"}
+    else:
+        roof = {"bound": "hbm", "achieved": None, "peak": pk["hbm"], "unit": "GB/s", "frac": None,
+                "traffic": traffic_from_profiles(kernel_names.get(dominant, dominant)),
+                "kernel": kernel_names.get(dominant, dominant)}
+    matches = [len(r[0]) for r in found]
+    line = {
+        "metric": METRIC, "value": value, "unit": "images/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "image": "2048x2048 u8", "template": "128x128", "poses": 5,
+                   "angle_range_deg": [-30, 30], "num_levels": 4, "min_score": 0.7, "num_matches": 5,
+                   "max_overlap": 0.5, "scenes_per_step": args.batch, "l2": "flushed (256 MiB write) between steps",
+                   "parallelism": f"replicas x{world}", "path": "plain FP32 CUDA-core correlation"},
+        "e2e": {"value": e2e, "unit": "images/s",
+                "h2d_bytes_per_step": int(sum(w.image.nbytes for w in wls)),
+                "d2h_bytes_per_step": int(args.batch * (4 * 8 * FIND["num_matches"] + 128))},
+        "roofline": roof,
+        "gpu_launches": int(launches_total),
+        "clocks": clocks.summary(),
+        "stages_ms_per_find": {k: round(v["ms"] / max(1, prof["finds"]), 4) for k, v in stages.items()},
+        "matches_per_scene": matches,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(wls, os.cpu_count() or 1)
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

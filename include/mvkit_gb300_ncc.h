@@ -101,6 +101,17 @@ MVG_API int32_t mvg_ncc_pyramid_level(const void* pixels, int32_t pixel_type, in
 /* Thread-local message of the last failed call (empty after success). */
 MVG_API const char* mvg_last_error(void);
 
+/* Per-thread stage profile of finds on this thread: CUDA events recorded on
+ * the find's stream around each kernel group while enabled.  Stages 0..10:
+ * upload, pyramid, prefix, coarse, nms, track, dedup, score, sort, select,
+ * refine.  ms: summed event time; launches: kernels launched (counted also
+ * while disabled); work: algorithmic multiply-adds (coarse, track) or
+ * bilinear taps (score); finds: completed finds since the last reset. */
+MVG_API int32_t mvg_profile_enable(int32_t on);
+MVG_API int32_t mvg_profile_reset(void);
+MVG_API int32_t mvg_profile_read(int32_t stage, const char** name, double* ms, int64_t* launches, double* work,
+                                 int64_t* finds);
+
 /* Page-locked host buffers for zero-staging uploads, and device buffers for
  * callers without their own allocator. */
 MVG_API int32_t mvg_host_alloc(size_t bytes, void** ptr);

@@ -1,6 +1,8 @@
 """GB300-native NCC template matching (mvkit FindNccModel / CreateNccModel)."""
 from .ncc import (MvError, NccModel, DeviceImage, PinnedBuffer, create_ncc_model, find_ncc_model,
-                  find_ncc_model_stage, get_ncc_model_params, load, pyramid_level)
+                  find_ncc_model_stage, get_ncc_model_params, load, profile_enable, profile_read, profile_reset,
+                  pyramid_level)
 
 __all__ = ["MvError", "NccModel", "DeviceImage", "PinnedBuffer", "create_ncc_model", "find_ncc_model",
-           "find_ncc_model_stage", "get_ncc_model_params", "load", "pyramid_level"]
+           "find_ncc_model_stage", "get_ncc_model_params", "load", "profile_enable", "profile_read",
+           "profile_reset", "pyramid_level"]

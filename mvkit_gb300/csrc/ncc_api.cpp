@@ -305,6 +305,74 @@ Workspace& workspace() {
   return *t_workspace;
 }
 
+// Per-thread stage profile: CUDA events on the find's stream around each
+// kernel group (only while enabled), launch counts and algorithmic work.
+enum Stage { kStUpload, kStPyramid, kStPrefix, kStCoarse, kStNms, kStTrack, kStDedup, kStScore, kStSort, kStSelect,
+             kStRefine, kStages };
+const char* const kStageNames[kStages] = {"upload", "pyramid", "prefix", "coarse", "nms", "track",
+                                          "dedup", "score", "sort", "select", "refine"};
+struct Profiler {
+  bool on = false;
+  struct Mark {
+    int stage;
+    cudaEvent_t a, b;
+  };
+  std::vector<cudaEvent_t> pool;
+  size_t used = 0;
+  std::vector<Mark> marks;
+  double ms[kStages] = {};
+  int64_t launches[kStages] = {};
+  double work[kStages] = {};
+  int64_t finds = 0;
+  ~Profiler() {
+    for (cudaEvent_t e : pool) cudaEventDestroy(e);
+  }
+  cudaEvent_t event() {
+    if (used == pool.size()) {
+      cudaEvent_t e;
+      check(cudaEventCreate(&e), "cudaEventCreate");
+      pool.push_back(e);
+    }
+    return pool[used++];
+  }
+  int open(int stage, cudaStream_t s) {
+    if (!on) return -1;
+    Mark m{stage, event(), event()};
+    check(cudaEventRecord(m.a, s), "cudaEventRecord");
+    marks.push_back(m);
+    return int(marks.size()) - 1;
+  }
+  void close(int i, cudaStream_t s) {
+    if (i >= 0) check(cudaEventRecord(marks[size_t(i)].b, s), "cudaEventRecord");
+  }
+  // after the stream has synchronised
+  void collect() {
+    for (const Mark& m : marks) {
+      float t = 0;
+      if (cudaEventElapsedTime(&t, m.a, m.b) == cudaSuccess) ms[m.stage] += t;
+    }
+    marks.clear();
+    used = 0;
+  }
+  void reset() {
+    marks.clear();
+    used = 0;
+    for (int i = 0; i < kStages; ++i) ms[i] = 0, launches[i] = 0, work[i] = 0;
+    finds = 0;
+  }
+};
+thread_local Profiler t_prof;
+
+struct Span {
+  int index;
+  cudaStream_t stream;
+  Span(int stage, cudaStream_t s, int nlaunch = 1) : stream(s) {
+    index = t_prof.open(stage, s);
+    t_prof.launches[stage] += nlaunch;
+  }
+  ~Span() { t_prof.close(index, stream); }
+};
+
 struct Match {
   double row, col, angle, score;
 };
@@ -317,6 +385,8 @@ struct FindOutput {
 constexpr double kMissing = -std::numeric_limits<double>::infinity();
 
 void fetch_stage(Workspace& ws, cudaStream_t s, const Cand* src, int slot, FindOutput& out) {
+  t_prof.marks.clear();
+  t_prof.used = 0;
   check(cudaMemcpyAsync(ws.h_state, ws.state.p, sizeof(QueryState), cudaMemcpyDeviceToHost, s), "state");
   check(cudaStreamSynchronize(s), "sync");
   const int n = slot < 0 ? ws.h_state->sorted_count : std::min(ws.h_state->count[slot], kMaxCandidates);
@@ -452,6 +522,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   if (location == MVG_MEMORY_HOST) {
     const size_t bytes = size_t(stride) * size_t(H - 1) + size_t(W * bpp);
     ws.image.reserve(bytes);
+    Span sp(kStUpload, s, 0);
     check(cudaMemcpyAsync(ws.image.p, pixels, bytes, cudaMemcpyHostToDevice, s), "image upload");
     dev_pixels = ws.image.p;
   }
@@ -487,14 +558,18 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   }
   QueryState* st = ws.state.p;
   int32_t* err_flag = &st->error;
-  check(launch_pyramid0(dev_pixels, type, pitch_elems, int(crop_row), int(crop_col), lev[0], err_flag, s), "pyramid0");
-  for (size_t l = 1; l < level_count; ++l) check(launch_pyramid(lev[l - 1], lev[l], err_flag, s), "pyramid");
+  {
+    Span sp(kStPyramid, s, int(level_count));
+    check(launch_pyramid0(dev_pixels, type, pitch_elems, int(crop_row), int(crop_col), lev[0], err_flag, s), "pyramid0");
+    for (size_t l = 1; l < level_count; ++l) check(launch_pyramid(lev[l - 1], lev[l], err_flag, s), "pyramid");
+  }
   const size_t first_target = std::max(finest, size_t(opt.subpixel ? 1 : 0));
   for (size_t l = 0; l < level_count; ++l) {
     const bool need = l == top || (l + 1 <= top && l >= first_target);
     if (!need) continue;
     ws.lev_p[l].reserve(size_t(lw[l] + 1) * size_t(lh[l]));
     lev[l].prefix = ws.lev_p[l].p;
+    Span sp(kStPrefix, s);
     check(launch_prefix(lev[l], s), "prefix");
   }
 
@@ -516,9 +591,17 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     ca.nplist = nplist;
     ca.planes = ws.planes.p;
     ca.absolute = hm.params.ignore_polarity;
-    const cudaError_t e = launch_coarse(ca, max_bh, max_bw, s, ws.smem_optin);
-    if (e == cudaErrorInvalidConfiguration) raise(kUnsupported, "coarse template raster exceeds on-chip tile");
-    check(e, "coarse");
+    {
+      Span sp(kStCoarse, s);
+      const cudaError_t e = launch_coarse(ca, max_bh, max_bw, s, ws.smem_optin);
+      if (e == cudaErrorInvalidConfiguration) raise(kUnsupported, "coarse template raster exceeds on-chip tile");
+      check(e, "coarse");
+    }
+    for (int k = 0; k < nplist; ++k) {
+      const PosRange& rg = plan[top].ranges[size_t(k)];
+      t_prof.work[kStCoarse] += double(std::max(0, rg.r1 - rg.r0)) * double(std::max(0, rg.c1 - rg.c0)) *
+                                double(top_desc[size_t(plan[top].plist[size_t(k)])].n);
+    }
     NmsArgs na;
     na.planes = ws.planes.p;
     na.nplist = nplist;
@@ -534,6 +617,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     na.out = ws.cand_a.p;
     na.state = st;
     na.max_candidates = kMaxCandidates;
+    Span sp(kStNms, s);
     check(launch_nms(na, s), "nms");
   }
   if (stage == 0) {
@@ -566,6 +650,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
       ta.offset = (ta.step - 1) * .5;
       ta.angle_limit = hm.params.angle_step * double(l == top ? angle_stride : 1) * 1.01;
       ta.absolute = hm.params.ignore_polarity;
+      Span sp(kStTrack, s);
       check(launch_track(ta, kMaxCandidates, s), "track");
     }
     check(cudaMemsetAsync(ws.table.p, 0xff, sizeof(int) * kHashSlots, s), "memset");
@@ -580,7 +665,10 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     da.snap = snap;
     da.height = Hd;
     da.width = Wd;
-    check(launch_dedup(da, kMaxCandidates, s), "dedup");
+    {
+      Span sp(kStDedup, s, snap ? 2 : 1);
+      check(launch_dedup(da, kMaxCandidates, s), "dedup");
+    }
     std::swap(cur, nxt);
     ++slot;
     ++step_no;
@@ -606,12 +694,16 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     sa.scale = fscale;
     sa.phase = fphase;
     sa.absolute = hm.params.ignore_polarity;
-    check(launch_score(sa, kMaxCandidates, s), "score");
+    {
+      Span sp(kStScore, s);
+      check(launch_score(sa, kMaxCandidates, s), "score");
+    }
     SortArgs so;
     so.in = cur;
     so.out = ws.sorted.p;
     so.state = st;
     so.slot = slot;
+    Span sp(kStSort, s);
     check(launch_sort(so, s), "sort");
   }
   if (stage == 100) {
@@ -664,15 +756,28 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   ra.finest = int(finest);
   ra.height = Hd;
   ra.width = Wd;
-  check(launch_select(se, s), "select");
-  for (int round = 0; round < 100000; ++round) {
-    check(launch_refine(ra, batch_limit, s), "refine");
+  {
+    Span sp(kStSelect, s);
     check(launch_select(se, s), "select");
+  }
+  for (int round = 0; round < 100000; ++round) {
+    {
+      Span sp(kStRefine, s);
+      check(launch_refine(ra, batch_limit, s), "refine");
+    }
+    {
+      Span sp(kStSelect, s);
+      check(launch_select(se, s), "select");
+    }
     check(cudaMemcpyAsync(ws.h_state, st, sizeof(QueryState), cudaMemcpyDeviceToHost, s), "state");
     check(cudaStreamSynchronize(s), "find");
     if (ws.h_state->done || !ws.h_state->need) break;
   }
   const QueryState hs = *ws.h_state;
+  t_prof.collect();
+  t_prof.finds += 1;
+  t_prof.work[kStTrack] += double(hs.track_macs);
+  t_prof.work[kStScore] += double(hs.count[slot]) * double(orig.n);
   if (hs.overflow) raise(kLimitExceeded, "coarse candidate budget exceeded");
   if (hs.error) raise(hs.error, "pyramid sums exceed the exact float range");
   std::vector<Cand> acc(size_t(hs.accepted));
@@ -875,6 +980,26 @@ int32_t mvg_ncc_pyramid_level(const void* pixels, int32_t pixel_type, int64_t wi
 }
 
 const char* mvg_last_error(void) { return g_last_error.c_str(); }
+
+int32_t mvg_profile_enable(int32_t on) {
+  return guarded([&] { t_prof.on = on != 0; });
+}
+
+int32_t mvg_profile_reset(void) {
+  return guarded([&] { t_prof.reset(); });
+}
+
+int32_t mvg_profile_read(int32_t stage, const char** name, double* ms, int64_t* launches, double* work,
+                         int64_t* finds) {
+  return guarded([&] {
+    if (stage < 0 || stage >= kStages) raise(kInvalidArgument, "stage out of range");
+    if (name) *name = kStageNames[stage];
+    if (ms) *ms = t_prof.ms[stage];
+    if (launches) *launches = t_prof.launches[stage];
+    if (work) *work = t_prof.work[stage];
+    if (finds) *finds = t_prof.finds;
+  });
+}
 
 int32_t mvg_host_alloc(size_t bytes, void** ptr) {
   return guarded([&] { check(cudaMallocHost(ptr, bytes), "cudaMallocHost"); });

@@ -6,8 +6,9 @@
 // the "variance <= 0 -> no score" rule of the reference is decided exactly.
 // The template dot product sum(w * (S - S_first)) runs in FP32 on the CUDA
 // cores; the full-resolution score and the Gauss-Newton moments accumulate in
-// FP32 per thread and combine in FP64.  Poses are FP64 with the reference's
-// expressions (no contraction: __dadd_rn/__dmul_rn).
+// FP32 per thread and combine as FP32 two-sum pairs, finished in FP64 on one
+// thread.  Poses are FP64 with the reference's expressions (no contraction:
+// __dadd_rn/__dmul_rn).
 #include <cuda_runtime.h>
 
 #include <cfloat>
@@ -243,6 +244,7 @@ __global__ void __launch_bounds__(256) track_kernel(TrackArgs a) {
     const int j = sel[k];
     const PatchDesc pd = a.view.patches[a.plist[j]];
     const PosRange rg = a.ranges[j];
+    if (lane == 0) atomicAdd(&a.state->track_macs, 25ull * (unsigned long long)pd.n);
     const int row = int(round(dsub(dsub(dsub(cd.row, a.crop_row), a.offset) / a.step, pd.orow)));
     const int col = int(round(dsub(dsub(dsub(cd.col, a.crop_col), a.offset) / a.step, pd.ocol)));
     const int r = row + dr, c = col + dc;

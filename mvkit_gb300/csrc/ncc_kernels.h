@@ -52,7 +52,7 @@ struct TrackArgs {
   int nplist;
   const Cand* in;
   Cand* out;
-  const QueryState* state;
+  QueryState* state;
   int in_slot;              // state->count index holding the input count
   double crop_row, crop_col, step, offset, angle_limit;
   int absolute;

@@ -77,6 +77,8 @@ struct QueryState {
   int32_t need;                    // 1: refinement results missing for `next`
   int32_t done;
   int32_t batch_count;             // entries in the refinement batch
+  int32_t pad_;
+  unsigned long long track_macs;   // algorithmic MACs of the tracking steps (25 positions x samples per patch)
 };
 
 }  // namespace mvg

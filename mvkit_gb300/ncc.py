@@ -76,6 +76,11 @@ def load() -> C.CDLL:
     lib.mvg_device_alloc.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
     lib.mvg_device_free.argtypes = [C.c_void_p]
     lib.mvg_copy_to_device.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
+    lib.mvg_profile_enable.argtypes = [C.c_int32]
+    lib.mvg_profile_reset.argtypes = []
+    lib.mvg_profile_read.argtypes = [C.c_int32, C.POINTER(C.c_char_p), _dp, _i64p, _dp, _i64p]
+    for name in ("mvg_profile_enable", "mvg_profile_reset", "mvg_profile_read"):
+        getattr(lib, name).restype = C.c_int32
     for name in ("mvg_create_ncc_model", "mvg_get_ncc_model_params", "mvg_clear_ncc_model", "mvg_find_ncc_model",
                  "mvg_find_ncc_model_stage", "mvg_ncc_pyramid_level", "mvg_host_alloc", "mvg_host_free",
                  "mvg_device_alloc", "mvg_device_free", "mvg_copy_to_device"):
@@ -345,3 +350,31 @@ class PinnedBuffer:
                 self.ptr = None
         except Exception:
             pass
+
+
+PROFILE_STAGES = 11
+
+
+def profile_enable(on: bool = True) -> None:
+    """Per-thread stage timing of finds (CUDA events on the find's stream)."""
+    _check(load().mvg_profile_enable(1 if on else 0), "profile")
+
+
+def profile_reset() -> None:
+    _check(load().mvg_profile_reset(), "profile")
+
+
+def profile_read() -> dict:
+    """{stage: {ms, launches, work}} plus 'finds' for this thread's finds since the last reset."""
+    out = {}
+    finds = 0
+    for i in range(PROFILE_STAGES):
+        name = C.c_char_p()
+        ms, work = C.c_double(), C.c_double()
+        launches, nf = C.c_int64(), C.c_int64()
+        _check(load().mvg_profile_read(i, C.byref(name), C.byref(ms), C.byref(launches), C.byref(work), C.byref(nf)),
+               "profile")
+        out[name.value.decode()] = dict(ms=ms.value, launches=launches.value, work=work.value)
+        finds = nf.value
+    out["finds"] = finds
+    return out

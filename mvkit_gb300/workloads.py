@@ -156,7 +156,8 @@ def _finish(img: np.ndarray, rng: np.random.Generator, noise_sigma: int, maxval:
 def make_workload(seed: int, height: int, width: int, tsize: int, n_poses: int,
                   angle_range: tuple = (0.0, 0.0), noise_sigma: int = 3, shapes: int = 40,
                   maxval: int = 255, contrast: float = 0.0, subpixel: bool = True,
-                  invert_odd: bool = False, border: float | None = None) -> Workload:
+                  invert_odd: bool = False, border: float | None = None,
+                  template_seed: int | None = None) -> Workload:
     """One search scene with `n_poses` pastes of one square template of side `tsize`.
 
     angle_range is in radians; contrast > 0 scales each paste by U[1-c, 1+c];
@@ -165,13 +166,16 @@ def make_workload(seed: int, height: int, width: int, tsize: int, n_poses: int,
     half the diagonal + 8) away from the image edge.
     """
     dtype = np.uint8 if maxval <= 255 else np.uint16
-    rng = np.random.default_rng([seed, 1])
-    src = scene(seed * 7919 + 17, max(2 * tsize, 64), max(2 * tsize, 64), shapes=max(8, shapes // 4),
+    tseed = seed if template_seed is None else template_seed
+    rng = np.random.default_rng([tseed, 1])
+    src = scene(tseed * 7919 + 17, max(2 * tsize, 64), max(2 * tsize, 64), shapes=max(8, shapes // 4),
                 maxval=maxval)
     ty = int(rng.integers(0, src.shape[0] - tsize + 1))
     tx = int(rng.integers(0, src.shape[1] - tsize + 1))
     tmpl_i = src[ty:ty + tsize, tx:tx + tsize]
     tmpl_i = np.clip(tmpl_i + _gauss_int(rng, tmpl_i.shape, noise_sigma), 0, maxval)
+    if template_seed is not None:
+        rng = np.random.default_rng([seed, 2])  # scene poses and noise of this scene
     img = scene(seed, height, width, shapes=shapes, maxval=maxval)
     diag = math.hypot(tsize, tsize)
     margin = diag / 2.0 + 8 if border is None else float(border)
