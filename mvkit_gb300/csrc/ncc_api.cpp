@@ -63,9 +63,11 @@ struct DevLevel {
   size_t model_patches = 0;         // trained patches; endpoints follow
   std::vector<int32_t> offs, runs, runs_end;
   std::vector<float> w;
+  std::vector<int2> sw;
   DevBuf<PatchDesc> d_desc;
   DevBuf<int32_t> d_offs, d_runs, d_runs_end;
   DevBuf<float> d_w;
+  DevBuf<int2> d_sw;
   void append(const Raster& r) {
     PatchDesc d{};
     d.angle = r.angle;
@@ -80,8 +82,13 @@ struct DevLevel {
     d.nruns = int32_t(r.run_row.size());
     d.run_off = int32_t(runs.size());
     for (size_t i = 0; i < r.size(); ++i) {
-      offs.push_back(int32_t((uint32_t(uint16_t(int16_t(r.rows[i]))) << 16) | uint16_t(int16_t(r.cols[i]))));
-      w.push_back(float(r.w[i]));
+      const int32_t o = int32_t((uint32_t(uint16_t(int16_t(r.rows[i]))) << 16) | uint16_t(int16_t(r.cols[i])));
+      const float wf = float(r.w[i]);
+      int32_t wbits;
+      std::memcpy(&wbits, &wf, sizeof(wbits));
+      offs.push_back(o);
+      w.push_back(wf);
+      sw.push_back(make_int2(o, wbits));
     }
     for (size_t j = 0; j < r.run_row.size(); ++j) {
       runs.push_back(int32_t((uint32_t(uint16_t(int16_t(r.run_row[j]))) << 16) | uint16_t(int16_t(r.run_begin[j]))));
@@ -107,7 +114,9 @@ struct DevLevel {
     retire(d_runs);
     retire(d_runs_end);
     retire(d_w);
+    retire(d_sw);
     d_desc.upload(desc, nullptr);
+    d_sw.upload(sw, nullptr);
     d_offs.upload(offs, nullptr);
     d_runs.upload(runs, nullptr);
     d_runs_end.upload(runs_end, nullptr);
@@ -119,6 +128,7 @@ struct DevLevel {
     v.patches = d_desc.p;
     v.offs = d_offs.p;
     v.w = d_w.p;
+    v.sw = d_sw.p;
     v.runs = d_runs.p;
     v.runs_end = d_runs_end.p;
     v.npatches = int32_t(desc.size());
@@ -236,7 +246,17 @@ void pose_interval(int& lo, int& hi, double crop, double step, double o, double 
 struct LevelPlan {
   std::vector<int32_t> plist;  // query patch order
   std::vector<PosRange> ranges;
+  // tracking into this level: plist entries inside the angle window of each
+  // source patch of the next coarser level (CSR by source patch index)
+  std::vector<int32_t> sel_off, sel_idx;
 };
+
+// True when a value is a multiple of 2^-4 of magnitude <= 2048: then every
+// lattice expression of the tracking step is exact in FP32.
+bool lattice_exact32(double v) {
+  const double s = v * 16;
+  return std::abs(v) <= 2048 && s == std::floor(s);
+}
 
 // ------------------------------------------------------------- workspace
 struct Workspace {
@@ -247,6 +267,7 @@ struct Workspace {
   DevBuf<longlong2> lev_p[kMaxLevels];
   DevBuf<float> planes;
   DevBuf<Cand> cand_a, cand_b, tmp, sorted, accepted;
+  DevBuf<RectAux> aux, accepted_aux;
   DevBuf<int> table;
   DevBuf<Refined> refined;
   DevBuf<int32_t> refined_flag, batch;
@@ -277,6 +298,8 @@ struct Workspace {
     tmp.reserve(kMaxCandidates);
     sorted.reserve(kMaxCandidates);
     accepted.reserve(kMaxCandidates);
+    aux.reserve(kMaxCandidates);
+    accepted_aux.reserve(kMaxCandidates);
     table.reserve(kHashSlots);
     refined.reserve(kMaxCandidates);
     refined_flag.reserve(kMaxCandidates);
@@ -510,6 +533,29 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     }
   }
 
+  // angle windows of the tracking steps (matcher.cpp:680): for target level
+  // t, the source is level t+1; the first step from the top level widens the
+  // window by the coarse angle stride
+  bool exact32 = std::max(W, H) <= 8192 && level_count <= 5;
+  for (size_t t = 0; t + 1 < level_count; ++t) {
+    const DevLevel& S = *m.levels[t + 1];
+    const DevLevel& T = *m.levels[t];
+    const double limit = hm.params.angle_step * double(t + 1 == top ? angle_stride : 1) * 1.01;
+    auto& off = plan[t].sel_off;
+    auto& idx = plan[t].sel_idx;
+    off.assign(S.desc.size() + 1, 0);
+    for (size_t src = 0; src < S.desc.size(); ++src) {
+      off[src] = int32_t(idx.size());
+      for (size_t j = 0; j < plan[t].plist.size(); ++j)
+        if (!(std::abs(T.angles[size_t(plan[t].plist[j])] - S.angles[src]) > limit)) idx.push_back(int32_t(j));
+    }
+    off[S.desc.size()] = int32_t(idx.size());
+  }
+  for (size_t li = 0; li < level_count && exact32; ++li)
+    for (int32_t p : plan[li].plist) {
+      const PatchDesc& d = m.levels[li]->desc[size_t(p)];
+      if (!lattice_exact32(d.orow) || !lattice_exact32(d.ocol)) exact32 = false;
+    }
   const size_t finest_level = finest;
   const OriginalView orig = finest_level ? coarse_original(m, finest_level).view() : m.original.view();
   for (size_t li = 0; li < level_count; ++li) views[li] = m.levels[li]->view();
@@ -528,21 +574,31 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   }
   const int32_t* d_plist[kMaxLevels];
   const PosRange* d_ranges[kMaxLevels];
+  const int32_t* d_sel_off[kMaxLevels];
+  const int32_t* d_sel_idx[kMaxLevels];
   {
     size_t total = 0;
-    std::vector<size_t> at(2 * level_count);
+    std::vector<size_t> at(4 * level_count);
+    auto reserve = [&](size_t k, size_t bytes) {
+      at[k] = total;
+      total += (bytes + 15) & ~size_t(15);
+    };
     for (size_t li = 0; li < level_count; ++li) {
-      at[2 * li] = total;
-      total += (plan[li].plist.size() * sizeof(int32_t) + 15) & ~size_t(15);
-      at[2 * li + 1] = total;
-      total += (plan[li].ranges.size() * sizeof(PosRange) + 15) & ~size_t(15);
+      reserve(4 * li, plan[li].plist.size() * sizeof(int32_t));
+      reserve(4 * li + 1, plan[li].ranges.size() * sizeof(PosRange));
+      reserve(4 * li + 2, plan[li].sel_off.size() * sizeof(int32_t));
+      reserve(4 * li + 3, plan[li].sel_idx.size() * sizeof(int32_t));
     }
     uint8_t* h = ws.stage_tables(std::max<size_t>(total, 16));
     for (size_t li = 0; li < level_count; ++li) {
-      std::memcpy(h + at[2 * li], plan[li].plist.data(), plan[li].plist.size() * sizeof(int32_t));
-      std::memcpy(h + at[2 * li + 1], plan[li].ranges.data(), plan[li].ranges.size() * sizeof(PosRange));
-      d_plist[li] = reinterpret_cast<const int32_t*>(ws.tables.p + at[2 * li]);
-      d_ranges[li] = reinterpret_cast<const PosRange*>(ws.tables.p + at[2 * li + 1]);
+      std::memcpy(h + at[4 * li], plan[li].plist.data(), plan[li].plist.size() * sizeof(int32_t));
+      std::memcpy(h + at[4 * li + 1], plan[li].ranges.data(), plan[li].ranges.size() * sizeof(PosRange));
+      std::memcpy(h + at[4 * li + 2], plan[li].sel_off.data(), plan[li].sel_off.size() * sizeof(int32_t));
+      std::memcpy(h + at[4 * li + 3], plan[li].sel_idx.data(), plan[li].sel_idx.size() * sizeof(int32_t));
+      d_plist[li] = reinterpret_cast<const int32_t*>(ws.tables.p + at[4 * li]);
+      d_ranges[li] = reinterpret_cast<const PosRange*>(ws.tables.p + at[4 * li + 1]);
+      d_sel_off[li] = reinterpret_cast<const int32_t*>(ws.tables.p + at[4 * li + 2]);
+      d_sel_idx[li] = reinterpret_cast<const int32_t*>(ws.tables.p + at[4 * li + 3]);
     }
     check(cudaMemcpyAsync(ws.tables.p, h, total, cudaMemcpyHostToDevice, s), "tables");
   }
@@ -613,7 +669,14 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     na.crop_col = double(crop_col);
     na.scale = scale;
     na.phase = phase;
-    na.threshold = opt.min_score * .4;
+    {
+      // smallest float whose double value is >= 0.4*MinScore (the
+      // reference's FP64 comparison, matcher.cpp:582)
+      const double thr = opt.min_score * .4;
+      float f = float(thr);
+      if (double(f) < thr) f = std::nextafter(f, std::numeric_limits<float>::infinity());
+      na.threshold = f;
+    }
     na.out = ws.cand_a.p;
     na.state = st;
     na.max_candidates = kMaxCandidates;
@@ -644,11 +707,13 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
       ta.out = ws.tmp.p;
       ta.state = st;
       ta.in_slot = slot;
+      ta.sel_off = d_sel_off[t];
+      ta.sel_idx = d_sel_idx[t];
       ta.crop_row = double(crop_row);
       ta.crop_col = double(crop_col);
       ta.step = std::ldexp(1., int(t));
       ta.offset = (ta.step - 1) * .5;
-      ta.angle_limit = hm.params.angle_step * double(l == top ? angle_stride : 1) * 1.01;
+      ta.exact32 = exact32;
       ta.absolute = hm.params.ignore_polarity;
       Span sp(kStTrack, s);
       check(launch_track(ta, kMaxCandidates, s), "track");
@@ -713,21 +778,26 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
 
   // greedy selection with refinement (matcher.cpp:1063-1076)
   check(cudaMemsetAsync(ws.refined_flag.p, 0, sizeof(int32_t) * kMaxCandidates, s), "memset");
-  const int batch_limit = int(std::min<int64_t>(64, opt.num_matches > 0 ? opt.num_matches + 4 : 32));
+  const int batch_limit = int(std::min<int64_t>(64, opt.num_matches > 0 ? 2 * opt.num_matches + 6 : 32));
+  RectGeom geom;
+  geom.left = -base.ocol - .5;
+  geom.right = double(base.width) - base.ocol - .5;
+  geom.top = -base.orow - .5;
+  geom.bottom = double(base.height) - base.orow - .5;
+  geom.area = double(base.width) * double(base.height);
   SelectArgs se;
   se.sorted = ws.sorted.p;
+  se.aux = ws.aux.p;
   se.refined = ws.refined.p;
   se.refined_flag = ws.refined_flag.p;
   se.batch = ws.batch.p;
   se.accepted = ws.accepted.p;
+  se.accepted_aux = ws.accepted_aux.p;
   se.state = st;
   se.batch_limit = batch_limit;
   se.num_matches = opt.num_matches;
   se.max_overlap = opt.max_overlap;
-  se.tmpl_w = double(base.width);
-  se.tmpl_h = double(base.height);
-  se.tmpl_orow = base.orow;
-  se.tmpl_ocol = base.ocol;
+  se.geom = geom;
   RefineArgs ra;
   ra.img = fine;
   ra.orig = orig;
@@ -756,8 +826,10 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   ra.finest = int(finest);
   ra.height = Hd;
   ra.width = Wd;
+  ra.geom = geom;
   {
-    Span sp(kStSelect, s);
+    Span sp(kStSelect, s, 2);
+    check(launch_rects(ws.sorted.p, ws.aux.p, st, geom, kMaxCandidates, s), "rects");
     check(launch_select(se, s), "select");
   }
   for (int round = 0; round < 100000; ++round) {

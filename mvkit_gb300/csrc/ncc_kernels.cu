@@ -5,10 +5,14 @@
 // prefix sums, so the variance numerator n*sum(S^2) - (sum S)^2 is exact and
 // the "variance <= 0 -> no score" rule of the reference is decided exactly.
 // The template dot product sum(w * (S - S_first)) runs in FP32 on the CUDA
-// cores; the full-resolution score and the Gauss-Newton moments accumulate in
-// FP32 per thread and combine as FP32 two-sum pairs, finished in FP64 on one
-// thread.  Poses are FP64 with the reference's expressions (no contraction:
-// __dadd_rn/__dmul_rn).
+// cores.  The full-resolution score and the Gauss-Newton moments accumulate
+// in FP32 per thread and combine as FP32 (hi, lo) two-sum pairs; the 3x3
+// normal equations are solved in FP64 on one thread.
+//
+// sm_103 issues FP64 at a small fraction of the FP32 rate, so FP64 appears
+// only where the reference's decisions need it: pose lattice arithmetic (or
+// an FP32 form the host proved exact), the normal-equation solve, and the
+// rectangle overlap of the MaxOverlap rule.
 #include <cuda_runtime.h>
 
 #include <cfloat>
@@ -34,6 +38,41 @@ __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a,
 __device__ __forceinline__ double lattice_pose(double crop, double step, int r, double o, double off) {
   return dadd(dadd(crop, dmul(step, dadd(double(r), o))), off);
 }
+__device__ __forceinline__ float lattice_pose32(float crop, float step, int r, float o, float off) {
+  return __fadd_rn(__fadd_rn(crop, __fmul_rn(step, __fadd_rn(float(r), o))), off);
+}
+
+// ------------------------------------------------------- FP32 pair arithmetic
+struct F2 {
+  float hi, lo;
+};
+__device__ __forceinline__ F2 f2(float x) { return F2{x, 0.f}; }
+__device__ __forceinline__ F2 f2_add(F2 x, F2 y) {
+  const float s = __fadd_rn(x.hi, y.hi);
+  const float bb = __fsub_rn(s, x.hi);
+  const float e = __fadd_rn(__fadd_rn(__fsub_rn(x.hi, __fsub_rn(s, bb)), __fsub_rn(y.hi, bb)), __fadd_rn(x.lo, y.lo));
+  const float h = __fadd_rn(s, e);
+  return F2{h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+__device__ __forceinline__ F2 f2_neg(F2 x) { return F2{-x.hi, -x.lo}; }
+__device__ __forceinline__ F2 f2_sub(F2 x, F2 y) { return f2_add(x, f2_neg(y)); }
+__device__ __forceinline__ F2 f2_mul(F2 x, F2 y) {
+  const float p = __fmul_rn(x.hi, y.hi);
+  float e = __fmaf_rn(x.hi, y.hi, -p);
+  e = __fmaf_rn(x.hi, y.lo, e);
+  e = __fmaf_rn(x.lo, y.hi, e);
+  const float h = __fadd_rn(p, e);
+  return F2{h, __fsub_rn(e, __fsub_rn(h, p))};
+}
+__device__ __forceinline__ F2 f2_div(F2 x, F2 y) {
+  const float q1 = __fdiv_rn(x.hi, y.hi);
+  const F2 r = f2_sub(x, f2_mul(f2(q1), y));
+  const float q2 = __fdiv_rn(r.hi, y.hi);
+  const float h = __fadd_rn(q1, q2);
+  return F2{h, __fsub_rn(q2, __fsub_rn(h, q1))};
+}
+__device__ __forceinline__ float f2_val(F2 x) { return x.hi + x.lo; }
+__device__ __forceinline__ double f2_dbl(F2 x) { return double(x.hi) + double(x.lo); }
 
 // Score of one window from the FP32 template dot and exact integer moments.
 // D = sum w (S - S0) relates to the reference's sum w q by a 4^k factor that
@@ -42,8 +81,11 @@ __device__ __forceinline__ double lattice_pose(double crop, double step, int r, 
 __device__ __forceinline__ float window_score(float dot, long long s1, long long s2, int n, int absolute) {
   const __int128 v = (__int128)n * s2 - (__int128)s1 * s1;
   if (v <= 0) return -INFINITY;
-  const float vn = float((double)(long long)v) / float(n);
-  float s = dot * rsqrtf(vn);
+  const long long hi = (long long)(v >> 62);
+  const float vf = hi ? __ll2float_rn(hi) * 4.611686018427387904e18f +
+                            __ull2float_rn((unsigned long long)(v & ((((__int128)1) << 62) - 1)))
+                      : __ll2float_rn((long long)v);
+  float s = dot * rsqrtf(vf / float(n));
   s = fminf(1.f, fmaxf(-1.f, s));
   return absolute ? fabsf(s) : s;
 }
@@ -62,6 +104,11 @@ __device__ __forceinline__ void window_moments(const longlong2* __restrict__ P, 
     s1 += hi.x - lo.x;
     s2 += hi.y - lo.y;
   }
+}
+
+// (score, order) with the first strict maximum in iteration order winning
+__device__ __forceinline__ bool better(float s, int o, float bs, int bo) {
+  return s > bs || (s == bs && o < bo);
 }
 
 // ------------------------------------------------------------------ pyramid
@@ -129,7 +176,7 @@ __global__ void __launch_bounds__(256) coarse_kernel(CoarseArgs a) {
   const int TW = kTileW + pd.cmax - pd.cmin, TH = kTileH + pd.rmax - pd.rmin;
   const int tid = threadIdx.y * kTileW + threadIdx.x;
   const int w = a.lev.w, h = a.lev.h;
-  // skip tiles with no valid position (still write -inf)
+  // tiles with no valid position only write -inf
   const bool any = R0 < rg.r1 && R0 + kTileH > rg.r0 && C0 < rg.c1 && C0 + kTileW > rg.c0;
   if (any) {
     for (int i = tid; i < TW * TH; i += 256) {
@@ -142,21 +189,20 @@ __global__ void __launch_bounds__(256) coarse_kernel(CoarseArgs a) {
   if (r >= h || c >= w) return;
   float score = -INFINITY;
   if (any && r >= rg.r0 && r < rg.r1 && c >= rg.c0 && c < rg.c1) {
-    const int32_t* offs = a.view.offs + pd.sample_off;
-    const float* wt = a.view.w + pd.sample_off;
+    const int2* sw = a.view.sw + pd.sample_off;
     const float* base = tile + (threadIdx.y - pd.rmin) * TW + (threadIdx.x - pd.cmin);
-    const int32_t o0 = __ldg(offs);
-    const float s0 = base[off_row(o0) * TW + off_col(o0)];
+    const int2 f0 = __ldg(sw);
+    const float s0 = base[off_row(f0.x) * TW + off_col(f0.x)];
     float acc0 = 0.f, acc1 = 0.f;
     int i = 0;
     for (; i + 1 < pd.n; i += 2) {
-      const int32_t oa = __ldg(offs + i), ob = __ldg(offs + i + 1);
-      acc0 = fmaf(__ldg(wt + i), base[off_row(oa) * TW + off_col(oa)] - s0, acc0);
-      acc1 = fmaf(__ldg(wt + i + 1), base[off_row(ob) * TW + off_col(ob)] - s0, acc1);
+      const int2 x = __ldg(sw + i), y = __ldg(sw + i + 1);
+      acc0 = fmaf(__int_as_float(x.y), base[off_row(x.x) * TW + off_col(x.x)] - s0, acc0);
+      acc1 = fmaf(__int_as_float(y.y), base[off_row(y.x) * TW + off_col(y.x)] - s0, acc1);
     }
     if (i < pd.n) {
-      const int32_t oa = __ldg(offs + i);
-      acc0 = fmaf(__ldg(wt + i), base[off_row(oa) * TW + off_col(oa)] - s0, acc0);
+      const int2 x = __ldg(sw + i);
+      acc0 = fmaf(__int_as_float(x.y), base[off_row(x.x) * TW + off_col(x.x)] - s0, acc0);
     }
     long long s1, s2;
     window_moments(a.lev.prefix, w + 1, r, c, a.view.runs + pd.run_off, a.view.runs_end + pd.run_off, pd.nruns, s1, s2);
@@ -176,7 +222,7 @@ __global__ void nms_kernel(NmsArgs a) {
   const int r = rem / a.w, c = rem % a.w;
   const float* s = a.planes + size_t(p) * plane;
   const float v = s[rem];
-  if (!(double(v) >= a.threshold) || !isfinite(v)) return;
+  if (!(v >= a.threshold) || !isfinite(v)) return;
   for (int dr = -1; dr <= 1; ++dr)
     for (int dc = -1; dc <= 1; ++dc) {
       const int rr = r + dr, cc = c + dc;
@@ -189,93 +235,162 @@ __global__ void nms_kernel(NmsArgs a) {
     atomicExch(&a.state->overflow, 1);
     return;
   }
-  const PatchDesc pd = a.view.patches[a.plist[p]];
+  const int32_t pi = a.plist[p];
+  const PatchDesc pd = a.view.patches[pi];
   Cand out;
   out.row = lattice_pose(a.crop_row, a.scale, r, pd.orow, a.phase);
   out.col = lattice_pose(a.crop_col, a.scale, c, pd.ocol, a.phase);
   out.angle = pd.angle;
   out.score = double(v);
+  out.patch = pi;
+  out.pad = 0;
   a.out[k] = out;
 }
 
 // ------------------------------------------------------------------ tracking
-// One block per candidate: every query patch of the target level within the
-// angle window, 5x5 positions each; the first strict maximum in (patch order,
-// dr, dc) wins (src/ncc_matching/matcher.cpp:670-757).
-__device__ __forceinline__ bool better(float s, int o, float bs, int bo) {
-  return s > bs || (s == bs && o < bo);
-}
+// One block per candidate: the target level's query patches inside the
+// candidate's angle window (a precomputed list per source patch), 5x5
+// positions each; the first strict maximum in (patch order, dr, dc) wins
+// (src/ncc_matching/matcher.cpp:670-757).  The union image window of all
+// those placements is staged in shared memory; each thread scores one
+// (patch, position) item, or a slice of its samples when items are few.
+constexpr int kTrackThreads = 256;
+constexpr int kTrackMaxSel = 64;
+constexpr int kTrackWindow = 12288;  // floats of staged image (48 KiB)
 
-__global__ void __launch_bounds__(256) track_kernel(TrackArgs a) {
+__global__ void __launch_bounds__(kTrackThreads) track_kernel(TrackArgs a) {
   const int i = blockIdx.x;
   if (i >= a.state->count[a.in_slot]) return;
-  __shared__ int sel[256];
-  __shared__ int nsel;
-  __shared__ float wscore[8];
-  __shared__ int worder[8];
+  __shared__ int s_sel[kTrackMaxSel];
+  __shared__ int s_row[kTrackMaxSel], s_col[kTrackMaxSel];
+  __shared__ int s_n, s_split, s_wr0, s_wc0, s_ww, s_wh, s_staged;
+  __shared__ float s_part[kTrackThreads];
+  __shared__ float s_wbest[kTrackThreads / 32];
+  __shared__ int s_word[kTrackThreads / 32];
+  __shared__ float win[kTrackWindow];
   const Cand cd = a.in[i];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (threadIdx.x == 0) nsel = 0;
-  __syncthreads();
-  // ordered selection of the patches inside the angle window (warp 0)
-  if (warp == 0) {
-    int count = 0;
-    for (int base = 0; base < a.nplist; base += 32) {
-      const int j = base + lane;
-      bool hit = false;
-      if (j < a.nplist) {
-        const double ang = a.view.patches[a.plist[j]].angle;
-        hit = !(fabs(dsub(ang, cd.angle)) > a.angle_limit);
-      }
-      const unsigned m = __ballot_sync(0xffffffffu, hit);
-      if (hit) {
-        const int pos = count + __popc(m & ((1u << lane) - 1));
-        if (pos < 256) sel[pos] = j;
-      }
-      count += __popc(m);
+  if (threadIdx.x == 0) {
+    const int src = cd.patch;
+    const int b = src >= 0 ? a.sel_off[src] : 0, e = src >= 0 ? a.sel_off[src + 1] : 0;
+    const int n = min(e - b, kTrackMaxSel);
+    int wr0 = INT32_MAX, wc0 = INT32_MAX, wr1 = INT32_MIN, wc1 = INT32_MIN;
+    // window centres: round((pose - crop - offset) / step - origin)
+    double xr = 0, xc = 0;
+    float xr32 = 0, xc32 = 0;
+    if (a.exact32) {
+      xr32 = __fmul_rn(__fsub_rn(__fsub_rn(float(cd.row), float(a.crop_row)), float(a.offset)), float(1.0 / a.step));
+      xc32 = __fmul_rn(__fsub_rn(__fsub_rn(float(cd.col), float(a.crop_col)), float(a.offset)), float(1.0 / a.step));
+    } else {
+      xr = dsub(dsub(cd.row, a.crop_row), a.offset) / a.step;
+      xc = dsub(dsub(cd.col, a.crop_col), a.offset) / a.step;
     }
-    if (lane == 0) nsel = min(count, 256);
+    for (int k = 0; k < n; ++k) {
+      const int j = a.sel_idx[b + k];
+      s_sel[k] = j;
+      const PatchDesc pd = a.view.patches[a.plist[j]];
+      int row, col;
+      if (a.exact32) {
+        row = int(roundf(__fsub_rn(xr32, float(pd.orow))));
+        col = int(roundf(__fsub_rn(xc32, float(pd.ocol))));
+      } else {
+        row = int(round(dsub(xr, pd.orow)));
+        col = int(round(dsub(xc, pd.ocol)));
+      }
+      s_row[k] = row;
+      s_col[k] = col;
+      const PosRange rg = a.ranges[j];
+      // only placements that can be scored need image data
+      const int r_lo = max(row - 2, rg.r0), r_hi = min(row + 2, rg.r1 - 1);
+      const int c_lo = max(col - 2, rg.c0), c_hi = min(col + 2, rg.c1 - 1);
+      if (r_lo <= r_hi && c_lo <= c_hi) {
+        wr0 = min(wr0, r_lo + pd.rmin);
+        wr1 = max(wr1, r_hi + pd.rmax);
+        wc0 = min(wc0, c_lo + pd.cmin);
+        wc1 = max(wc1, c_hi + pd.cmax);
+      }
+    }
+    s_n = n;
+    const int items = n * 25;
+    s_split = items > 0 ? max(1, min(8, kTrackThreads / items)) : 1;
+    const bool any = wr0 <= wr1;
+    s_wr0 = any ? wr0 : 0;
+    s_wc0 = any ? wc0 : 0;
+    s_wh = any ? wr1 - wr0 + 1 : 0;
+    s_ww = any ? wc1 - wc0 + 1 : 0;
+    s_staged = any && s_wh * s_ww <= kTrackWindow;
+  }
+  __syncthreads();
+  const int n = s_n, split = s_split;
+  const int pitch = a.lev.w;
+  const bool staged = s_staged != 0;
+  const int ww = staged ? s_ww : pitch;
+  // staged: window coordinates; else: the level itself with a zero origin
+  const int wr0 = staged ? s_wr0 : 0, wc0 = staged ? s_wc0 : 0;
+  const float* img = staged ? win : a.lev.v;
+  if (staged) {
+    const int cells = s_wh * s_ww;
+    for (int t = threadIdx.x; t < cells; t += kTrackThreads) {
+      const int rr = t / s_ww, cc = t % s_ww;
+      win[t] = a.lev.v[size_t(s_wr0 + rr) * pitch + s_wc0 + cc];
+    }
   }
   __syncthreads();
   float best = -INFINITY;
   int border = INT32_MAX;
-  const int dr = lane / 5 - 2, dc = lane % 5 - 2;
-  for (int k = warp; k < nsel; k += 8) {
-    const int j = sel[k];
-    const PatchDesc pd = a.view.patches[a.plist[j]];
-    const PosRange rg = a.ranges[j];
-    if (lane == 0) atomicAdd(&a.state->track_macs, 25ull * (unsigned long long)pd.n);
-    const int row = int(round(dsub(dsub(dsub(cd.row, a.crop_row), a.offset) / a.step, pd.orow)));
-    const int col = int(round(dsub(dsub(dsub(cd.col, a.crop_col), a.offset) / a.step, pd.ocol)));
-    const int r = row + dr, c = col + dc;
-    if (lane < 25 && r >= rg.r0 && r < rg.r1 && c >= rg.c0 && c < rg.c1) {
-      const int32_t* offs = a.view.offs + pd.sample_off;
-      const float* wt = a.view.w + pd.sample_off;
-      const int pitch = a.lev.w;
-      const float* base = a.lev.v + size_t(r) * pitch + c;
-      const int32_t o0 = __ldg(offs);
-      const float s0 = __ldg(base + off_row(o0) * pitch + off_col(o0));
-      float acc0 = 0.f, acc1 = 0.f;
-      int s = 0;
-      for (; s + 1 < pd.n; s += 2) {
-        const int32_t oa = __ldg(offs + s), ob = __ldg(offs + s + 1);
-        acc0 = fmaf(__ldg(wt + s), __ldg(base + off_row(oa) * pitch + off_col(oa)) - s0, acc0);
-        acc1 = fmaf(__ldg(wt + s + 1), __ldg(base + off_row(ob) * pitch + off_col(ob)) - s0, acc1);
+  const int items = n * 25;
+  const int passes = (items * split + kTrackThreads - 1) / kTrackThreads;
+  for (int pass = 0; pass < passes; ++pass) {
+    const int t = pass * kTrackThreads + threadIdx.x;
+    const int item = t / split, part = t % split;
+    bool valid = false;
+    int r = 0, c = 0;
+    PatchDesc pd{};
+    float acc = 0.f;
+    if (item < items) {
+      const int k = item / 25, pos = item % 25;
+      const int j = s_sel[k];
+      pd = a.view.patches[a.plist[j]];
+      const PosRange rg = a.ranges[j];
+      r = s_row[k] + pos / 5 - 2;
+      c = s_col[k] + pos % 5 - 2;
+      valid = r >= rg.r0 && r < rg.r1 && c >= rg.c0 && c < rg.c1;
+    }
+    if (valid) {
+      const int2* sw = a.view.sw + pd.sample_off;
+      const float* base = img + size_t(r - wr0) * ww + (c - wc0);
+      const int2 f0 = __ldg(sw);
+      const float s0 = base[off_row(f0.x) * ww + off_col(f0.x)];
+      float acc1 = 0.f;
+      int s = part;
+      for (; s + split < pd.n; s += 2 * split) {
+        const int2 x = __ldg(sw + s), y = __ldg(sw + s + split);
+        acc = fmaf(__int_as_float(x.y), base[off_row(x.x) * ww + off_col(x.x)] - s0, acc);
+        acc1 = fmaf(__int_as_float(y.y), base[off_row(y.x) * ww + off_col(y.x)] - s0, acc1);
       }
       if (s < pd.n) {
-        const int32_t oa = __ldg(offs + s);
-        acc0 = fmaf(__ldg(wt + s), __ldg(base + off_row(oa) * pitch + off_col(oa)) - s0, acc0);
+        const int2 x = __ldg(sw + s);
+        acc = fmaf(__int_as_float(x.y), base[off_row(x.x) * ww + off_col(x.x)] - s0, acc);
       }
+      acc += acc1;
+    }
+    // combine the sample slices of one item (consecutive threads)
+    if (split > 1) {
+      s_part[threadIdx.x] = acc;
+      __syncthreads();
+    }
+    if (part == 0 && valid) {
+      float dot = acc;
+      for (int q = 1; q < split; ++q) dot += s_part[threadIdx.x + q];
       long long s1, s2;
       window_moments(a.lev.prefix, pitch + 1, r, c, a.view.runs + pd.run_off, a.view.runs_end + pd.run_off,
                      pd.nruns, s1, s2);
-      const float sc = window_score(acc0 + acc1, s1, s2, pd.n, a.absolute);
-      const int order = k * 25 + lane;
-      if (better(sc, order, best, border)) {
+      const float sc = window_score(dot, s1, s2, pd.n, a.absolute);
+      if (better(sc, item, best, border)) {
         best = sc;
-        border = order;
+        border = item;
       }
     }
+    if (split > 1) __syncthreads();
   }
   for (int o = 16; o > 0; o >>= 1) {
     const float ob = __shfl_down_sync(0xffffffffu, best, o);
@@ -285,30 +400,40 @@ __global__ void __launch_bounds__(256) track_kernel(TrackArgs a) {
       border = oo;
     }
   }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (lane == 0) {
-    wscore[warp] = best;
-    worder[warp] = border;
+    s_wbest[warp] = best;
+    s_word[warp] = border;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     float bs = -INFINITY;
     int bo = INT32_MAX;
-    for (int w = 0; w < 8; ++w)
-      if (better(wscore[w], worder[w], bs, bo)) {
-        bs = wscore[w];
-        bo = worder[w];
+    unsigned long long macs = 0;
+    for (int w = 0; w < kTrackThreads / 32; ++w)
+      if (better(s_wbest[w], s_word[w], bs, bo)) {
+        bs = s_wbest[w];
+        bo = s_word[w];
       }
+    for (int k = 0; k < n; ++k) macs += 25ull * (unsigned long long)a.view.patches[a.plist[s_sel[k]]].n;
+    atomicAdd(&a.state->track_macs, macs);
     Cand out = cd;
     out.score = -INFINITY;
     if (bo != INT32_MAX && bs > -INFINITY) {
       const int k = bo / 25, l = bo % 25;
-      const PatchDesc pd = a.view.patches[a.plist[sel[k]]];
-      const int row = int(round(dsub(dsub(dsub(cd.row, a.crop_row), a.offset) / a.step, pd.orow)));
-      const int col = int(round(dsub(dsub(dsub(cd.col, a.crop_col), a.offset) / a.step, pd.ocol)));
-      out.row = lattice_pose(a.crop_row, a.step, row + l / 5 - 2, pd.orow, a.offset);
-      out.col = lattice_pose(a.crop_col, a.step, col + l % 5 - 2, pd.ocol, a.offset);
+      const int32_t pi = a.plist[s_sel[k]];
+      const PatchDesc pd = a.view.patches[pi];
+      const int r = s_row[k] + l / 5 - 2, c = s_col[k] + l % 5 - 2;
+      if (a.exact32) {
+        out.row = double(lattice_pose32(float(a.crop_row), float(a.step), r, float(pd.orow), float(a.offset)));
+        out.col = double(lattice_pose32(float(a.crop_col), float(a.step), c, float(pd.ocol), float(a.offset)));
+      } else {
+        out.row = lattice_pose(a.crop_row, a.step, r, pd.orow, a.offset);
+        out.col = lattice_pose(a.crop_col, a.step, c, pd.ocol, a.offset);
+      }
       out.angle = pd.angle;
       out.score = double(bs);
+      out.patch = pi;
     }
     a.out[i] = out;
   }
@@ -344,6 +469,7 @@ __device__ void snap_pose(Cand& p, double height, double width) {
   if (isfinite(best)) {
     p.row = nr;
     p.col = nc;
+    p.patch = -1;
   } else {
     p.score = -INFINITY;
   }
@@ -376,46 +502,31 @@ __global__ void dedup_kernel(DedupArgs a) {
       return;
     }
     const Cand q = a.in[prev];
-    if (q.row == p.row && q.col == p.col && q.angle == p.angle) return;
+    if ((unsigned long long)__double_as_longlong(q.row) == kr && (unsigned long long)__double_as_longlong(q.col) == kc &&
+        (unsigned long long)__double_as_longlong(q.angle) == ka)
+      return;
     slot = (slot + 1) & (kHashSlots - 1);
   }
 }
 
 // -------------------------------------------------- full-resolution scoring
-// Cross-thread sums use FP32 (hi, lo) pairs (Knuth two-sum): per-thread FP32
-// partials combine with ~2^-44 relative error without FP64 instructions (the
-// FP64 pipe of sm_103 is narrow).  Thread 0 finishes each pass in FP64 and
-// broadcasts through shared memory.
-struct F2 {
-  float hi, lo;
-};
-__device__ __forceinline__ F2 f2_add(F2 x, F2 y) {
-  const float s = x.hi + y.hi;
-  const float bb = s - x.hi;
-  const float e = ((x.hi - (s - bb)) + (y.hi - bb)) + (x.lo + y.lo);
-  const float h = s + e;
-  return F2{h, e - (h - s)};
-}
-
-// Totals of K per-thread values; valid on thread 0 only.  scratch: K*64 floats.
+// Totals of K per-thread values as FP32 pairs; valid on thread 0 only.
+// scratch: K*64 floats.
 template <int K>
-__device__ void block_total(const float (&v)[K], double (&out)[K], float* scratch) {
+__device__ void block_total(const float (&v)[K], F2 (&out)[K], float* scratch) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  F2 x[K];
 #pragma unroll
-  for (int k = 0; k < K; ++k) x[k] = F2{v[k], 0.f};
-#pragma unroll
-  for (int k = 0; k < K; ++k)
+  for (int k = 0; k < K; ++k) {
+    F2 x = f2(v[k]);
     for (int o = 16; o > 0; o >>= 1) {
-      const F2 y{__shfl_down_sync(0xffffffffu, x[k].hi, o), __shfl_down_sync(0xffffffffu, x[k].lo, o)};
-      x[k] = f2_add(x[k], y);
+      const F2 y{__shfl_down_sync(0xffffffffu, x.hi, o), __shfl_down_sync(0xffffffffu, x.lo, o)};
+      x = f2_add(x, y);
     }
-  if (lane == 0)
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      scratch[(k * 32 + warp) * 2] = x[k].hi;
-      scratch[(k * 32 + warp) * 2 + 1] = x[k].lo;
+    if (lane == 0) {
+      scratch[(k * 32 + warp) * 2] = x.hi;
+      scratch[(k * 32 + warp) * 2 + 1] = x.lo;
     }
+  }
   __syncthreads();
   if (warp == 0) {
 #pragma unroll
@@ -425,13 +536,13 @@ __device__ void block_total(const float (&v)[K], double (&out)[K], float* scratc
         const F2 z{__shfl_down_sync(0xffffffffu, y.hi, o), __shfl_down_sync(0xffffffffu, y.lo, o)};
         y = f2_add(y, z);
       }
-      out[k] = double(y.hi) + double(y.lo);
+      out[k] = y;
     }
   }
   __syncthreads();
 }
 
-// Pose in the frame of an integer anchor: FP64 only here (thread 0).
+// Pose in the frame of an integer anchor.
 struct LocalPose {
   int R0, C0;        // integer anchor
   float fr, fc;      // fractional part of the pose relative to the anchor
@@ -445,10 +556,7 @@ __device__ __forceinline__ LocalPose make_local(double row, double col, double a
   l.C0 = int(fc);
   l.fr = float(row - fr);
   l.fc = float(col - fc);
-  double s, c;
-  sincos(angle, &s, &c);
-  l.ca = float(c);
-  l.sa = float(s);
+  sincosf(float(angle), &l.sa, &l.ca);
   return l;
 }
 
@@ -466,6 +574,16 @@ __device__ __forceinline__ float bilinear_at(const ImageView& img, int r, int c,
   const float* v = img.v;
   return (1 - fy) * ((1 - fx) * __ldg(v + size_t(r) * img.w + c) + fx * __ldg(v + size_t(r) * img.w + c1)) +
          fy * ((1 - fx) * __ldg(v + size_t(r1) * img.w + c) + fx * __ldg(v + size_t(r1) * img.w + c1));
+}
+
+// FP32 score from pair totals of sum q, sum q^2, sum w q.
+__device__ __forceinline__ float pair_score(F2 sum, F2 sq, F2 dot, int n, int absolute, bool* ok) {
+  const F2 var = f2_sub(sq, f2_div(f2_mul(sum, sum), f2(float(n))));
+  const float v = f2_val(var);
+  *ok = v > 0;
+  if (!*ok) return -INFINITY;
+  float s = fminf(1.f, fmaxf(-1.f, f2_val(dot) / sqrtf(v)));
+  return absolute ? fabsf(s) : s;
 }
 
 // continuous() of src/ncc_matching/matcher.cpp:144-156 at a level-local pose;
@@ -502,18 +620,12 @@ __device__ void continuous_pass(const ImageView& img, const OriginalView& orig, 
     acc[1] = fmaf(q, q, acc[1]);
     acc[2] = fmaf(w, q, acc[2]);
   }
-  double t[4];
+  F2 t[4];
   block_total<4>(acc, t, sh.scratch);
   if (threadIdx.x == 0) {
-    double sc = -INFINITY;
-    if (!(t[3] > 0)) {
-      const double var = t[1] - t[0] * t[0] / double(orig.n);
-      if (var > 0) {
-        sc = fmin(1., fmax(-1., t[2] / sqrt(var)));
-        if (absolute) sc = fabs(sc);
-      }
-    }
-    sh.score = sc;
+    bool ok = false;
+    const float sc = t[3].hi > 0 ? -INFINITY : pair_score(t[0], t[1], t[2], orig.n, absolute, &ok);
+    sh.score = (t[3].hi > 0 || !ok) ? -INFINITY : double(sc);
   }
   __syncthreads();
 }
@@ -532,13 +644,20 @@ __global__ void __launch_bounds__(128) score_kernel(ScoreArgs a) {
 
 // --------------------------------------------------------------------- sort
 // Candidates by score (descending), then row, column, angle ascending
-// (src/ncc_matching/matcher.cpp:824-827).  One block, bitonic on indices.
-__device__ __forceinline__ bool before(const Cand* c, const double* key, const int* idx, int a, int b) {
+// (src/ncc_matching/matcher.cpp:824-827).  One block, bitonic on 64-bit
+// order-preserving keys; exact score ties fall back to the pose.
+__device__ __forceinline__ unsigned long long desc_key(double s) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(s);
+  const unsigned long long asc = (b >> 63) ? ~b : (b | 0x8000000000000000ULL);
+  return ~asc;
+}
+
+__device__ __forceinline__ bool before(const Cand* c, const unsigned long long* key, const int* idx, int a, int b) {
   const int ia = idx[a], ib = idx[b];
   if (ia < 0) return false;
   if (ib < 0) return true;
-  const double ka = key[a], kb = key[b];
-  if (ka != kb) return ka > kb;
+  const unsigned long long ka = key[a], kb = key[b];
+  if (ka != kb) return ka < kb;
   const Cand x = c[ia], y = c[ib];
   if (x.row != y.row) return x.row < y.row;
   if (x.col != y.col) return x.col < y.col;
@@ -550,11 +669,11 @@ __global__ void __launch_bounds__(1024) sort_kernel(SortArgs a) {
   const int n = a.state->count[a.slot];
   int P = 1;
   while (P < n) P <<= 1;
-  double* key = reinterpret_cast<double*>(smem);
+  unsigned long long* key = reinterpret_cast<unsigned long long*>(smem);
   int* idx = reinterpret_cast<int*>(key + P);
   for (int t = threadIdx.x; t < P; t += blockDim.x) {
     idx[t] = t < n ? t : -1;
-    key[t] = t < n ? a.in[t].score : -INFINITY;
+    key[t] = t < n ? desc_key(a.in[t].score) : ~0ULL;
   }
   __syncthreads();
   for (int k = 2; k <= P; k <<= 1)
@@ -565,7 +684,7 @@ __global__ void __launch_bounds__(1024) sort_kernel(SortArgs a) {
           const bool up = (t & k) == 0;
           const bool swap = up ? before(a.in, key, idx, l, t) : before(a.in, key, idx, t, l);
           if (swap) {
-            const double tk = key[t];
+            const unsigned long long tk = key[t];
             key[t] = key[l];
             key[l] = tk;
             const int ti = idx[t];
@@ -591,34 +710,51 @@ __global__ void __launch_bounds__(1024) sort_kernel(SortArgs a) {
 }
 
 // ----------------------------------------------------------------- overlap
-// Intersection area of two rotated template rectangles over the template
-// area (src/ncc_matching/matcher.cpp:252-277).  a is the candidate, b the
-// accepted match.
-struct Pt { double x, y; };
-
-__device__ void rect_corners(const Cand& m, const Cand& a, const SelectArgs& s, Pt out[4]) {
-  double sa, ca;
-  sincos(m.angle, &sa, &ca);
-  const double left = -s.tmpl_ocol - .5, right = s.tmpl_w - s.tmpl_ocol - .5;
-  const double top = -s.tmpl_orow - .5, bottom = s.tmpl_h - s.tmpl_orow - .5;
-  const Pt in[4] = {{left, top}, {right, top}, {right, bottom}, {left, bottom}};
-  for (int i = 0; i < 4; ++i) {
-    out[i].x = dadd(dadd(dsub(m.col, a.col), dmul(ca, in[i].x)), dmul(sa, in[i].y));
-    out[i].y = dadd(dsub(dsub(m.row, a.row), dmul(sa, in[i].x)), dmul(ca, in[i].y));
-  }
+// Rotated rectangle of a pose: FP64 cos/sin once per pose, a conservative
+// FP32 box for the cheap disjointness test.
+__device__ RectAux make_rect(const Cand& m, const RectGeom& g) {
+  RectAux r;
+  sincos(m.angle, &r.sa, &r.ca);
+  float x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
+  const double xs[2] = {g.left, g.right}, ys[2] = {g.top, g.bottom};
+  for (double x : xs)
+    for (double y : ys) {
+      const float px = float(m.col) + float(r.ca) * float(x) + float(r.sa) * float(y);
+      const float py = float(m.row) - float(r.sa) * float(x) + float(r.ca) * float(y);
+      x0 = fminf(x0, px);
+      x1 = fmaxf(x1, px);
+      y0 = fminf(y0, py);
+      y1 = fmaxf(y1, py);
+    }
+  const float pad = 1e-3f * (1.f + fabsf(float(m.row)) + fabsf(float(m.col)));
+  r.x0 = x0 - pad;
+  r.y0 = y0 - pad;
+  r.x1 = x1 + pad;
+  r.y1 = y1 + pad;
+  return r;
 }
 
-__device__ double overlap_ratio(const Cand& a, const Cand& b, const SelectArgs& s) {
+__device__ __forceinline__ bool boxes_disjoint(const RectAux& a, const RectAux& b) {
+  return a.x1 < b.x0 || b.x1 < a.x0 || a.y1 < b.y0 || b.y1 < a.y0;
+}
+
+struct Pt {
+  double x, y;
+};
+
+// Intersection area of two rotated template rectangles over the template
+// area (src/ncc_matching/matcher.cpp:252-277); a is the candidate, b the
+// accepted match.  Corners are relative to a's centre.
+__device__ double overlap_ratio(const Cand& a, const RectAux& ra, const Cand& b, const RectAux& rb, const RectGeom& g) {
+  if (boxes_disjoint(ra, rb)) return 0.;
+  const Pt in[4] = {{g.left, g.top}, {g.right, g.top}, {g.right, g.bottom}, {g.left, g.bottom}};
   Pt clip[4], poly[16], next[16];
-  rect_corners(b, a, s, clip);
-  rect_corners(a, a, s, poly);
-  // axis-aligned boxes disjoint -> empty intersection
-  double ax0 = poly[0].x, ax1 = ax0, ay0 = poly[0].y, ay1 = ay0, bx0 = clip[0].x, bx1 = bx0, by0 = clip[0].y, by1 = by0;
-  for (int i = 1; i < 4; ++i) {
-    ax0 = fmin(ax0, poly[i].x); ax1 = fmax(ax1, poly[i].x); ay0 = fmin(ay0, poly[i].y); ay1 = fmax(ay1, poly[i].y);
-    bx0 = fmin(bx0, clip[i].x); bx1 = fmax(bx1, clip[i].x); by0 = fmin(by0, clip[i].y); by1 = fmax(by1, clip[i].y);
+  for (int i = 0; i < 4; ++i) {
+    clip[i].x = dadd(dadd(dsub(b.col, a.col), dmul(rb.ca, in[i].x)), dmul(rb.sa, in[i].y));
+    clip[i].y = dadd(dsub(dsub(b.row, a.row), dmul(rb.sa, in[i].x)), dmul(rb.ca, in[i].y));
+    poly[i].x = dadd(dmul(ra.ca, in[i].x), dmul(ra.sa, in[i].y));
+    poly[i].y = dadd(-dmul(ra.sa, in[i].x), dmul(ra.ca, in[i].y));
   }
-  if (ax1 < bx0 || bx1 < ax0 || ay1 < by0 || by1 < ay0) return 0.;
   int count = 4;
   for (int edge = 0; edge < 4 && count; ++edge) {
     const Pt p = clip[edge], q = clip[(edge + 1) & 3];
@@ -639,88 +775,129 @@ __device__ double overlap_ratio(const Cand& a, const Cand& b, const SelectArgs& 
   double area = 0;
   for (int i = 0; i < count; ++i)
     area = dadd(area, dsub(dmul(poly[i].x, poly[(i + 1) % count].y), dmul(poly[(i + 1) % count].x, poly[i].y)));
-  return fabs(area) * .5 / (s.tmpl_w * s.tmpl_h);
+  return fabs(area) * .5 / g.area;
+}
+
+__global__ void rects_kernel(const Cand* sorted, RectAux* aux, const QueryState* state, RectGeom g) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= state->sorted_count) return;
+  aux[i] = make_rect(sorted[i], g);
 }
 
 // Greedy MaxOverlap selection over the sorted candidates
-// (src/ncc_matching/matcher.cpp:1063-1076).  Refinement results come from
-// refine_kernel; when the next candidate has none, the kernel queues a batch
-// of candidates that the current accepted set does not suppress and returns
-// with state->need = 1.
-__device__ bool suppressed_by(const Cand& c, const Cand* list, int n, const SelectArgs& s) {
-  __shared__ int hit;
-  if (threadIdx.x == 0) hit = 0;
-  __syncthreads();
-  for (int j = threadIdx.x; j < n; j += blockDim.x)
-    if (overlap_ratio(c, list[j], s) > s.max_overlap + 1e-12) hit = 1;
-  __syncthreads();
-  const bool r = hit != 0;
-  __syncthreads();
-  return r;
-}
+// (src/ncc_matching/matcher.cpp:1063-1076).  A window of candidates is tested
+// against the accepted matches in parallel; the first unsuppressed one is
+// then accepted or rejected from its refinement result.  When it has none,
+// the kernel queues it and the next unsuppressed, unrefined candidates that
+// do not overlap a higher-ranked queued one, and returns with need = 1.
+constexpr int kSelectThreads = 1024;
 
-__global__ void __launch_bounds__(256) select_kernel(SelectArgs a) {
-  __shared__ Cand batch_poses[64];
+__global__ void __launch_bounds__(kSelectThreads) select_kernel(SelectArgs a) {
+  __shared__ int s_next, s_acc, s_first, s_hit;
+  __shared__ unsigned char s_sup[kSelectThreads];
+  __shared__ int s_batch[64];
   QueryState* st = a.state;
   if (st->done) return;
   const int total = st->sorted_count;
-  if (threadIdx.x == 0) st->need = 0;
+  const double thr = a.max_overlap + 1e-12;
+  if (threadIdx.x == 0) {
+    s_next = st->next;
+    s_acc = st->accepted;
+    st->need = 0;
+  }
+  __syncthreads();
   while (true) {
-    const int i = st->next;
-    const int accepted = st->accepted;
+    const int base = s_next, acc = s_acc;
+    if (base >= total || (a.num_matches && acc >= a.num_matches)) break;
+    // suppression of the window by the accepted matches
+    const int wcount = min(kSelectThreads, total - base);
+    const int t = threadIdx.x;
+    bool sup = true;
+    if (t < wcount) {
+      const int idx = base + t;
+      const Cand c = a.sorted[idx];
+      const RectAux rc = a.aux[idx];
+      sup = false;
+      for (int j = 0; j < acc && !sup; ++j)
+        if (overlap_ratio(c, rc, a.accepted[j], a.accepted_aux[j], a.geom) > thr) sup = true;
+    }
+    s_sup[t] = sup ? 1 : 0;
+    if (t == 0) s_first = INT32_MAX;
     __syncthreads();
-    if (i >= total || (a.num_matches && accepted >= a.num_matches)) break;
-    const Cand c = a.sorted[i];
-    if (suppressed_by(c, a.accepted, accepted, a)) {
+    if (!sup) atomicMin(&s_first, t);
+    __syncthreads();
+    const int first = s_first;
+    if (first == INT32_MAX) {
       __syncthreads();
-      if (threadIdx.x == 0) st->next = i + 1;
+      if (threadIdx.x == 0) s_next = base + wcount;
       __syncthreads();
       continue;
     }
+    const int i = base + first;
     if (a.refined_flag[i] != 2) {
-      // queue a refinement batch starting at i
-      int nb = 0;
-      for (int k = i; k < total && nb < a.batch_limit && nb < 64; ++k) {
-        if (a.refined_flag[k] == 2) continue;
-        const Cand ck = a.sorted[k];
-        if (k != i && suppressed_by(ck, a.accepted, accepted, a)) continue;
-        if (k != i && suppressed_by(ck, batch_poses, nb, a)) continue;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-          batch_poses[nb] = ck;
-          a.batch[nb] = k;
-          a.refined_flag[k] = 1;
-        }
-        ++nb;
-        __syncthreads();
-      }
+      // queue i and the next unsuppressed, unrefined candidates of the window
+      // that no higher-ranked queued candidate overlaps (speculation only)
       if (threadIdx.x == 0) {
+        int nb = 0;
+        s_batch[nb++] = i;
+        for (int k = first + 1; k < wcount && nb < a.batch_limit && nb < 64; ++k) {
+          const int idx = base + k;
+          if (s_sup[k] || a.refined_flag[idx] == 2) continue;
+          const RectAux rk = a.aux[idx];
+          bool dup = false;
+          for (int q = 0; q < nb && !dup; ++q) {
+            const RectAux rq = a.aux[s_batch[q]];
+            // boxes overlapping by more than half of the smaller box
+            const float ix = fminf(rk.x1, rq.x1) - fmaxf(rk.x0, rq.x0), iy = fminf(rk.y1, rq.y1) - fmaxf(rk.y0, rq.y0);
+            if (ix > 0 && iy > 0) {
+              const float ak = (rk.x1 - rk.x0) * (rk.y1 - rk.y0), aq = (rq.x1 - rq.x0) * (rq.y1 - rq.y0);
+              if (ix * iy > 0.5f * fminf(ak, aq)) dup = true;
+            }
+          }
+          if (!dup) s_batch[nb++] = idx;
+        }
+        for (int q = 0; q < nb; ++q) {
+          a.batch[q] = s_batch[q];
+          a.refined_flag[s_batch[q]] = 1;
+        }
         st->batch_count = nb;
         st->need = 1;
+        st->next = i;
+        st->accepted = acc;
       }
       return;
     }
     const Refined r = a.refined[i];
-    bool keep = r.ok != 0;
+    const bool keep = r.ok != 0;
     Cand rc;
     rc.row = r.row;
     rc.col = r.col;
     rc.angle = r.angle;
     rc.score = r.score;
-    if (keep && suppressed_by(rc, a.accepted, accepted, a)) keep = false;
+    rc.patch = -1;
+    rc.pad = 0;
+    // re-check against the accepted matches with the refined pose
+    if (threadIdx.x == 0) s_hit = 0;
+    __syncthreads();
+    if (keep)
+      for (int j = threadIdx.x; j < acc; j += kSelectThreads)
+        if (overlap_ratio(rc, r.rect, a.accepted[j], a.accepted_aux[j], a.geom) > thr) s_hit = 1;
     __syncthreads();
     if (threadIdx.x == 0) {
-      if (keep) {
-        a.accepted[accepted] = rc;
-        st->accepted = accepted + 1;
+      if (keep && !s_hit) {
+        a.accepted[acc] = rc;
+        a.accepted_aux[acc] = r.rect;
+        s_acc = acc + 1;
       }
-      st->next = i + 1;
+      s_next = i + 1;
     }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
+    st->next = s_next;
+    st->accepted = s_acc;
     // final order: score desc, row, column, angle (src/ncc_matching/matcher.cpp:1072-1075)
-    const int n = st->accepted;
+    const int n = s_acc;
     for (int x = 1; x < n; ++x) {
       const Cand v = a.accepted[x];
       int y = x - 1;
@@ -742,9 +919,9 @@ __global__ void __launch_bounds__(256) select_kernel(SelectArgs a) {
 
 // --------------------------------------------------------------- refinement
 // refinement_step of src/ncc_matching/matcher.cpp:170-240 at a level-local
-// pose: bilinear samples with the analytic gradient, FP32 per thread, two-sum
-// combination, FP64 normal equations and Gauss-Jordan solve on thread 0.
-// Afterwards sh.ok / sh.gscore / sh.delta hold the result for every thread.
+// pose: bilinear samples with the analytic gradient, FP32 per thread, pair
+// totals, normal equations in pair arithmetic and the Gauss-Jordan solve in
+// FP64 on thread 0.  Afterwards sh.ok / sh.gscore / sh.delta hold the result.
 __device__ void gn_pass(const ImageView& img, const OriginalView& orig, double row, double col, double angle,
                         int absolute, int rotate, bool use_minimum, double minimum, PoseShared& sh) {
   if (threadIdx.x == 0) sh.lp = make_local(row, col, angle);
@@ -799,27 +976,38 @@ __device__ void gn_pass(const ImageView& img, const OriginalView& orig, double r
     acc[16] = fmaf(g2, gx, acc[16]);
     acc[17] = fmaf(g2, g2, acc[17]);
   }
-  double t[19];
+  F2 t[19];
   block_total<19>(acc, t, sh.scratch);
   if (threadIdx.x == 0) {
     sh.ok = 0;
     sh.gscore = -INFINITY;
     sh.delta[0] = sh.delta[1] = sh.delta[2] = 0;
-    const double n = double(orig.n);
-    const double sum = t[0], dot = t[2];
-    const double energy = t[1] - sum * sum / n;
-    if (!(t[18] > 0) && energy > 0) {
-      const double sign = absolute && dot < 0 ? -1 : 1, score = sign * dot / sqrt(energy);
-      sh.gscore = fmin(1., fmax(-1., score));
+    const F2 n = f2(float(orig.n));
+    const F2 sum = t[0], dot = t[2];
+    const F2 energy = f2_sub(t[1], f2_div(f2_mul(sum, sum), n));
+    const float ef = f2_val(energy);
+    if (!(t[18].hi > 0) && ef > 0) {
+      const float sign = absolute && f2_val(dot) < 0 ? -1.f : 1.f;
+      const float sq = sqrtf(ef);
+      const float score = sign * f2_val(dot) / sq;
+      sh.gscore = double(fminf(1.f, fmaxf(-1.f, score)));
       if (!(use_minimum && sh.gscore <= minimum)) {
         const int axes = rotate ? 3 : 2;
-        double gs[3] = {t[3], t[4], t[5]}, qg[3] = {t[6], t[7], t[8]}, wg[3] = {t[9], t[10], t[11]};
-        const double gg[3][3] = {{t[12], t[13], t[15]}, {t[13], t[14], t[16]}, {t[15], t[16], t[17]}};
+        const F2 gs[3] = {t[3], t[4], t[5]}, wg[3] = {t[9], t[10], t[11]};
+        F2 qg[3] = {t[6], t[7], t[8]};
+        const F2 gg[3][3] = {{t[12], t[13], t[15]}, {t[13], t[14], t[16]}, {t[15], t[16], t[17]}};
+        const F2 sn = f2_div(sum, n);
+        for (int i = 0; i < axes; ++i) qg[i] = f2_sub(qg[i], f2_mul(sn, gs[i]));
+        // entries in pair arithmetic, then FP64 for the elimination
+        const F2 inv_e = f2_div(f2(1.f), energy);
         double m[3][4];
-        for (int i = 0; i < axes; ++i) qg[i] -= sum * gs[i] / n;
         for (int i = 0; i < axes; ++i) {
-          for (int j = 0; j < axes; ++j) m[i][j] = (gg[i][j] - gs[i] * gs[j] / n - qg[i] * qg[j] / energy) / energy;
-          m[i][axes] = sign * wg[i] / sqrt(energy) - score * qg[i] / energy;
+          for (int j = 0; j < axes; ++j) {
+            const F2 e = f2_sub(f2_sub(gg[i][j], f2_div(f2_mul(gs[i], gs[j]), n)), f2_mul(f2_mul(qg[i], qg[j]), inv_e));
+            m[i][j] = f2_dbl(f2_mul(e, inv_e));
+          }
+          const F2 r = f2_sub(f2_mul(f2(sign / sq), wg[i]), f2_mul(f2_mul(f2(score), qg[i]), inv_e));
+          m[i][axes] = f2_dbl(r);
         }
         bool good = true;
         for (int i = 0; i < axes && good; ++i) {
@@ -835,8 +1023,8 @@ __device__ void gn_pass(const ImageView& img, const OriginalView& orig, double r
             m[i][k] = m[pivot][k];
             m[pivot][k] = tmp;
           }
-          const double div = m[i][i];
-          for (int k = i; k <= axes; ++k) m[i][k] /= div;
+          const double inv = 1.0 / m[i][i];
+          for (int k = i; k <= axes; ++k) m[i][k] *= inv;
           for (int j = 0; j < axes; ++j)
             if (j != i) {
               const double f = m[j][i];
@@ -866,8 +1054,8 @@ struct FitShared {
   Cand c, imp, best, seed;
   double next_delta[3], delta[3], factor;
   int cached, accepted, next_valid, flag;
-  float wbest[8];
-  int word[8];
+  float wbest[32];
+  int word[32];
 };
 
 __device__ __forceinline__ double local_row(const RefineArgs& a, double row) { return (row - a.crop_row - a.phase) / a.scale; }
@@ -1010,17 +1198,16 @@ __device__ void recovery_search(const RefineArgs& a, FitShared& f) {
     for (int pos = warp; pos < 25; pos += nw) {
       const int r = r0 + pos / 5 - 2, c = c0 + pos % 5 - 2;
       if (r < rg.r0 || r >= rg.r1 || c < rg.c0 || c >= rg.c1) continue;
-      const int32_t* offs = a.view0.offs + pd.sample_off;
-      const float* wt = a.view0.w + pd.sample_off;
+      const int2* sw = a.view0.sw + pd.sample_off;
       const float* base = a.lev0.v + size_t(r) * a.lev0.w + c;
-      const int32_t o0 = __ldg(offs);
-      const float s0 = base[off_row(o0) * a.lev0.w + off_col(o0)];
+      const int2 f0 = __ldg(sw);
+      const float s0 = base[off_row(f0.x) * a.lev0.w + off_col(f0.x)];
       float dot = 0.f;
       long long s1 = 0, s2 = 0;
       for (int s = lane; s < pd.n; s += 32) {
-        const int32_t o = __ldg(offs + s);
-        const float x = base[off_row(o) * a.lev0.w + off_col(o)] - s0;
-        dot = fmaf(__ldg(wt + s), x, dot);
+        const int2 o = __ldg(sw + s);
+        const float x = base[off_row(o.x) * a.lev0.w + off_col(o.x)] - s0;
+        dot = fmaf(__int_as_float(o.y), x, dot);
         const long long xi = (long long)x;
         s1 += xi;
         s2 += xi * xi;
@@ -1077,9 +1264,11 @@ __device__ void recovery_search(const RefineArgs& a, FitShared& f) {
   __syncthreads();
 }
 
+constexpr int kRefineThreads = 512;
+
 // refine_candidate (src/ncc_matching/matcher.cpp:878-1061) for one queued
 // candidate per block.
-__global__ void __launch_bounds__(256) refine_kernel(RefineArgs a) {
+__global__ void __launch_bounds__(kRefineThreads) refine_kernel(RefineArgs a) {
   __shared__ FitShared f;
   const int b = blockIdx.x;
   if (b >= a.state->batch_count) return;
@@ -1106,7 +1295,7 @@ __global__ void __launch_bounds__(256) refine_kernel(RefineArgs a) {
         score_pose(a, f, f.best);
         if (threadIdx.x == 0) {
           f.best.score = f.ps.score;
-          f.seed = f.c;      // keep the fitted candidate
+          f.seed = f.c;  // keep the fitted candidate
           f.c = f.best;
         }
         __syncthreads();
@@ -1124,6 +1313,7 @@ __global__ void __launch_bounds__(256) refine_kernel(RefineArgs a) {
     r.score = f.c.score;
     r.ok = (f.c.score >= a.min_score) && inside_image(f.c.row, f.c.col, a.height, a.width);
     r.pad = 0;
+    r.rect = make_rect(f.c, a.geom);
     a.refined[i] = r;
     __threadfence();
     a.refined_flag[i] = 2;
@@ -1177,7 +1367,7 @@ cudaError_t launch_nms(const NmsArgs& a, cudaStream_t s) {
 }
 
 cudaError_t launch_track(const TrackArgs& a, int max_candidates, cudaStream_t s) {
-  track_kernel<<<max_candidates, 256, 0, s>>>(a);
+  track_kernel<<<max_candidates, kTrackThreads, 0, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -1194,7 +1384,7 @@ cudaError_t launch_score(const ScoreArgs& a, int max_candidates, cudaStream_t s)
 }
 
 cudaError_t launch_sort(const SortArgs& a, cudaStream_t s) {
-  const size_t smem = 16384 * (sizeof(double) + sizeof(int));
+  const size_t smem = 16384 * (sizeof(unsigned long long) + sizeof(int));
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
@@ -1204,13 +1394,19 @@ cudaError_t launch_sort(const SortArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+cudaError_t launch_rects(const Cand* sorted, RectAux* aux, const QueryState* state, RectGeom g, int max_candidates,
+                         cudaStream_t s) {
+  rects_kernel<<<unsigned((max_candidates + 255) / 256), 256, 0, s>>>(sorted, aux, state, g);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_select(const SelectArgs& a, cudaStream_t s) {
-  select_kernel<<<1, 256, 0, s>>>(a);
+  select_kernel<<<1, kSelectThreads, 0, s>>>(a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_refine(const RefineArgs& a, int batch_limit, cudaStream_t s) {
-  refine_kernel<<<batch_limit, 256, 0, s>>>(a);
+  refine_kernel<<<batch_limit, kRefineThreads, 0, s>>>(a);
   return cudaGetLastError();
 }
 

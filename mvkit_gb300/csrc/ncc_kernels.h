@@ -38,7 +38,8 @@ struct NmsArgs {
   int nplist, w, h;
   const int32_t* plist;
   LevelView view;
-  double crop_row, crop_col, scale, phase, threshold;
+  double crop_row, crop_col, scale, phase;
+  float threshold;          // smallest float f with double(f) >= 0.4 * MinScore
   Cand* out;
   QueryState* state;
   int max_candidates;
@@ -50,11 +51,16 @@ struct TrackArgs {
   const int32_t* plist;     // query patches of level t, reference iteration order
   const PosRange* ranges;   // per plist entry
   int nplist;
+  // patches of level t inside the angle window of each source patch of level
+  // t+1, as plist entries in reference order (CSR by source patch index)
+  const int32_t* sel_off;
+  const int32_t* sel_idx;
   const Cand* in;
   Cand* out;
   QueryState* state;
   int in_slot;              // state->count index holding the input count
-  double crop_row, crop_col, step, offset, angle_limit;
+  double crop_row, crop_col, step, offset;
+  int exact32;              // lattice arithmetic is exact in FP32 (host-checked)
   int absolute;
 };
 
@@ -91,18 +97,26 @@ struct SortArgs {
   int slot;
 };
 
+// Level-0 model rectangle about the origin: [left, right] x [top, bottom]
+// (src/ncc_matching/matcher.cpp:257-258).
+struct RectGeom {
+  double left, right, top, bottom, area;
+};
+
 // Refinement / selection
 struct SelectArgs {
   const Cand* sorted;
+  const RectAux* aux;       // per sorted candidate
   Refined* refined;         // per sorted index
   int32_t* refined_flag;    // 0 none, 1 queued, 2 done
   int32_t* batch;           // indices to refine next
   Cand* accepted;
+  RectAux* accepted_aux;
   QueryState* state;
   int batch_limit;
   int64_t num_matches;
   double max_overlap;
-  double tmpl_w, tmpl_h, tmpl_orow, tmpl_ocol;  // level-0 model rectangle
+  RectGeom geom;
 };
 
 struct RefineArgs {
@@ -122,6 +136,7 @@ struct RefineArgs {
   double angle_start, angle_end, angle_step, min_score;
   int rotate, subpixel, absolute, top, finest;
   double height, width;     // full image (domain test)
+  RectGeom geom;
 };
 
 cudaError_t launch_pyramid0(const void* src, int type, int64_t pitch_elems, int crop_row, int crop_col, LevelImage dst,
@@ -134,6 +149,8 @@ cudaError_t launch_track(const TrackArgs& a, int max_candidates, cudaStream_t s)
 cudaError_t launch_dedup(const DedupArgs& a, int max_candidates, cudaStream_t s);
 cudaError_t launch_score(const ScoreArgs& a, int max_candidates, cudaStream_t s);
 cudaError_t launch_sort(const SortArgs& a, cudaStream_t s);
+cudaError_t launch_rects(const Cand* sorted, RectAux* aux, const QueryState* state, RectGeom g, int max_candidates,
+                         cudaStream_t s);
 cudaError_t launch_select(const SelectArgs& a, cudaStream_t s);
 cudaError_t launch_refine(const RefineArgs& a, int batch_limit, cudaStream_t s);
 

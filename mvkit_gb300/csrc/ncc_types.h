@@ -2,6 +2,8 @@
 #pragma once
 #include <cstdint>
 
+#include <vector_types.h>
+
 namespace mvg {
 
 constexpr int kMaxLevels = 16;
@@ -38,6 +40,7 @@ struct LevelView {
   const PatchDesc* patches;
   const int32_t* offs;          // packed (row << 16) | (col & 0xffff), int16 each
   const float* w;               // sample weights (float of the FP64 model weight)
+  const int2* sw;               // interleaved {offs, float bits of w} per sample
   const int32_t* runs;          // packed row(16) | begin; end in runs_end
   const int32_t* runs_end;
   int32_t npatches;
@@ -57,6 +60,15 @@ struct OriginalView {
 struct Cand {
   double row, col, angle;
   double score;
+  int32_t patch;                // patch index on the candidate's level (-1 off the lattice)
+  int32_t pad;
+};
+
+// Rotated template rectangle of a pose for the MaxOverlap test: FP64 cos/sin
+// and a conservative FP32 axis-aligned box in image coordinates.
+struct RectAux {
+  double ca, sa;
+  float x0, y0, x1, y1;
 };
 
 // Result of refining one candidate (src/ncc_matching/matcher.cpp:878-1061).
@@ -64,6 +76,7 @@ struct Refined {
   double row, col, angle, score;
   int32_t ok;                   // score >= MinScore and inside the domain
   int32_t pad;
+  RectAux rect;
 };
 
 // Per-query device state that kernels read and write.
