@@ -181,6 +181,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--batch", type=int, default=8, help="scenes per step")
+    ap.add_argument("--streams", type=int, default=8, help="finds in flight (host threads, one stream each)")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -207,8 +208,8 @@ def main():
     model = mg.create_ncc_model(wls[0].template, **CREATE)
     ctl = (FIND["angle_start"], FIND["angle_extent"], FIND["min_score"], FIND["num_matches"], FIND["max_overlap"],
            FIND["subpixel"], FIND["num_levels"])
-    stream = torch.cuda.Stream()
-    sp = stream.cuda_stream
+    threads = max(1, min(args.streams, args.batch))
+    streams = [torch.cuda.Stream() for _ in range(threads)]
     dev = [mg.DeviceImage(w.image) for w in wls]
     pinned = []
     for w in wls:
@@ -218,29 +219,50 @@ def main():
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
     found = []
 
-    def one_step(images, location_host: bool):
+    from concurrent.futures import ThreadPoolExecutor
+    pool = ThreadPoolExecutor(threads)
+    profiles = []
+
+    def worker(j, images, location_host: bool, ends, profile: bool):
+        # each host thread owns one stream and the library's per-thread workspace
+        torch.cuda.set_device(local)
+        st = streams[j]
+        if profile:
+            mg.profile_reset()
+            mg.profile_enable(True)
         out = []
-        for im in images:
-            if location_host:
-                out.append(mg.find_ncc_model(im.array, model, *ctl, stream=sp))
-            else:
-                out.append(mg.find_ncc_model(im, model, *ctl, stream=sp))
+        for im in images[j::threads]:
+            arg = im.array if location_host else im
+            out.append(mg.find_ncc_model(arg, model, *ctl, stream=st.cuda_stream))
+        if ends is not None:
+            ends[j].record(st)
+        if profile:
+            mg.profile_enable(False)
+            profiles.append(mg.profile_read())
         return out
 
-    def timed(images, host: bool, steps: int):
+    def one_step(images, location_host: bool, ends=None, profile=False):
+        futs = [pool.submit(worker, j, images, location_host, ends, profile) for j in range(threads)]
+        res = [f.result() for f in futs]
+        out = []
+        for i in range(len(images)):
+            out.append(res[i % threads][i // threads])
+        return out
+
+    def timed(images, host: bool, steps: int, profile=False):
         total = 0.0
-        with torch.cuda.stream(stream):
-            for _ in range(steps):
-                flush.zero_()
-                torch.cuda.synchronize()
-                if world > 1:
-                    torch.distributed.barrier()
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-                found[:] = one_step(images, host)
-                e1.record(stream)
-                torch.cuda.synchronize()
-                total += e0.elapsed_time(e1)
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            if world > 1:
+                torch.distributed.barrier()
+            e0 = torch.cuda.Event(enable_timing=True)
+            ends = [torch.cuda.Event(enable_timing=True) for _ in range(threads)]
+            e0.record(streams[0])
+            torch.cuda.synchronize()
+            found[:] = one_step(images, host, ends, profile)
+            torch.cuda.synchronize()
+            total += max(e0.elapsed_time(e) for e in ends)
         return total
 
     for _ in range(args.warmup):
@@ -248,12 +270,17 @@ def main():
         one_step(pinned, True)
     torch.cuda.synchronize()
 
-    mg.profile_reset()
-    mg.profile_enable(True)
     with ClockSampler(local) as clocks:
-        dev_ms = timed(dev, False, args.steps)
-    mg.profile_enable(False)
-    prof = mg.profile_read()
+        dev_ms = timed(dev, False, args.steps, profile=True)
+    prof = {}
+    for p in profiles:
+        for k, v in p.items():
+            if k == "finds":
+                prof["finds"] = prof.get("finds", 0) + v
+                continue
+            acc = prof.setdefault(k, dict(ms=0.0, launches=0, work=0.0))
+            for f in ("ms", "launches", "work"):
+                acc[f] += v[f]
     host_ms = timed(pinned, True, args.steps)
 
     def maxed(x):
@@ -302,7 +329,8 @@ def main():
         "config": {"workload": WORKLOAD, "image": "2048x2048 u8", "template": "128x128", "poses": 5,
                    "angle_range_deg": [-30, 30], "num_levels": 4, "min_score": 0.7, "num_matches": 5,
                    "max_overlap": 0.5, "scenes_per_step": args.batch, "l2": "flushed (256 MiB write) between steps",
-                   "parallelism": f"replicas x{world}", "path": "plain FP32 CUDA-core correlation"},
+                   "finds_in_flight": threads, "parallelism": f"replicas x{world}",
+                   "path": "plain FP32 CUDA-core correlation"},
         "e2e": {"value": e2e, "unit": "images/s",
                 "h2d_bytes_per_step": int(sum(w.image.nbytes for w in wls)),
                 "d2h_bytes_per_step": int(args.batch * (4 * 8 * FIND["num_matches"] + 128))},

@@ -268,6 +268,8 @@ struct Workspace {
   DevBuf<float> planes;
   DevBuf<Cand> cand_a, cand_b, tmp, sorted, accepted;
   DevBuf<RectAux> aux, accepted_aux;
+  DevBuf<int32_t> tested;
+  DevBuf<uint8_t> sup;
   DevBuf<int> table;
   DevBuf<Refined> refined;
   DevBuf<int32_t> refined_flag, batch;
@@ -300,6 +302,8 @@ struct Workspace {
     accepted.reserve(kMaxCandidates);
     aux.reserve(kMaxCandidates);
     accepted_aux.reserve(kMaxCandidates);
+    tested.reserve(kMaxCandidates);
+    sup.reserve(kMaxCandidates);
     table.reserve(kHashSlots);
     refined.reserve(kMaxCandidates);
     refined_flag.reserve(kMaxCandidates);
@@ -778,7 +782,11 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
 
   // greedy selection with refinement (matcher.cpp:1063-1076)
   check(cudaMemsetAsync(ws.refined_flag.p, 0, sizeof(int32_t) * kMaxCandidates, s), "memset");
-  const int batch_limit = int(std::min<int64_t>(64, opt.num_matches > 0 ? 2 * opt.num_matches + 6 : 32));
+  check(cudaMemsetAsync(ws.tested.p, 0, sizeof(int32_t) * kMaxCandidates, s), "memset");
+  check(cudaMemsetAsync(ws.sup.p, 0, kMaxCandidates, s), "memset");
+  // speculative refinement batch: the next NumMatches unsuppressed,
+  // mutually non-overlapping candidates (32 when all matches are wanted)
+  const int batch_limit = int(std::min<int64_t>(64, opt.num_matches > 0 ? opt.num_matches : 32));
   RectGeom geom;
   geom.left = -base.ocol - .5;
   geom.right = double(base.width) - base.ocol - .5;
@@ -793,6 +801,8 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   se.batch = ws.batch.p;
   se.accepted = ws.accepted.p;
   se.accepted_aux = ws.accepted_aux.p;
+  se.tested = ws.tested.p;
+  se.sup = ws.sup.p;
   se.state = st;
   se.batch_limit = batch_limit;
   se.num_matches = opt.num_matches;

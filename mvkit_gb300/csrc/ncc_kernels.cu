@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(kTrackThreads) track_kernel(TrackArgs a) {
   if (i >= a.state->count[a.in_slot]) return;
   __shared__ int s_sel[kTrackMaxSel];
   __shared__ int s_row[kTrackMaxSel], s_col[kTrackMaxSel];
-  __shared__ int s_n, s_split, s_wr0, s_wc0, s_ww, s_wh, s_staged;
+  __shared__ int s_n, s_split, s_wr0, s_wc0, s_ww, s_wh, s_wcols, s_staged;
   __shared__ float s_part[kTrackThreads];
   __shared__ float s_wbest[kTrackThreads / 32];
   __shared__ int s_word[kTrackThreads / 32];
@@ -316,7 +316,10 @@ __global__ void __launch_bounds__(kTrackThreads) track_kernel(TrackArgs a) {
     s_wr0 = any ? wr0 : 0;
     s_wc0 = any ? wc0 : 0;
     s_wh = any ? wr1 - wr0 + 1 : 0;
-    s_ww = any ? wc1 - wc0 + 1 : 0;
+    s_wcols = any ? wc1 - wc0 + 1 : 0;
+    // row pitch = 5 (mod 32): the 5x5 placements of one patch read 25
+    // distinct shared-memory banks
+    s_ww = s_wcols + ((5 - s_wcols) % 32 + 32) % 32;
     s_staged = any && s_wh * s_ww <= kTrackWindow;
   }
   __syncthreads();
@@ -328,10 +331,10 @@ __global__ void __launch_bounds__(kTrackThreads) track_kernel(TrackArgs a) {
   const int wr0 = staged ? s_wr0 : 0, wc0 = staged ? s_wc0 : 0;
   const float* img = staged ? win : a.lev.v;
   if (staged) {
-    const int cells = s_wh * s_ww;
+    const int cols = s_wcols, cells = s_wh * cols;
     for (int t = threadIdx.x; t < cells; t += kTrackThreads) {
-      const int rr = t / s_ww, cc = t % s_ww;
-      win[t] = a.lev.v[size_t(s_wr0 + rr) * pitch + s_wc0 + cc];
+      const int rr = t / cols, cc = t % cols;
+      win[rr * s_ww + cc] = a.lev.v[size_t(s_wr0 + rr) * pitch + s_wc0 + cc];
     }
   }
   __syncthreads();
@@ -340,13 +343,15 @@ __global__ void __launch_bounds__(kTrackThreads) track_kernel(TrackArgs a) {
   const int items = n * 25;
   const int passes = (items * split + kTrackThreads - 1) / kTrackThreads;
   for (int pass = 0; pass < passes; ++pass) {
+    // slices are part-major: the lanes of a warp work on neighbouring
+    // placements of one sample (broadcast sample loads)
     const int t = pass * kTrackThreads + threadIdx.x;
-    const int item = t / split, part = t % split;
+    const int item = split > 1 ? t % items : t, part = split > 1 ? t / items : 0;
     bool valid = false;
     int r = 0, c = 0;
     PatchDesc pd{};
     float acc = 0.f;
-    if (item < items) {
+    if (item < items && part < split) {
       const int k = item / 25, pos = item % 25;
       const int j = s_sel[k];
       pd = a.view.patches[a.plist[j]];
@@ -380,7 +385,7 @@ __global__ void __launch_bounds__(kTrackThreads) track_kernel(TrackArgs a) {
     }
     if (part == 0 && valid) {
       float dot = acc;
-      for (int q = 1; q < split; ++q) dot += s_part[threadIdx.x + q];
+      for (int q = 1; q < split; ++q) dot += s_part[threadIdx.x + q * items];
       long long s1, s2;
       window_moments(a.lev.prefix, pitch + 1, r, c, a.view.runs + pd.run_off, a.view.runs_end + pd.run_off,
                      pd.nruns, s1, s2);
@@ -778,6 +783,61 @@ __device__ double overlap_ratio(const Cand& a, const RectAux& ra, const Cand& b,
   return fabs(area) * .5 / g.area;
 }
 
+// The same clip in FP32 (corners relative to a's centre are small numbers):
+// within 1e-3 of the true ratio, used to decide clear cases without FP64.
+__device__ float overlap_ratio32(const Cand& a, const RectAux& ra, const Cand& b, const RectAux& rb, const RectGeom& g) {
+  if (boxes_disjoint(ra, rb)) return 0.f;
+  const float L = float(g.left), R = float(g.right), T = float(g.top), B = float(g.bottom);
+  const float inx[4] = {L, R, R, L}, iny[4] = {T, T, B, B};
+  const float dx = float(b.col - a.col), dy = float(b.row - a.row);
+  const float bca = float(rb.ca), bsa = float(rb.sa), aca = float(ra.ca), asa = float(ra.sa);
+  float cx[4], cy[4], px[16], py[16], nx[16], ny[16];
+  for (int i = 0; i < 4; ++i) {
+    cx[i] = dx + bca * inx[i] + bsa * iny[i];
+    cy[i] = dy - bsa * inx[i] + bca * iny[i];
+    px[i] = aca * inx[i] + asa * iny[i];
+    py[i] = -asa * inx[i] + aca * iny[i];
+  }
+  int count = 4;
+  for (int edge = 0; edge < 4 && count; ++edge) {
+    const float p0x = cx[edge], p0y = cy[edge], qx = cx[(edge + 1) & 3], qy = cy[(edge + 1) & 3];
+    int out = 0;
+    for (int i = 0; i < count; ++i) {
+      const int j = (i + 1) % count;
+      const float du = (qx - p0x) * (py[i] - p0y) - (qy - p0y) * (px[i] - p0x);
+      const float dv = (qx - p0x) * (py[j] - p0y) - (qy - p0y) * (px[j] - p0x);
+      if (du >= 0 && out < 16) {
+        nx[out] = px[i];
+        ny[out++] = py[i];
+      }
+      if ((du >= 0) != (dv >= 0) && out < 16) {
+        const float t = du / (du - dv);
+        nx[out] = px[i] + t * (px[j] - px[i]);
+        ny[out++] = py[i] + t * (py[j] - py[i]);
+      }
+    }
+    for (int i = 0; i < out; ++i) {
+      px[i] = nx[i];
+      py[i] = ny[i];
+    }
+    count = out;
+  }
+  float area = 0;
+  for (int i = 0; i < count; ++i) area += px[i] * py[(i + 1) % count] - px[(i + 1) % count] * py[i];
+  return fabsf(area) * .5f / float(g.area);
+}
+
+// overlap(a, b) > thr, deciding in FP32 when the FP32 ratio is clearly on
+// one side and in FP64 otherwise.
+__device__ __forceinline__ bool overlaps(const Cand& a, const RectAux& ra, const Cand& b, const RectAux& rb,
+                                         const RectGeom& g, double thr) {
+  if (boxes_disjoint(ra, rb)) return 0. > thr;
+  const float r32 = overlap_ratio32(a, ra, b, rb, g);
+  if (double(r32) > thr + 1e-3) return true;
+  if (double(r32) < thr - 1e-3) return false;
+  return overlap_ratio(a, ra, b, rb, g) > thr;
+}
+
 __global__ void rects_kernel(const Cand* sorted, RectAux* aux, const QueryState* state, RectGeom g) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= state->sorted_count) return;
@@ -809,17 +869,23 @@ __global__ void __launch_bounds__(kSelectThreads) select_kernel(SelectArgs a) {
   while (true) {
     const int base = s_next, acc = s_acc;
     if (base >= total || (a.num_matches && acc >= a.num_matches)) break;
-    // suppression of the window by the accepted matches
+    // suppression of the window by the accepted matches; each candidate is
+    // tested only against matches accepted since its last test
     const int wcount = min(kSelectThreads, total - base);
     const int t = threadIdx.x;
     bool sup = true;
     if (t < wcount) {
       const int idx = base + t;
-      const Cand c = a.sorted[idx];
-      const RectAux rc = a.aux[idx];
-      sup = false;
-      for (int j = 0; j < acc && !sup; ++j)
-        if (overlap_ratio(c, rc, a.accepted[j], a.accepted_aux[j], a.geom) > thr) sup = true;
+      sup = a.sup[idx] != 0;
+      const int from = a.tested[idx];
+      if (!sup && from < acc) {
+        const Cand c = a.sorted[idx];
+        const RectAux rc = a.aux[idx];
+        for (int j = from; j < acc && !sup; ++j)
+          if (overlaps(c, rc, a.accepted[j], a.accepted_aux[j], a.geom, thr)) sup = true;
+        a.tested[idx] = acc;
+        if (sup) a.sup[idx] = 1;
+      }
     }
     s_sup[t] = sup ? 1 : 0;
     if (t == 0) s_first = INT32_MAX;
@@ -881,7 +947,7 @@ __global__ void __launch_bounds__(kSelectThreads) select_kernel(SelectArgs a) {
     __syncthreads();
     if (keep)
       for (int j = threadIdx.x; j < acc; j += kSelectThreads)
-        if (overlap_ratio(rc, r.rect, a.accepted[j], a.accepted_aux[j], a.geom) > thr) s_hit = 1;
+        if (overlaps(rc, r.rect, a.accepted[j], a.accepted_aux[j], a.geom, thr)) s_hit = 1;
     __syncthreads();
     if (threadIdx.x == 0) {
       if (keep && !s_hit) {
@@ -978,37 +1044,54 @@ __device__ void gn_pass(const ImageView& img, const OriginalView& orig, double r
   }
   F2 t[19];
   block_total<19>(acc, t, sh.scratch);
-  if (threadIdx.x == 0) {
-    sh.ok = 0;
-    sh.gscore = -INFINITY;
-    sh.delta[0] = sh.delta[1] = sh.delta[2] = 0;
+  if (threadIdx.x < 32) {
+    // totals from lane 0 to the warp; every lane evaluates the scalar terms,
+    // lane l < axes*(axes+1) one matrix/rhs entry, lane 0 the elimination
+    const int lane = threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < 19; ++k) {
+      t[k].hi = __shfl_sync(0xffffffffu, t[k].hi, 0);
+      t[k].lo = __shfl_sync(0xffffffffu, t[k].lo, 0);
+    }
     const F2 n = f2(float(orig.n));
     const F2 sum = t[0], dot = t[2];
     const F2 energy = f2_sub(t[1], f2_div(f2_mul(sum, sum), n));
     const float ef = f2_val(energy);
-    if (!(t[18].hi > 0) && ef > 0) {
-      const float sign = absolute && f2_val(dot) < 0 ? -1.f : 1.f;
-      const float sq = sqrtf(ef);
-      const float score = sign * f2_val(dot) / sq;
-      sh.gscore = double(fminf(1.f, fmaxf(-1.f, score)));
-      if (!(use_minimum && sh.gscore <= minimum)) {
-        const int axes = rotate ? 3 : 2;
-        const F2 gs[3] = {t[3], t[4], t[5]}, wg[3] = {t[9], t[10], t[11]};
-        F2 qg[3] = {t[6], t[7], t[8]};
-        const F2 gg[3][3] = {{t[12], t[13], t[15]}, {t[13], t[14], t[16]}, {t[15], t[16], t[17]}};
-        const F2 sn = f2_div(sum, n);
-        for (int i = 0; i < axes; ++i) qg[i] = f2_sub(qg[i], f2_mul(sn, gs[i]));
-        // entries in pair arithmetic, then FP64 for the elimination
-        const F2 inv_e = f2_div(f2(1.f), energy);
-        double m[3][4];
-        for (int i = 0; i < axes; ++i) {
-          for (int j = 0; j < axes; ++j) {
-            const F2 e = f2_sub(f2_sub(gg[i][j], f2_div(f2_mul(gs[i], gs[j]), n)), f2_mul(f2_mul(qg[i], qg[j]), inv_e));
-            m[i][j] = f2_dbl(f2_mul(e, inv_e));
-          }
-          const F2 r = f2_sub(f2_mul(f2(sign / sq), wg[i]), f2_mul(f2_mul(f2(score), qg[i]), inv_e));
-          m[i][axes] = f2_dbl(r);
-        }
+    const bool scored = !(t[18].hi > 0) && ef > 0;
+    const float sign = absolute && f2_val(dot) < 0 ? -1.f : 1.f;
+    const float sq = scored ? sqrtf(ef) : 1.f;
+    const float score = sign * f2_val(dot) / sq;
+    const double gscore = scored ? double(fminf(1.f, fmaxf(-1.f, score))) : -INFINITY;
+    const bool solve = scored && !(use_minimum && gscore <= minimum);
+    const int axes = rotate ? 3 : 2;
+    double entry = 0;
+    if (solve && lane < axes * (axes + 1)) {
+      const int i = lane / (axes + 1), j = lane % (axes + 1);
+      const F2 gs[3] = {t[3], t[4], t[5]}, wg[3] = {t[9], t[10], t[11]};
+      const F2 gg[3][3] = {{t[12], t[13], t[15]}, {t[13], t[14], t[16]}, {t[15], t[16], t[17]}};
+      const F2 sn = f2_div(sum, n);
+      const F2 inv_e = f2_div(f2(1.f), energy);
+      const F2 qi = f2_sub(t[6 + i], f2_mul(sn, gs[i]));
+      if (j < axes) {
+        const F2 qj = f2_sub(t[6 + j], f2_mul(sn, gs[j]));
+        const F2 e = f2_sub(f2_sub(gg[i][j], f2_div(f2_mul(gs[i], gs[j]), n)), f2_mul(f2_mul(qi, qj), inv_e));
+        entry = f2_dbl(f2_mul(e, inv_e));
+      } else {
+        entry = f2_dbl(f2_sub(f2_mul(f2(sign / sq), wg[i]), f2_mul(f2_mul(f2(score), qi), inv_e)));
+      }
+    }
+    double m[3][4];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 4; ++j) m[i][j] = 0;
+    for (int l = 0; l < axes * (axes + 1); ++l) {
+      const double v = __shfl_sync(0xffffffffu, entry, l);
+      m[l / (axes + 1)][l % (axes + 1)] = v;
+    }
+    if (lane == 0) {
+      sh.ok = 0;
+      sh.gscore = gscore;
+      sh.delta[0] = sh.delta[1] = sh.delta[2] = 0;
+      if (solve) {
         bool good = true;
         for (int i = 0; i < axes && good; ++i) {
           int pivot = i;

@@ -112,6 +112,8 @@ struct SelectArgs {
   int32_t* batch;           // indices to refine next
   Cand* accepted;
   RectAux* accepted_aux;
+  int32_t* tested;          // per sorted candidate: accepted matches it was tested against
+  uint8_t* sup;             // per sorted candidate: suppressed by an accepted match
   QueryState* state;
   int batch_limit;
   int64_t num_matches;
