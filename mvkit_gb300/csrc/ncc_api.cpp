@@ -58,16 +58,24 @@ template <class T> struct DevBuf {
 
 // ------------------------------------------------------------------ model
 struct DevLevel {
+  int32_t lin_pitch = 0, lin_rows = 0;  // staged tracking window geometry
   std::vector<PatchDesc> desc;      // host copy (model patches + query endpoints)
   std::vector<double> angles;
   size_t model_patches = 0;         // trained patches; endpoints follow
   std::vector<int32_t> offs, runs, runs_end;
   std::vector<float> w;
-  std::vector<int2> sw;
+  std::vector<int2> sw, lw;
   DevBuf<PatchDesc> d_desc;
   DevBuf<int32_t> d_offs, d_runs, d_runs_end;
   DevBuf<float> d_w;
-  DevBuf<int2> d_sw;
+  DevBuf<int2> d_sw, d_lw;
+  // Window geometry for a level of width x height: any rotation's raster
+  // fits the diagonal; 5x5 placements and centre rounding add 8 cells.
+  void set_geometry(size_t width, size_t height) {
+    const int diag = int(std::ceil(std::hypot(double(width), double(height)))) + 1;
+    lin_rows = diag + 8;
+    lin_pitch = lin_rows + ((5 - lin_rows) % 32 + 32) % 32;
+  }
   void append(const Raster& r) {
     PatchDesc d{};
     d.angle = r.angle;
@@ -81,6 +89,7 @@ struct DevLevel {
     d.sample_off = int32_t(offs.size());
     d.nruns = int32_t(r.run_row.size());
     d.run_off = int32_t(runs.size());
+    double wsum = 0;
     for (size_t i = 0; i < r.size(); ++i) {
       const int32_t o = int32_t((uint32_t(uint16_t(int16_t(r.rows[i]))) << 16) | uint16_t(int16_t(r.cols[i])));
       const float wf = float(r.w[i]);
@@ -89,7 +98,10 @@ struct DevLevel {
       offs.push_back(o);
       w.push_back(wf);
       sw.push_back(make_int2(o, wbits));
+      lw.push_back(make_int2(r.rows[i] * lin_pitch + r.cols[i], wbits));
+      wsum += double(wf);
     }
+    d.wsum = float(wsum);
     for (size_t j = 0; j < r.run_row.size(); ++j) {
       runs.push_back(int32_t((uint32_t(uint16_t(int16_t(r.run_row[j]))) << 16) | uint16_t(int16_t(r.run_begin[j]))));
       runs_end.push_back(r.run_end[j]);
@@ -115,8 +127,10 @@ struct DevLevel {
     retire(d_runs_end);
     retire(d_w);
     retire(d_sw);
+    retire(d_lw);
     d_desc.upload(desc, nullptr);
     d_sw.upload(sw, nullptr);
+    d_lw.upload(lw, nullptr);
     d_offs.upload(offs, nullptr);
     d_runs.upload(runs, nullptr);
     d_runs_end.upload(runs_end, nullptr);
@@ -129,6 +143,9 @@ struct DevLevel {
     v.offs = d_offs.p;
     v.w = d_w.p;
     v.sw = d_sw.p;
+    v.lw = d_lw.p;
+    v.lin_pitch = lin_pitch;
+    v.lin_rows = lin_rows;
     v.runs = d_runs.p;
     v.runs_end = d_runs_end.p;
     v.npatches = int32_t(desc.size());
@@ -720,7 +737,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
       ta.exact32 = exact32;
       ta.absolute = hm.params.ignore_polarity;
       Span sp(kStTrack, s);
-      check(launch_track(ta, kMaxCandidates, s), "track");
+      check(launch_track(ta, kMaxCandidates, s, ws.smem_optin), "track");
     }
     check(cudaMemsetAsync(ws.table.p, 0xff, sizeof(int) * kHashSlots, s), "memset");
     DedupArgs da;
@@ -934,6 +951,7 @@ int32_t mvg_create_ncc_model(const void* pixels, int32_t pixel_type, int64_t wid
     check(cudaGetDevice(&m->device), "cudaGetDevice");
     for (const ModelLevel& L : m->host.levels) {
       auto d = std::make_unique<DevLevel>();
+      d->set_geometry(L.width, L.height);
       for (const Raster& r : L.patches) d->append(r);
       d->model_patches = d->desc.size();
       d->upload();

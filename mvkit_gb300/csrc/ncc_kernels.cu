@@ -251,24 +251,30 @@ __global__ void nms_kernel(NmsArgs a) {
 // One block per candidate: the target level's query patches inside the
 // candidate's angle window (a precomputed list per source patch), 5x5
 // positions each; the first strict maximum in (patch order, dr, dc) wins
-// (src/ncc_matching/matcher.cpp:670-757).  The union image window of all
-// those placements is staged in shared memory; each thread scores one
-// (patch, position) item, or a slice of its samples when items are few.
+// (src/ncc_matching/matcher.cpp:670-757).
+//
+// The union image window of all those placements is staged in shared memory,
+// centred on one of its pixels (exact small integers in float) with the
+// level's fixed row pitch, so each sample costs one shared load and one FMA
+// against precomputed linear offsets.  Each thread scores one (patch,
+// position) item, or a slice of its samples when items are few.  Windows
+// larger than the level's staged geometry read the level directly.
 constexpr int kTrackThreads = 256;
 constexpr int kTrackMaxSel = 64;
-constexpr int kTrackWindow = 12288;  // floats of staged image (48 KiB)
 
 __global__ void __launch_bounds__(kTrackThreads) track_kernel(TrackArgs a) {
+  extern __shared__ float win[];
   const int i = blockIdx.x;
   if (i >= a.state->count[a.in_slot]) return;
   __shared__ int s_sel[kTrackMaxSel];
   __shared__ int s_row[kTrackMaxSel], s_col[kTrackMaxSel];
-  __shared__ int s_n, s_split, s_wr0, s_wc0, s_ww, s_wh, s_wcols, s_staged;
+  __shared__ int s_n, s_split, s_wr0, s_wc0, s_wh, s_wcols, s_staged;
+  __shared__ float s_centre;
   __shared__ float s_part[kTrackThreads];
   __shared__ float s_wbest[kTrackThreads / 32];
   __shared__ int s_word[kTrackThreads / 32];
-  __shared__ float win[kTrackWindow];
   const Cand cd = a.in[i];
+  const int WW = a.view.lin_pitch;
   if (threadIdx.x == 0) {
     const int src = cd.patch;
     const int b = src >= 0 ? a.sel_off[src] : 0, e = src >= 0 ? a.sel_off[src + 1] : 0;
@@ -317,24 +323,20 @@ __global__ void __launch_bounds__(kTrackThreads) track_kernel(TrackArgs a) {
     s_wc0 = any ? wc0 : 0;
     s_wh = any ? wr1 - wr0 + 1 : 0;
     s_wcols = any ? wc1 - wc0 + 1 : 0;
-    // row pitch = 5 (mod 32): the 5x5 placements of one patch read 25
-    // distinct shared-memory banks
-    s_ww = s_wcols + ((5 - s_wcols) % 32 + 32) % 32;
-    s_staged = any && s_wh * s_ww <= kTrackWindow;
+    s_staged = any && s_wh <= a.view.lin_rows && s_wcols <= WW && a.staged_ok;
+    s_centre = any ? a.lev.v[size_t(wr0 + (wr1 - wr0) / 2) * a.lev.w + wc0 + (wc1 - wc0) / 2] : 0.f;
   }
   __syncthreads();
   const int n = s_n, split = s_split;
   const int pitch = a.lev.w;
   const bool staged = s_staged != 0;
-  const int ww = staged ? s_ww : pitch;
-  // staged: window coordinates; else: the level itself with a zero origin
-  const int wr0 = staged ? s_wr0 : 0, wc0 = staged ? s_wc0 : 0;
-  const float* img = staged ? win : a.lev.v;
+  const int wr0 = s_wr0, wc0 = s_wc0;
+  const float centre = s_centre;
   if (staged) {
     const int cols = s_wcols, cells = s_wh * cols;
     for (int t = threadIdx.x; t < cells; t += kTrackThreads) {
       const int rr = t / cols, cc = t % cols;
-      win[rr * s_ww + cc] = a.lev.v[size_t(s_wr0 + rr) * pitch + s_wc0 + cc];
+      win[rr * WW + cc] = a.lev.v[size_t(wr0 + rr) * pitch + wc0 + cc] - centre;
     }
   }
   __syncthreads();
@@ -350,7 +352,7 @@ __global__ void __launch_bounds__(kTrackThreads) track_kernel(TrackArgs a) {
     bool valid = false;
     int r = 0, c = 0;
     PatchDesc pd{};
-    float acc = 0.f;
+    float acc = 0.f, x0 = 0.f;
     if (item < items && part < split) {
       const int k = item / 25, pos = item % 25;
       const int j = s_sel[k];
@@ -360,25 +362,45 @@ __global__ void __launch_bounds__(kTrackThreads) track_kernel(TrackArgs a) {
       c = s_col[k] + pos % 5 - 2;
       valid = r >= rg.r0 && r < rg.r1 && c >= rg.c0 && c < rg.c1;
     }
-    if (valid) {
+    if (valid && staged) {
+      // sum w (S - centre); the first-sample shift is applied once below
+      const int2* lw = a.view.lw + pd.sample_off;
+      const float* base = win + (r - wr0) * WW + (c - wc0);
+      float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+      int s = part;
+      for (; s + 3 * split < pd.n; s += 4 * split) {
+        const int2 p0 = __ldg(lw + s), p1 = __ldg(lw + s + split), p2 = __ldg(lw + s + 2 * split),
+                   p3 = __ldg(lw + s + 3 * split);
+        a0 = fmaf(__int_as_float(p0.y), base[p0.x], a0);
+        a1 = fmaf(__int_as_float(p1.y), base[p1.x], a1);
+        a2 = fmaf(__int_as_float(p2.y), base[p2.x], a2);
+        a3 = fmaf(__int_as_float(p3.y), base[p3.x], a3);
+      }
+      for (; s < pd.n; s += split) {
+        const int2 p0 = __ldg(lw + s);
+        a0 = fmaf(__int_as_float(p0.y), base[p0.x], a0);
+      }
+      acc = (a0 + a1) + (a2 + a3);
+      if (part == 0) x0 = base[__ldg(lw).x];
+    } else if (valid) {
       const int2* sw = a.view.sw + pd.sample_off;
-      const float* base = img + size_t(r - wr0) * ww + (c - wc0);
+      const float* base = a.lev.v + size_t(r) * pitch + c;
       const int2 f0 = __ldg(sw);
-      const float s0 = base[off_row(f0.x) * ww + off_col(f0.x)];
+      const float s0 = base[off_row(f0.x) * pitch + off_col(f0.x)];
       float acc1 = 0.f;
       int s = part;
       for (; s + split < pd.n; s += 2 * split) {
         const int2 x = __ldg(sw + s), y = __ldg(sw + s + split);
-        acc = fmaf(__int_as_float(x.y), base[off_row(x.x) * ww + off_col(x.x)] - s0, acc);
-        acc1 = fmaf(__int_as_float(y.y), base[off_row(y.x) * ww + off_col(y.x)] - s0, acc1);
+        acc = fmaf(__int_as_float(x.y), base[off_row(x.x) * pitch + off_col(x.x)] - s0, acc);
+        acc1 = fmaf(__int_as_float(y.y), base[off_row(y.x) * pitch + off_col(y.x)] - s0, acc1);
       }
       if (s < pd.n) {
         const int2 x = __ldg(sw + s);
-        acc = fmaf(__int_as_float(x.y), base[off_row(x.x) * ww + off_col(x.x)] - s0, acc);
+        acc = fmaf(__int_as_float(x.y), base[off_row(x.x) * pitch + off_col(x.x)] - s0, acc);
       }
       acc += acc1;
     }
-    // combine the sample slices of one item (consecutive threads)
+    // combine the sample slices of one item (threads item + q * items)
     if (split > 1) {
       s_part[threadIdx.x] = acc;
       __syncthreads();
@@ -386,6 +408,8 @@ __global__ void __launch_bounds__(kTrackThreads) track_kernel(TrackArgs a) {
     if (part == 0 && valid) {
       float dot = acc;
       for (int q = 1; q < split; ++q) dot += s_part[threadIdx.x + q * items];
+      // sum w (S - S0) = sum w (S - centre) - (S0 - centre) sum w
+      if (staged) dot = fmaf(-x0, pd.wsum, dot);
       long long s1, s2;
       window_moments(a.lev.prefix, pitch + 1, r, c, a.view.runs + pd.run_off, a.view.runs_end + pd.run_off,
                      pd.nruns, s1, s2);
@@ -1449,8 +1473,22 @@ cudaError_t launch_nms(const NmsArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_track(const TrackArgs& a, int max_candidates, cudaStream_t s) {
-  track_kernel<<<max_candidates, kTrackThreads, 0, s>>>(a);
+cudaError_t launch_track(const TrackArgs& a, int max_candidates, cudaStream_t s, size_t smem_limit) {
+  TrackArgs b = a;
+  size_t smem = size_t(a.view.lin_pitch) * size_t(a.view.lin_rows) * sizeof(float);
+  const size_t fixed = 8 * 1024;  // static shared memory of the kernel
+  if (smem + fixed > smem_limit || smem > 160 * 1024) {
+    b.staged_ok = 0;
+    smem = 0;
+  } else {
+    b.staged_ok = 1;
+  }
+  static size_t attr = 0;
+  if (smem > attr) {
+    cudaFuncSetAttribute(track_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    attr = smem;
+  }
+  track_kernel<<<max_candidates, kTrackThreads, smem, s>>>(b);
   return cudaGetLastError();
 }
 

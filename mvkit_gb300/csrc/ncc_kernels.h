@@ -62,6 +62,7 @@ struct TrackArgs {
   double crop_row, crop_col, step, offset;
   int exact32;              // lattice arithmetic is exact in FP32 (host-checked)
   int absolute;
+  int staged_ok;            // set by the launcher: dynamic shared memory holds the window
 };
 
 struct DedupArgs {
@@ -147,7 +148,7 @@ cudaError_t launch_pyramid(const LevelImage& src, LevelImage dst, int32_t* error
 cudaError_t launch_prefix(const LevelImage& lev, cudaStream_t s);
 cudaError_t launch_coarse(const CoarseArgs& a, int max_bh, int max_bw, cudaStream_t s, size_t smem_limit);
 cudaError_t launch_nms(const NmsArgs& a, cudaStream_t s);
-cudaError_t launch_track(const TrackArgs& a, int max_candidates, cudaStream_t s);
+cudaError_t launch_track(const TrackArgs& a, int max_candidates, cudaStream_t s, size_t smem_limit);
 cudaError_t launch_dedup(const DedupArgs& a, int max_candidates, cudaStream_t s);
 cudaError_t launch_score(const ScoreArgs& a, int max_candidates, cudaStream_t s);
 cudaError_t launch_sort(const SortArgs& a, cudaStream_t s);

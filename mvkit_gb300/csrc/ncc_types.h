@@ -33,6 +33,8 @@ struct PatchDesc {
   int32_t sample_off;           // into the level's sample arrays
   int32_t nruns;                // contiguous row spans
   int32_t run_off;
+  float wsum;                   // sum of the float sample weights
+  int32_t pad_;
 };
 
 // Device view of one model level (its patches and their samples).
@@ -41,6 +43,9 @@ struct LevelView {
   const int32_t* offs;          // packed (row << 16) | (col & 0xffff), int16 each
   const float* w;               // sample weights (float of the FP64 model weight)
   const int2* sw;               // interleaved {offs, float bits of w} per sample
+  const int2* lw;               // interleaved {row * lin_pitch + col, float bits of w} per sample
+  int32_t lin_pitch;            // row pitch of lw offsets (= 5 mod 32)
+  int32_t lin_rows;             // rows of a window that holds any 5x5 placement set
   const int32_t* runs;          // packed row(16) | begin; end in runs_end
   const int32_t* runs_end;
   int32_t npatches;
