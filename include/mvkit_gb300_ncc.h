@@ -98,6 +98,29 @@ MVG_API int32_t mvg_ncc_pyramid_level(const void* pixels, int32_t pixel_type, in
                               int64_t row_stride, mvg_ncc_model model_id, int32_t highest_level, int32_t level,
                               float* out, int64_t capacity, double* geom);
 
+/* Search-pyramid level `level` of the whole image (sums of 4^level input
+ * pixels, the same values as mvg_ncc_pyramid_level) for callers that cannot
+ * allocate device memory: frameworks that own every device buffer through
+ * their own pool, real-time loops where an allocation may stall, processes
+ * with a device-memory budget fixed at start-up.  No counterpart in the
+ * reference (its pyramid is an internal step of the find).
+ *
+ * pixels: the image in device memory (row_stride bytes apart); out: a device
+ * buffer of out_capacity floats that receives the level, row-major,
+ * *out_width x *out_height.  Allocates nothing: the levels below the
+ * requested one are built in one fixed device array of 6 Mi floats (24 MiB)
+ * that the library holds on every GPU that loads it until the process exits;
+ * images whose lower levels need more than that are rejected with
+ * MV_STATUS_LIMIT_EXCEEDED (-103).  The first call on a device looks the
+ * array's device address up (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU (concurrent streams or threads on one
+ * device) race and must be serialised by the caller.  stream: a cudaStream_t
+ * or NULL; the call returns when the level is complete. */
+MVG_API int32_t mvg_ncc_pyramid_level_noalloc(const void* pixels, int32_t pixel_type, int64_t width, int64_t height,
+                                              int64_t row_stride, int32_t level, float* out, int64_t out_capacity,
+                                              int64_t* out_width, int64_t* out_height, void* stream);
+
 /* Thread-local message of the last failed call (empty after success). */
 MVG_API const char* mvg_last_error(void);
 

@@ -924,6 +924,10 @@ FindParams make_params(double angle_start, double angle_extent, double min_score
 }
 
 }  // namespace
+
+// Thread-local error message shared by every entry point of the library.
+void set_last_error(const char* message) { g_last_error = message ? message : ""; }
+
 }  // namespace mvg
 
 using namespace mvg;
