@@ -183,6 +183,9 @@ def main():
     ap.add_argument("--batch", type=int, default=8, help="scenes per step")
     ap.add_argument("--streams", type=int, default=8, help="finds in flight (host threads, one stream each)")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--path", default="tensor", choices=["tensor", "plain"],
+                    help="correlation path of the headline line (tensor cores or FP32 CUDA cores)")
+    ap.add_argument("--no-compare", action="store_true", help="skip timing the other correlation path")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -223,9 +226,12 @@ def main():
     pool = ThreadPoolExecutor(threads)
     profiles = []
 
+    path = [args.path]
+
     def worker(j, images, location_host: bool, ends, profile: bool):
         # each host thread owns one stream and the library's per-thread workspace
         torch.cuda.set_device(local)
+        mg.set_correlation_path(path[0])
         st = streams[j]
         if profile:
             mg.profile_reset()
@@ -265,6 +271,33 @@ def main():
             total += max(e0.elapsed_time(e) for e in ends)
         return total
 
+    def aggregate():
+        prof = {"finds": 0, "tensor_issued_macs": 0.0}
+        for p in profiles:
+            for k, v in p.items():
+                if k in ("finds", "tensor_issued_macs"):
+                    prof[k] += v
+                    continue
+                acc = prof.setdefault(k, dict(ms=0.0, launches=0, work=0.0))
+                for f in ("ms", "launches", "work"):
+                    acc[f] += v[f]
+        profiles.clear()
+        return prof
+
+    # the other correlation path, device-resident scenes, same protocol
+    other = None
+    if not args.no_compare:
+        path[0] = "plain" if args.path == "tensor" else "tensor"
+        for _ in range(args.warmup):
+            one_step(dev, False)
+        torch.cuda.synchronize()
+        other_ms = timed(dev, False, args.steps, profile=True)
+        oprof = aggregate()
+        other = {"path": path[0], "ms": other_ms,
+                 "stages_ms_per_find": {k: round(v["ms"] / max(1, oprof["finds"]), 4) for k, v in oprof.items()
+                                        if isinstance(v, dict)}}
+        path[0] = args.path
+
     for _ in range(args.warmup):
         one_step(dev, False)
         one_step(pinned, True)
@@ -272,15 +305,7 @@ def main():
 
     with ClockSampler(local) as clocks:
         dev_ms = timed(dev, False, args.steps, profile=True)
-    prof = {}
-    for p in profiles:
-        for k, v in p.items():
-            if k == "finds":
-                prof["finds"] = prof.get("finds", 0) + v
-                continue
-            acc = prof.setdefault(k, dict(ms=0.0, launches=0, work=0.0))
-            for f in ("ms", "launches", "work"):
-                acc[f] += v[f]
+    prof = aggregate()
     host_ms = timed(pinned, True, args.steps)
 
     def maxed(x):
@@ -291,6 +316,8 @@ def main():
         return float(t.item())
 
     dev_ms, host_ms = maxed(dev_ms), maxed(host_ms)
+    if other is not None:
+        other["value"] = args.steps * args.batch * world / (maxed(other.pop("ms")) / 1e3)
     images = args.steps * args.batch * world
     value = images / (dev_ms / 1e3)
     e2e = images / (host_ms / 1e3)
@@ -299,28 +326,28 @@ def main():
             torch.distributed.destroy_process_group()
         return
 
-    stages = {k: v for k, v in prof.items() if k != "finds"}
-    dominant = max(stages, key=lambda k: stages[k]["ms"])
-    d = stages[dominant]
+    stages = {k: v for k, v in prof.items() if isinstance(v, dict)}
     pk = peaks()
     launches_total = sum(v["launches"] for v in stages.values())
-    kernel_names = {"track": "track_kernel", "coarse": "coarse_kernel", "score": "score_kernel",
-                    "refine": "refine_kernel", "sort": "sort_kernel", "select": "select_kernel"}
-    if dominant in ("track", "coarse") and d["launches"]:
-        flops = 2.0 * d["work"] / d["launches"]
-        per_launch_s = d["ms"] / 1e3 / d["launches"]
-        achieved = flops / per_launch_s / 1e12
-        roof = {"bound": "tensor", "achieved": achieved, "peak": pk["tflops_sustained"], "unit": "TFLOP/s",
-                "frac": achieved / pk["tflops_sustained"],
-                "traffic": traffic_from_profiles(kernel_names.get(dominant, dominant)),
-                "kernel": kernel_names.get(dominant, dominant),
-                "note": f"algorithmic correlation FLOPs (2 x MACs) per launch over the launch's event time; peak = "
-                        f"{pk['source']} dense bf16 sustained (no INT8 peak is measured on this pool); the kernel "
-                        f"runs on FP32 CUDA cores"}
-    else:
-        roof = {"bound": "hbm", "achieved": None, "peak": pk["hbm"], "unit": "GB/s", "frac": None,
-                "traffic": traffic_from_profiles(kernel_names.get(dominant, dominant)),
-                "kernel": kernel_names.get(dominant, dominant)}
+    kernel_names = {"track": "track_kernel", "track_tc": "tc_track_kernel", "coarse": "coarse_kernel",
+                    "score": "score_kernel", "refine": "refine_kernel", "sort": "sort_kernel",
+                    "select": "select_kernel"}
+    # roofline of the correlation kernel of the chosen path: tensor-core
+    # tracking (its event time also covers three small grouping launches) or
+    # the CUDA-core tracking kernel
+    rstage = "track_tc" if args.path == "tensor" and stages.get("track_tc", {}).get("ms") else "track"
+    d = stages[rstage]
+    achieved = 2.0 * d["work"] / (d["ms"] / 1e3) / 1e12 if d["ms"] else None
+    roof = {"bound": "tensor", "achieved": achieved, "peak": pk["tflops_sustained"], "unit": "TFLOP/s",
+            "frac": achieved / pk["tflops_sustained"] if achieved else None,
+            "traffic": traffic_from_profiles(kernel_names[rstage]),
+            "kernel": kernel_names[rstage],
+            "stage_share": d["ms"] / sum(v["ms"] for v in stages.values()),
+            "note": f"algorithmic correlation FLOPs (2 x MACs) over the stage's event time; peak = {pk['source']} "
+                    f"dense bf16 sustained; " + (
+                        f"fp16 operands (exact integer halves), FP32 accumulation in tensor memory; issued/"
+                        f"algorithmic MACs = {prof['tensor_issued_macs'] / max(1.0, d['work']):.2f}"
+                        if rstage == "track_tc" else "FP32 CUDA cores")}
     matches = [len(r[0]) for r in found]
     line = {
         "metric": METRIC, "value": value, "unit": "images/s", "n_gpus": world, "steps": args.steps,
@@ -330,7 +357,8 @@ def main():
                    "angle_range_deg": [-30, 30], "num_levels": 4, "min_score": 0.7, "num_matches": 5,
                    "max_overlap": 0.5, "scenes_per_step": args.batch, "l2": "flushed (256 MiB write) between steps",
                    "finds_in_flight": threads, "parallelism": f"replicas x{world}",
-                   "path": "plain FP32 CUDA-core correlation"},
+                   "path": ("tensor-core (tcgen05) tracking correlation" if args.path == "tensor"
+                            else "plain FP32 CUDA-core correlation")},
         "e2e": {"value": e2e, "unit": "images/s",
                 "h2d_bytes_per_step": int(sum(w.image.nbytes for w in wls)),
                 "d2h_bytes_per_step": int(args.batch * (4 * 8 * FIND["num_matches"] + 128))},
@@ -340,6 +368,8 @@ def main():
         "stages_ms_per_find": {k: round(v["ms"] / max(1, prof["finds"]), 4) for k, v in stages.items()},
         "matches_per_scene": matches,
     }
+    if other is not None:
+        line["compare"] = other
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(wls, os.cpu_count() or 1)
     print(json.dumps(line), flush=True)

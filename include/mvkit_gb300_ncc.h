@@ -124,16 +124,28 @@ MVG_API int32_t mvg_ncc_pyramid_level_noalloc(const void* pixels, int32_t pixel_
 /* Thread-local message of the last failed call (empty after success). */
 MVG_API const char* mvg_last_error(void);
 
+/* Correlation path of the calling thread's finds: 0 (default) scores the
+ * rotated patches of the coarse-to-fine tracking on the tensor cores
+ * (tcgen05, fp16 halves of exact integer sums, FP32 accumulation) wherever a
+ * level's sums allow it; 1 scores everything on the FP32 CUDA cores.  Both
+ * return the same matches within the parity tolerances. */
+MVG_API int32_t mvg_set_correlation_path(int32_t path);
+
 /* Per-thread stage profile of finds on this thread: CUDA events recorded on
- * the find's stream around each kernel group while enabled.  Stages 0..10:
+ * the find's stream around each kernel group while enabled.  Stages 0..11:
  * upload, pyramid, prefix, coarse, nms, track, dedup, score, sort, select,
- * refine.  ms: summed event time; launches: kernels launched (counted also
+ * refine, track_tc.  ms: summed event time; launches: kernels launched (counted also
  * while disabled); work: algorithmic multiply-adds (coarse, track) or
  * bilinear taps (score); finds: completed finds since the last reset. */
 MVG_API int32_t mvg_profile_enable(int32_t on);
 MVG_API int32_t mvg_profile_reset(void);
 MVG_API int32_t mvg_profile_read(int32_t stage, const char** name, double* ms, int64_t* launches, double* work,
                                  int64_t* finds);
+
+/* Multiply-adds the tensor cores were issued by the profiled finds of this
+ * thread (M x N x K of every MMA, padding rows and columns included); the
+ * track_tc stage's work is the algorithmic part of it. */
+MVG_API int32_t mvg_profile_tensor_issued(double* macs);
 
 /* Page-locked host buffers for zero-staging uploads, and device buffers for
  * callers without their own allocator. */

@@ -1,8 +1,8 @@
 """GB300-native NCC template matching (mvkit FindNccModel / CreateNccModel)."""
 from .ncc import (MvError, NccModel, DeviceImage, PinnedBuffer, create_ncc_model, find_ncc_model,
                   find_ncc_model_stage, get_ncc_model_params, load, profile_enable, profile_read, profile_reset,
-                  pyramid_level)
+                  pyramid_level, set_correlation_path)
 
 __all__ = ["MvError", "NccModel", "DeviceImage", "PinnedBuffer", "create_ncc_model", "find_ncc_model",
            "find_ncc_model_stage", "get_ncc_model_params", "load", "profile_enable", "profile_read",
-           "profile_reset", "pyramid_level"]
+           "profile_reset", "pyramid_level", "set_correlation_path"]

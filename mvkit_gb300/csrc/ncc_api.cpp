@@ -4,12 +4,14 @@
 //   prepare  src/ncc_matching/matcher.cpp:343-851
 //   find     src/ncc_matching/matcher.cpp:1063-1076
 //   C API    src/c_api/ncc_matching_api.cpp:29-203
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <new>
@@ -57,6 +59,20 @@ template <class T> struct DevBuf {
 };
 
 // ------------------------------------------------------------------ model
+// Tensor-core groups of one tracking step (cached per target level and query
+// plan): group table, source patch -> group, weight matrices, launch shape.
+struct TcPlan {
+  int parts = 1;          // fp16 planes per level value
+  float offset = 0;       // level value subtracted in the planes
+  int stages = 2;         // weight-chunk buffers
+  int sets = 1, npad = 32;  // accumulator sets, tensor-memory columns per set
+  int rows_slab = 16;     // staged window rows (one TMA box)
+  size_t smem = 0;        // dynamic shared memory of the launch
+  std::vector<TcGroup> groups;
+  std::vector<int32_t> group_of_src;
+  std::vector<std::unique_ptr<DevBuf<uint8_t>>> weights;
+};
+
 struct DevLevel {
   int32_t lin_pitch = 0, lin_rows = 0;  // staged tracking window geometry
   std::vector<PatchDesc> desc;      // host copy (model patches + query endpoints)
@@ -109,6 +125,8 @@ struct DevLevel {
     desc.push_back(d);
     angles.push_back(r.angle);
   }
+  // tensor-core plans of tracking steps into this level, by query plan
+  std::map<std::vector<int32_t>, std::shared_ptr<const TcPlan>> tc_plans;
   // Replaced device tables stay allocated until the model is cleared: finds
   // on other threads may still be reading them.
   std::vector<void*> retired;
@@ -212,6 +230,61 @@ const OrigDev& coarse_original(mvg_ncc_model_s& m, size_t level) {
   return *m.coarse_original[level];
 }
 
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// 3-D TMA descriptor of the fp16 planes (x, row, plane): boxes of 8 columns x
+// `rows` rows of one plane, zero fill outside.
+void encode_planes_map(CUtensorMap* map, const uint16_t* planes, int pitch, int height, int parts, int rows) {
+  static const EncodeTiledFn fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<EncodeTiledFn>(f);
+  }();
+  if (!fn) raise(kInternal, "cuTensorMapEncodeTiled is not available from the driver");
+  const cuuint64_t dims[3] = {cuuint64_t(pitch), cuuint64_t(height), cuuint64_t(kTcPlaneShifts * parts)};
+  const cuuint64_t strides[2] = {cuuint64_t(pitch) * 2, cuuint64_t(pitch) * 2 * cuuint64_t(height)};
+  const cuuint32_t box[3] = {8, cuuint32_t(rows), 1};
+  const cuuint32_t elem[3] = {1, 1, 1};
+  const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, const_cast<uint16_t*>(planes), dims, strides, box,
+                        elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) raise(kInternal, "cuTensorMapEncodeTiled failed (" + std::to_string(int(r)) + ")");
+}
+
+// Correlation path of this thread's finds: tensor cores where applicable
+// (0) or FP32 CUDA cores only (1).
+thread_local int t_path = 0;
+
+uint16_t half_bits(double x) {
+  const _Float16 h = static_cast<_Float16>(x);
+  uint16_t b;
+  std::memcpy(&b, &h, sizeof(b));
+  return b;
+}
+double half_value(uint16_t b) {
+  _Float16 h;
+  std::memcpy(&h, &b, sizeof(b));
+  return double(h);
+}
+
+// fp16 planes of level t: the level minus `offset` is an exact fp16 integer
+// (parts 1), or 64 x an exact high part plus a low part in [0, 64) (parts
+// 2); 0 when neither holds (the CUDA-core path scores that level).
+int tc_parts(int type, size_t t, float* offset) {
+  const double maxv = (type == 1 ? 65535.0 : 255.0) * std::ldexp(1., int(2 * t));
+  const double off = std::floor((maxv + 1) * .5);
+  *offset = float(off);
+  const double range = std::max(off, maxv - off);
+  if (range <= 2048.0) return 1;
+  if (range <= 2048.0 * 64.0) return 2;
+  return 0;
+}
+
 // ------------------------------------------------------------- query plan
 struct FindParams {
   double angle_start = 0, angle_extent = 0, min_score = .8, max_overlap = .5;
@@ -275,6 +348,193 @@ bool lattice_exact32(double v) {
   return std::abs(v) <= 2048 && s == std::floor(s);
 }
 
+// Builds the tensor-core groups of the tracking step into level T (query
+// plan `lp`, `nsrc` patches on the source level).  A group is the rotated
+// patches (origin on the lattice) of one source patch's selected list; the
+// sources with identical lists share it.  Weights: for grid row y, an N x K
+// fp16 matrix in the canonical K-major no-swizzle layout (8 x 8 core
+// matrices of 128 bytes, K-adjacent cores 128 bytes apart, N-adjacent cores
+// K/8 x 128 bytes apart); column (p, dc, half) holds the high or low fp16
+// half of sigma w_p(y, x - dc), row x + part kw the same for each plane part
+// (x 64 for the high part of a split level).  The last 16 rows hold the
+// column's row sum for grid row y as two fp16 terms (x 64 for the high part),
+// which the centring columns of the window multiply.
+std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, const LevelPlan& lp, int parts,
+                                            float offset, size_t budget) {
+  auto plan = std::make_shared<TcPlan>();
+  plan->parts = parts;
+  plan->offset = offset;
+  plan->group_of_src.assign(nsrc, -1);
+  struct Proto {
+    std::vector<int32_t> ks, descs;
+    int rmin = INT32_MAX, rmax = INT32_MIN, cmin = INT32_MAX, cmax = INT32_MIN;
+    int kr = 0, kw = 0, n = 0;
+  };
+  std::vector<Proto> protos;
+  std::map<std::vector<int32_t>, int> by_key;
+  for (size_t src = 0; src < nsrc && protos.size() < size_t(kTcMaxGroups); ++src) {
+    const int b = lp.sel_off[src], e = lp.sel_off[src + 1];
+    if (e == b || e - b > kTcMaxP) continue;
+    Proto pr;
+    for (int k = 0; k < e - b; ++k) {
+      const int32_t di = lp.plist[size_t(lp.sel_idx[size_t(b + k)])];
+      const PatchDesc& d = T.desc[size_t(di)];
+      if (d.orow != 0 || d.ocol != 0) continue;
+      pr.ks.push_back(k);
+      pr.descs.push_back(di);
+      pr.rmin = std::min(pr.rmin, d.rmin);
+      pr.rmax = std::max(pr.rmax, d.rmax);
+      pr.cmin = std::min(pr.cmin, d.cmin);
+      pr.cmax = std::max(pr.cmax, d.cmax);
+    }
+    if (pr.descs.empty()) continue;
+    std::vector<int32_t> key(pr.descs);
+    key.insert(key.end(), pr.ks.begin(), pr.ks.end());
+    const auto it = by_key.find(key);
+    if (it != by_key.end()) {
+      plan->group_of_src[src] = it->second;
+      continue;
+    }
+    pr.kr = pr.rmax - pr.rmin + 1;
+    pr.kw = (pr.cmax - pr.cmin + 1 + 4 + 15) / 16 * 16;
+    pr.n = (10 * int(pr.descs.size()) + 15) / 16 * 16;
+    by_key[key] = int(protos.size());
+    plan->group_of_src[src] = int(protos.size());
+    protos.push_back(std::move(pr));
+  }
+  if (protos.empty()) return plan;
+  // one launch shape for the step: weight buffers from the largest chunk, the
+  // window slab as tall as every group allows
+  size_t max_chunk = 0;
+  int max_kr = 0;
+  int max_n = 0;
+  for (const Proto& pr : protos) {
+    max_chunk = std::max(max_chunk, size_t(pr.n) * size_t(parts * pr.kw + 16) * 2);
+    max_kr = std::max(max_kr, pr.kr);
+    max_n = std::max(max_n, pr.n);
+  }
+  plan->npad = (max_n + 31) / 32 * 32;
+  plan->sets = std::max(1, std::min(4, 512 / plan->npad));
+  const int stages = int(std::min<size_t>(kTcMaxStages, std::max<size_t>(2, (48 * 1024) / max_chunk)));
+  int rows = std::min(256, (max_kr + 7 + 7) / 8 * 8);
+  for (const Proto& pr : protos) {
+    const size_t chunk = size_t(pr.n) * size_t(parts * pr.kw + 16) * 2;
+    const size_t need = size_t(stages) * chunk + 1024;
+    const size_t per_row = size_t(kTcCands) * size_t(parts * pr.kw / 8 + 2) * 16;
+    const int fit = need < budget ? int((budget - need) / per_row) / 8 * 8 : 0;
+    rows = std::min(rows, fit);
+  }
+  if (rows < 16) {
+    plan->group_of_src.assign(nsrc, -1);
+    return plan;
+  }
+  plan->stages = stages;
+  plan->rows_slab = rows;
+  for (const Proto& pr : protos) {
+    const int P = int(pr.descs.size()), K = parts * pr.kw + 16, N = pr.n;
+    const size_t chunk_elems = size_t(N) * size_t(K);
+    double maxw = 0, maxrow = 0;
+    for (int32_t di : pr.descs) {
+      const PatchDesc& d = T.desc[size_t(di)];
+      std::vector<double> row(size_t(pr.kr), 0.0);
+      for (int i = 0; i < d.n; ++i) {
+        const double w = double(T.w[size_t(d.sample_off + i)]);
+        maxw = std::max(maxw, std::abs(w));
+        row[size_t((T.offs[size_t(d.sample_off + i)] >> 16) - pr.rmin)] += std::abs(w);
+      }
+      for (double r : row) maxrow = std::max(maxrow, r);
+    }
+    // weight scale: a power of two keeping the weights (x 64 for a split
+    // level) and the centring row sums (x 64 likewise) within fp16 range
+    const double m64 = parts == 2 ? 64.0 : 1.0;
+    const double limit = std::min(maxw > 0 ? 16384.0 / (maxw * m64) : 1e30, maxrow > 0 ? 16384.0 / (maxrow * m64) : 1e30);
+    const double sigma = limit < 1e30 ? std::ldexp(1., int(std::floor(std::log2(limit)))) : 1.0;
+    std::vector<uint16_t> host(size_t(pr.kr) * chunk_elems, 0);
+    TcGroup g{};
+    g.kr = pr.kr;
+    g.kw = pr.kw;
+    g.parts = parts;
+    g.rmin = pr.rmin;
+    g.cmin = pr.cmin;
+    g.p = P;
+    g.n = N;
+    g.rows_slab = rows;
+    g.inv_scale = float(1.0 / sigma);
+    g.macs = 0;
+    auto at = [&](size_t y, int n, int k) {
+      return y * chunk_elems + size_t(n / 8) * size_t(K / 8) * 64 + size_t(k / 8) * 64 + size_t(n % 8) * 8 +
+             size_t(k % 8);
+    };
+    for (int q = 0; q < P; ++q) {
+      const PatchDesc& d = T.desc[size_t(pr.descs[size_t(q)])];
+      double sum = 0;
+      std::vector<double> rs(size_t(pr.kr) * 2, 0.0);  // row sums of the two halves
+      for (int i = 0; i < d.n; ++i) {
+        const int32_t o = T.offs[size_t(d.sample_off + i)];
+        const int row = o >> 16, col = int(int16_t(o & 0xffff));
+        const double ws = double(T.w[size_t(d.sample_off + i)]) * sigma;
+        const uint16_t hi = half_bits(ws);
+        const double hv = half_value(hi);
+        const uint16_t lo = half_bits(ws - hv);
+        const double lv = half_value(lo);
+        sum += hv + lv;
+        const size_t y = size_t(row - pr.rmin);
+        rs[y * 2] += hv;
+        rs[y * 2 + 1] += lv;
+        for (int dc = 0; dc < 5; ++dc) {
+          const int x = col - pr.cmin + dc;
+          for (int part = 0; part < parts; ++part) {
+            const double mult = (parts == 2 && part == 0) ? 64.0 : 1.0;
+            const int k = part * pr.kw + x;
+            for (int half = 0; half < 2; ++half)
+              host[at(y, (q * 5 + dc) * 2 + half, k)] = half_bits((half ? lv : hv) * mult);
+          }
+        }
+      }
+      // centring rows: the row sum of each column as two fp16 terms
+      double ecorr = 0;
+      const int kc0 = parts * pr.kw;
+      for (size_t y = 0; y < size_t(pr.kr); ++y)
+        for (int half = 0; half < 2; ++half) {
+          const double r = rs[y * 2 + size_t(half)];
+          const uint16_t f1 = half_bits(r);
+          const uint16_t f2 = half_bits(r - half_value(f1));
+          ecorr += half_value(f1) + half_value(f2);
+          for (int dc = 0; dc < 5; ++dc) {
+            const int n = (q * 5 + dc) * 2 + half;
+            if (parts == 2) {
+              host[at(y, n, kc0)] = half_bits(64.0 * half_value(f1));
+              host[at(y, n, kc0 + 1)] = half_bits(64.0 * half_value(f2));
+              host[at(y, n, kc0 + 2)] = f1;
+              host[at(y, n, kc0 + 3)] = f2;
+            } else {
+              host[at(y, n, kc0)] = f1;
+              host[at(y, n, kc0 + 1)] = f2;
+            }
+          }
+        }
+      g.ecorr[q] = float(ecorr / sigma);
+      g.k_of[q] = pr.ks[size_t(q)];
+      const int32_t o0 = T.offs[size_t(d.sample_off)];
+      g.r0[q] = o0 >> 16;
+      g.c0[q] = int(int16_t(o0 & 0xffff));
+      g.weff[q] = float(sum / sigma);
+      g.macs += 25ll * d.n;
+    }
+    auto buf = std::make_unique<DevBuf<uint8_t>>();
+    buf->reserve(host.size() * 2);
+    check(cudaMemcpy(buf->p, host.data(), host.size() * 2, cudaMemcpyHostToDevice), "tc weights");
+    g.b = buf->p;
+    plan->weights.push_back(std::move(buf));
+    const size_t abytes = size_t(kTcCands) * size_t(parts * pr.kw / 8 + 2) * size_t(rows) * 16;
+    const size_t bbytes = size_t(stages) * chunk_elems * 2;
+    const size_t dbytes = size_t(128) * size_t(N + 1) * 4;
+    plan->smem = std::max(plan->smem, std::max(abytes + bbytes, dbytes) + 1024);
+    plan->groups.push_back(g);
+  }
+  return plan;
+}
+
 // ------------------------------------------------------------- workspace
 struct Workspace {
   int device = -1;
@@ -291,12 +551,17 @@ struct Workspace {
   DevBuf<Refined> refined;
   DevBuf<int32_t> refined_flag, batch;
   DevBuf<QueryState> state;
+  DevBuf<float> tc_dots;
+  DevBuf<uint16_t> tc_planes;
+  DevBuf<int32_t> tc_order, tc_counts, tc_offsets, tc_cursor;
+  DevBuf<TcTiles> tc_tiles;
   DevBuf<uint8_t> tables;            // query patch lists and ranges, one upload
   uint8_t* h_tables = nullptr;       // pinned staging of the same
   size_t h_tables_size = 0;
   QueryState* h_state = nullptr;
   int32_t* h_error = nullptr;
   size_t smem_optin = 0;
+  int sm_count = 0;
   ~Workspace() {
     if (h_tables) cudaFreeHost(h_tables);
     if (h_state) cudaFreeHost(h_state);
@@ -312,6 +577,7 @@ struct Workspace {
     int optin = 0;
     check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "attribute");
     smem_optin = size_t(optin);
+    check(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev), "attribute");
     cand_a.reserve(kMaxCandidates);
     cand_b.reserve(kMaxCandidates);
     tmp.reserve(kMaxCandidates);
@@ -352,9 +618,9 @@ Workspace& workspace() {
 // Per-thread stage profile: CUDA events on the find's stream around each
 // kernel group (only while enabled), launch counts and algorithmic work.
 enum Stage { kStUpload, kStPyramid, kStPrefix, kStCoarse, kStNms, kStTrack, kStDedup, kStScore, kStSort, kStSelect,
-             kStRefine, kStages };
+             kStRefine, kStTrackTc, kStages };
 const char* const kStageNames[kStages] = {"upload", "pyramid", "prefix", "coarse", "nms", "track",
-                                          "dedup", "score", "sort", "select", "refine"};
+                                          "dedup", "score", "sort", "select", "refine", "track_tc"};
 struct Profiler {
   bool on = false;
   struct Mark {
@@ -367,6 +633,7 @@ struct Profiler {
   double ms[kStages] = {};
   int64_t launches[kStages] = {};
   double work[kStages] = {};
+  double issued_tc = 0;  // MACs issued to the tensor cores, padding included
   int64_t finds = 0;
   ~Profiler() {
     for (cudaEvent_t e : pool) cudaEventDestroy(e);
@@ -402,6 +669,7 @@ struct Profiler {
     marks.clear();
     used = 0;
     for (int i = 0; i < kStages; ++i) ms[i] = 0, launches[i] = 0, work[i] = 0;
+    issued_tc = 0;
     finds = 0;
   }
 };
@@ -577,6 +845,28 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
       const PatchDesc& d = m.levels[li]->desc[size_t(p)];
       if (!lattice_exact32(d.orow) || !lattice_exact32(d.ocol)) exact32 = false;
     }
+  // tensor-core plans of the tracking steps (cached per target level)
+  std::vector<std::shared_ptr<const TcPlan>> tc(level_count);
+  if (t_path == 0) {
+    const size_t budget = ws.smem_optin - tc_kernel_static_smem() - 1024;
+    for (size_t t = std::max(finest, size_t(opt.subpixel ? 1 : 0)); t + 1 < level_count; ++t) {
+      float offset = 0;
+      const int parts = tc_parts(type, t, &offset);
+      if (!parts) continue;
+      DevLevel& T = *m.levels[t];
+      const size_t nsrc = m.levels[t + 1]->desc.size();
+      std::vector<int32_t> key{int32_t(parts), int32_t(nsrc)};
+      key.insert(key.end(), plan[t].plist.begin(), plan[t].plist.end());
+      key.insert(key.end(), plan[t].sel_off.begin(), plan[t].sel_off.end());
+      key.insert(key.end(), plan[t].sel_idx.begin(), plan[t].sel_idx.end());
+      auto it = T.tc_plans.find(key);
+      if (it == T.tc_plans.end()) {
+        if (T.tc_plans.size() >= 32) T.tc_plans.clear();  // finds in flight keep their plans alive
+        it = T.tc_plans.emplace(std::move(key), build_tc_plan(T, nsrc, plan[t], parts, offset, budget)).first;
+      }
+      if (!it->second->groups.empty()) tc[t] = it->second;
+    }
+  }
   const size_t finest_level = finest;
   const OriginalView orig = finest_level ? coarse_original(m, finest_level).view() : m.original.view();
   for (size_t li = 0; li < level_count; ++li) views[li] = m.levels[li]->view();
@@ -597,6 +887,8 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   const PosRange* d_ranges[kMaxLevels];
   const int32_t* d_sel_off[kMaxLevels];
   const int32_t* d_sel_idx[kMaxLevels];
+  const TcGroup* d_tc_groups[kMaxLevels];
+  const int32_t* d_tc_gsrc[kMaxLevels];
   {
     size_t total = 0;
     std::vector<size_t> at(4 * level_count);
@@ -610,6 +902,13 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
       reserve(4 * li + 2, plan[li].sel_off.size() * sizeof(int32_t));
       reserve(4 * li + 3, plan[li].sel_idx.size() * sizeof(int32_t));
     }
+    std::vector<size_t> tc_at(2 * level_count);
+    for (size_t li = 0; li < level_count; ++li) {
+      tc_at[2 * li] = total;
+      total += tc[li] ? (tc[li]->groups.size() * sizeof(TcGroup) + 15) & ~size_t(15) : 0;
+      tc_at[2 * li + 1] = total;
+      total += tc[li] ? (tc[li]->group_of_src.size() * sizeof(int32_t) + 15) & ~size_t(15) : 0;
+    }
     uint8_t* h = ws.stage_tables(std::max<size_t>(total, 16));
     for (size_t li = 0; li < level_count; ++li) {
       std::memcpy(h + at[4 * li], plan[li].plist.data(), plan[li].plist.size() * sizeof(int32_t));
@@ -620,6 +919,13 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
       d_ranges[li] = reinterpret_cast<const PosRange*>(ws.tables.p + at[4 * li + 1]);
       d_sel_off[li] = reinterpret_cast<const int32_t*>(ws.tables.p + at[4 * li + 2]);
       d_sel_idx[li] = reinterpret_cast<const int32_t*>(ws.tables.p + at[4 * li + 3]);
+      if (tc[li]) {
+        std::memcpy(h + tc_at[2 * li], tc[li]->groups.data(), tc[li]->groups.size() * sizeof(TcGroup));
+        std::memcpy(h + tc_at[2 * li + 1], tc[li]->group_of_src.data(),
+                    tc[li]->group_of_src.size() * sizeof(int32_t));
+      }
+      d_tc_groups[li] = reinterpret_cast<const TcGroup*>(ws.tables.p + tc_at[2 * li]);
+      d_tc_gsrc[li] = reinterpret_cast<const int32_t*>(ws.tables.p + tc_at[2 * li + 1]);
     }
     check(cudaMemcpyAsync(ws.tables.p, h, total, cudaMemcpyHostToDevice, s), "tables");
   }
@@ -736,6 +1042,53 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
       ta.offset = (ta.step - 1) * .5;
       ta.exact32 = exact32;
       ta.absolute = hm.params.ignore_polarity;
+      ta.tc_dots = nullptr;
+      ta.tc_group_of_src = nullptr;
+      if (tc[t]) {
+        const TcPlan& P = *tc[t];
+        const int ng = int(P.groups.size());
+        const int pitch = (lev[t].w + kTcPlaneMargin + 7) & ~7;
+        ws.tc_dots.reserve(size_t(kMaxCandidates) * kTcScoreStride);
+        ws.tc_planes.reserve(size_t(P.parts) * kTcPlaneShifts * size_t(lev[t].h) * size_t(pitch));
+        ws.tc_order.reserve(kMaxCandidates);
+        ws.tc_counts.reserve(size_t(ng));
+        ws.tc_offsets.reserve(size_t(ng));
+        ws.tc_cursor.reserve(size_t(ng));
+        ws.tc_tiles.reserve(1);
+        CUtensorMap map;
+        encode_planes_map(&map, ws.tc_planes.p, pitch, lev[t].h, P.parts, P.rows_slab);
+        TcArgs tca;
+        tca.lev = lev[t];
+        tca.in = cur;
+        tca.state = st;
+        tca.state_rw = st;
+        tca.in_slot = slot;
+        tca.groups = d_tc_groups[t];
+        tca.group_of_src = d_tc_gsrc[t];
+        tca.tiles = ws.tc_tiles.p;
+        tca.order = ws.tc_order.p;
+        tca.dots = ws.tc_dots.p;
+        tca.crop_row = double(crop_row);
+        tca.crop_col = double(crop_col);
+        tca.step = ta.step;
+        tca.offset = ta.offset;
+        tca.exact32 = exact32;
+        tca.stages = P.stages;
+        tca.sets = P.sets;
+        tca.npad = P.npad;
+        tca.plane_offset = P.offset;
+        tca.error = &st->error;
+        Span spt(kStTrackTc, s, 5);
+        check(launch_tc_planes(lev[t], ws.tc_planes.p, pitch, P.parts, P.offset, s), "tc planes");
+        // more than half an SM's shared memory: one block per SM, which owns
+        // all 512 tensor-memory columns
+        const size_t smem = std::max(P.smem, ws.smem_optin / 2 + 1024);
+        check(launch_tc_track(tca, &map, ng, ws.tc_counts.p, ws.tc_offsets.p, ws.tc_cursor.p, kMaxCandidates, smem,
+                              std::min(kTcMaxTiles, ws.sm_count), s),
+              "tc track");
+        ta.tc_dots = ws.tc_dots.p;
+        ta.tc_group_of_src = d_tc_gsrc[t];
+      }
       Span sp(kStTrack, s);
       check(launch_track(ta, kMaxCandidates, s, ws.smem_optin), "track");
     }
@@ -876,6 +1229,8 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   t_prof.collect();
   t_prof.finds += 1;
   t_prof.work[kStTrack] += double(hs.track_macs);
+  t_prof.work[kStTrackTc] += double(hs.tc_macs);
+  t_prof.issued_tc += double(hs.tc_issued);
   t_prof.work[kStScore] += double(hs.count[slot]) * double(orig.n);
   if (hs.overflow) raise(kLimitExceeded, "coarse candidate budget exceeded");
   if (hs.error) raise(hs.error, "pyramid sums exceed the exact float range");
@@ -1085,6 +1440,13 @@ int32_t mvg_ncc_pyramid_level(const void* pixels, int32_t pixel_type, int64_t wi
 
 const char* mvg_last_error(void) { return g_last_error.c_str(); }
 
+int32_t mvg_set_correlation_path(int32_t path) {
+  return guarded([&] {
+    if (path != 0 && path != 1) raise(kInvalidArgument, "path must be 0 (tensor cores) or 1 (CUDA cores)");
+    t_path = path;
+  });
+}
+
 int32_t mvg_profile_enable(int32_t on) {
   return guarded([&] { t_prof.on = on != 0; });
 }
@@ -1102,6 +1464,13 @@ int32_t mvg_profile_read(int32_t stage, const char** name, double* ms, int64_t* 
     if (launches) *launches = t_prof.launches[stage];
     if (work) *work = t_prof.work[stage];
     if (finds) *finds = t_prof.finds;
+  });
+}
+
+int32_t mvg_profile_tensor_issued(double* macs) {
+  return guarded([&] {
+    if (!macs) raise(kInvalidArgument, "macs must not be null");
+    *macs = t_prof.issued_tc;
   });
 }
 

@@ -18,6 +18,9 @@
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "ncc_kernels.h"
 
@@ -268,6 +271,7 @@ __global__ void __launch_bounds__(kTrackThreads) track_kernel(TrackArgs a) {
   if (i >= a.state->count[a.in_slot]) return;
   __shared__ int s_sel[kTrackMaxSel];
   __shared__ int s_row[kTrackMaxSel], s_col[kTrackMaxSel];
+  __shared__ unsigned char s_istc[kTrackMaxSel];
   __shared__ int s_n, s_split, s_wr0, s_wc0, s_wh, s_wcols, s_staged;
   __shared__ float s_centre;
   __shared__ float s_part[kTrackThreads];
@@ -279,6 +283,8 @@ __global__ void __launch_bounds__(kTrackThreads) track_kernel(TrackArgs a) {
     const int src = cd.patch;
     const int b = src >= 0 ? a.sel_off[src] : 0, e = src >= 0 ? a.sel_off[src + 1] : 0;
     const int n = min(e - b, kTrackMaxSel);
+    // rotated patches of a tensor-core group were scored by tc_track_kernel
+    const bool tc = a.tc_dots && src >= 0 && a.tc_group_of_src[src] >= 0;
     int wr0 = INT32_MAX, wc0 = INT32_MAX, wr1 = INT32_MIN, wc1 = INT32_MIN;
     // window centres: round((pose - crop - offset) / step - origin)
     double xr = 0, xc = 0;
@@ -304,11 +310,12 @@ __global__ void __launch_bounds__(kTrackThreads) track_kernel(TrackArgs a) {
       }
       s_row[k] = row;
       s_col[k] = col;
+      s_istc[k] = tc && pd.orow == 0 && pd.ocol == 0 && k < 16;
       const PosRange rg = a.ranges[j];
-      // only placements that can be scored need image data
+      // only placements scored here need image data
       const int r_lo = max(row - 2, rg.r0), r_hi = min(row + 2, rg.r1 - 1);
       const int c_lo = max(col - 2, rg.c0), c_hi = min(col + 2, rg.c1 - 1);
-      if (r_lo <= r_hi && c_lo <= c_hi) {
+      if (!s_istc[k] && r_lo <= r_hi && c_lo <= c_hi) {
         wr0 = min(wr0, r_lo + pd.rmin);
         wr1 = max(wr1, r_hi + pd.rmax);
         wc0 = min(wc0, c_lo + pd.cmin);
@@ -349,7 +356,7 @@ __global__ void __launch_bounds__(kTrackThreads) track_kernel(TrackArgs a) {
     // placements of one sample (broadcast sample loads)
     const int t = pass * kTrackThreads + threadIdx.x;
     const int item = split > 1 ? t % items : t, part = split > 1 ? t / items : 0;
-    bool valid = false;
+    bool valid = false, is_tc = false;
     int r = 0, c = 0;
     PatchDesc pd{};
     float acc = 0.f, x0 = 0.f;
@@ -361,8 +368,11 @@ __global__ void __launch_bounds__(kTrackThreads) track_kernel(TrackArgs a) {
       r = s_row[k] + pos / 5 - 2;
       c = s_col[k] + pos % 5 - 2;
       valid = r >= rg.r0 && r < rg.r1 && c >= rg.c0 && c < rg.c1;
+      is_tc = s_istc[k] != 0;
     }
-    if (valid && staged) {
+    if (is_tc) {
+      // precomputed on the tensor cores
+    } else if (valid && staged) {
       // sum w (S - centre); the first-sample shift is applied once below
       const int2* lw = a.view.lw + pd.sample_off;
       const float* base = win + (r - wr0) * WW + (c - wc0);
@@ -406,10 +416,15 @@ __global__ void __launch_bounds__(kTrackThreads) track_kernel(TrackArgs a) {
       __syncthreads();
     }
     if (part == 0 && valid) {
-      float dot = acc;
-      for (int q = 1; q < split; ++q) dot += s_part[threadIdx.x + q * items];
-      // sum w (S - S0) = sum w (S - centre) - (S0 - centre) sum w
-      if (staged) dot = fmaf(-x0, pd.wsum, dot);
+      float dot;
+      if (is_tc) {
+        dot = a.tc_dots[size_t(i) * kTcScoreStride + item];
+      } else {
+        dot = acc;
+        for (int q = 1; q < split; ++q) dot += s_part[threadIdx.x + q * items];
+        // sum w (S - S0) = sum w (S - centre) - (S0 - centre) sum w
+        if (staged) dot = fmaf(-x0, pd.wsum, dot);
+      }
       long long s1, s2;
       window_moments(a.lev.prefix, pitch + 1, r, c, a.view.runs + pd.run_off, a.view.runs_end + pd.run_off,
                      pd.nruns, s1, s2);
@@ -444,7 +459,8 @@ __global__ void __launch_bounds__(kTrackThreads) track_kernel(TrackArgs a) {
         bs = s_wbest[w];
         bo = s_word[w];
       }
-    for (int k = 0; k < n; ++k) macs += 25ull * (unsigned long long)a.view.patches[a.plist[s_sel[k]]].n;
+    for (int k = 0; k < n; ++k)
+      if (!s_istc[k]) macs += 25ull * (unsigned long long)a.view.patches[a.plist[s_sel[k]]].n;
     atomicAdd(&a.state->track_macs, macs);
     Cand out = cd;
     out.score = -INFINITY;
@@ -1430,6 +1446,19 @@ __global__ void __launch_bounds__(kRefineThreads) refine_kernel(RefineArgs a) {
 }  // namespace
 
 // --------------------------------------------------------------- launchers
+cudaError_t reserve_dynamic_smem(const void* kernel, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> granted;
+  int dev = 0;
+  if (const cudaError_t e = cudaGetDevice(&dev)) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = granted[{kernel, dev}];
+  if (bytes <= cur) return cudaSuccess;
+  const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+  if (e == cudaSuccess) cur = bytes;
+  return e;
+}
+
 cudaError_t launch_pyramid0(const void* src, int type, int64_t pitch_elems, int crop_row, int crop_col, LevelImage dst,
                             int32_t* error_flag, cudaStream_t s) {
   (void)error_flag;
@@ -1457,11 +1486,7 @@ cudaError_t launch_prefix(const LevelImage& lev, cudaStream_t s) {
 cudaError_t launch_coarse(const CoarseArgs& a, int max_bh, int max_bw, cudaStream_t s, size_t smem_limit) {
   const size_t smem = size_t(kTileH + max_bh) * size_t(kTileW + max_bw) * sizeof(float);
   if (smem > smem_limit) return cudaErrorInvalidConfiguration;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(coarse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_limit));
-    attr = true;
-  }
+  if (const cudaError_t e = reserve_dynamic_smem(reinterpret_cast<const void*>(coarse_kernel), smem)) return e;
   const dim3 block(kTileW, kTileH), grid((a.lev.w + kTileW - 1) / kTileW, (a.lev.h + kTileH - 1) / kTileH, a.nplist);
   coarse_kernel<<<grid, block, smem, s>>>(a);
   return cudaGetLastError();
@@ -1483,11 +1508,7 @@ cudaError_t launch_track(const TrackArgs& a, int max_candidates, cudaStream_t s,
   } else {
     b.staged_ok = 1;
   }
-  static size_t attr = 0;
-  if (smem > attr) {
-    cudaFuncSetAttribute(track_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    attr = smem;
-  }
+  if (const cudaError_t e = reserve_dynamic_smem(reinterpret_cast<const void*>(track_kernel), smem)) return e;
   track_kernel<<<max_candidates, kTrackThreads, smem, s>>>(b);
   return cudaGetLastError();
 }
@@ -1506,11 +1527,7 @@ cudaError_t launch_score(const ScoreArgs& a, int max_candidates, cudaStream_t s)
 
 cudaError_t launch_sort(const SortArgs& a, cudaStream_t s) {
   const size_t smem = 16384 * (sizeof(unsigned long long) + sizeof(int));
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    attr = true;
-  }
+  if (const cudaError_t e = reserve_dynamic_smem(reinterpret_cast<const void*>(sort_kernel), smem)) return e;
   sort_kernel<<<1, 1024, smem, s>>>(a);
   return cudaGetLastError();
 }

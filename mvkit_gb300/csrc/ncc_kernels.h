@@ -63,7 +63,78 @@ struct TrackArgs {
   int exact32;              // lattice arithmetic is exact in FP32 (host-checked)
   int absolute;
   int staged_ok;            // set by the launcher: dynamic shared memory holds the window
+  // sum w (S - S0) of the rotated patches of tensor-core groups (nullable),
+  // kTcScoreStride per candidate
+  const float* tc_dots;
+  const int32_t* tc_group_of_src;
 };
+
+// Raises a kernel's dynamic shared-memory limit on the current device to at
+// least `bytes` (never lowers it; safe from several host threads).
+cudaError_t reserve_dynamic_smem(const void* kernel, size_t bytes);
+
+// Tensor-core tracking (ncc_tc.cu).  A tile is up to 16 candidates of one
+// group (candidates found with the same source patch search the same target
+// patches); MMA rows are (candidate, row placement), MMA columns (patch,
+// column placement, weight half); K runs over the window columns of one
+// grid row, and the grid rows accumulate in tensor memory.
+constexpr int kTcMaxP = 16;              // patches of one group (N = 10 P <= 160)
+constexpr int kTcCands = 16;             // candidates per tile (M = 16 x 8 rows)
+constexpr int kTcScoreStride = 16 * 25;  // dots per candidate: [selected patch][placement]
+constexpr int kTcMaxGroups = 4096;       // groups of one tracking step
+constexpr int kTcMaxTiles = kMaxCandidates / kTcCands + kTcMaxGroups + 1;
+constexpr int kTcMaxStages = 8;          // weight-chunk buffers
+constexpr int kTcPlaneShifts = 8;        // column-shifted copies of a level plane
+constexpr int kTcPlaneMargin = 8;        // plane columns left of the level
+
+struct TcGroup {
+  const uint8_t* b;                      // kr chunks: N x (parts kw) fp16 weights, canonical K-major
+  long long macs;                        // algorithmic MACs per candidate (25 x samples of all patches)
+  int kr, kw;                            // grid rows; window columns per part (multiple of 16)
+  int parts;                             // planes per value: 1, or 2 (64 x high part, low part)
+  int rmin, cmin;                        // grid origin relative to the placement centre
+  int p, n;                              // patches; MMA N (10 p rounded up to 16)
+  int rows_slab;                         // window rows per staged slab (multiple of 8, >= 16)
+  float inv_scale;                       // 1 / weight scale
+  int k_of[kTcMaxP];                     // index in the candidate's selected list
+  int r0[kTcMaxP], c0[kTcMaxP];          // first sample offset of each patch
+  float weff[kTcMaxP];                   // sum of the fp16 weights / scale
+  float ecorr[kTcMaxP];                  // sum over grid rows of the centring row sums / scale
+};
+
+struct TcTiles {
+  int count;
+  int group[kTcMaxTiles], first[kTcMaxTiles], last[kTcMaxTiles];
+};
+
+struct TcArgs {
+  LevelImage lev;
+  const Cand* in;
+  const QueryState* state;
+  QueryState* state_rw;                  // MAC counters
+  int in_slot;
+  const TcGroup* groups;
+  const int32_t* group_of_src;           // source patch -> group (-1: CUDA-core path)
+  TcTiles* tiles;
+  int32_t* order;
+  float* dots;                           // kTcScoreStride per candidate: sum w (S - S0)
+  double crop_row, crop_col, step, offset;
+  int exact32;
+  int stages;                            // weight-chunk buffers in use
+  int sets, npad;                        // accumulator sets (grid row y -> set y mod sets), columns per set
+  float plane_offset;                    // level value subtracted in the planes
+  int32_t* error;
+};
+
+// fp16 planes of a level for the tensor-core tracking: parts x 8 shifted
+// copies (plane d holds level column x - kTcPlaneMargin + d at x), `pitch`
+// elements per row (a multiple of 8, at least the level width + 8).
+cudaError_t launch_tc_planes(const LevelImage& lev, uint16_t* planes, int pitch, int parts, float offset,
+                             cudaStream_t s);
+size_t tc_kernel_static_smem();
+// `map` is the 3-D TMA descriptor (x, row, plane) of the planes (128 bytes).
+cudaError_t launch_tc_track(const TcArgs& a, const void* map, int ngroups, int32_t* counts, int32_t* offsets,
+                            int32_t* cursor, int max_candidates, size_t smem, int grid, cudaStream_t s);
 
 struct DedupArgs {
   const Cand* in;

@@ -1,0 +1,484 @@
+// Tensor-core (tcgen05) correlation for the coarse-to-fine tracking step.
+//
+// The candidates of one tracking step are grouped by the patch they were
+// found with: all candidates of a group search the same target patches (the
+// reference's angle window, src/ncc_matching/matcher.cpp:680-697), so the
+// group shares one weight matrix per grid row.  A tile is up to 16
+// candidates of a group and one MMA computes, for one grid row y of the
+// patches' union grid,
+//
+//   D[(candidate g, row placement dr)][(patch p, column placement dc, half)]
+//     += sum_x window_g(y + dr, x) * w_{p,half}(y, x - dc)
+//
+// with M = 16 x 8 rows (dr = 0..4 used), N = 10 P, K = the window columns
+// plus one 16-column step that subtracts the candidate's centre value times
+// the row sum of each weight column (centred accumulation, as the CUDA-core
+// path's window centring).  Grid rows accumulate round-robin into up to four
+// accumulator sets in tensor memory, summed in FP32 by the epilogue.
+// Windows come straight from fp16 copies of the level ("planes", exact
+// integers: the level minus a constant, split into a high and a low plane
+// when a level's values exceed fp16's integer range) by TMA, one 16-byte
+// column strip per transfer, into the canonical no-swizzle K-major layout
+// whose row pitch is 16 bytes, so grid row y is the same tiles started y rows
+// later.  Eight column-shifted copies of each plane keep every TMA start on a
+// 16-byte boundary; planes start 8 columns left of the level so that a
+// transfer outside a plane is outside the level too (zero fill).  Weights
+// (fp16 high and low halves of the scaled weights) stream through a ring of
+// shared-memory buffers with bulk copies;
+// one thread issues the MMAs, accumulation is FP32 in tensor memory.  The
+// epilogue writes sum w (S - S0) per placement; track_kernel adds the exact
+// integer window moments and applies the reference's selection rule.
+#include <cuda.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+
+#include "ncc_kernels.h"
+
+namespace mvg {
+namespace {
+
+constexpr int kTcThreads = 128;
+constexpr int kTcRows = 128;                  // MMA M
+constexpr uint32_t kTmemCols = 512;           // accumulator sets x columns per set
+constexpr long long kSpinLimit = 1ll << 22;   // mbarrier polls before giving up
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
+
+// shared-memory matrix descriptor: canonical layout without swizzle
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = uint64_t((addr & 0x3FFFF) >> 4);
+  d |= uint64_t((lbo >> 4) & 0x3FFF) << 16;
+  d |= uint64_t((sbo >> 4) & 0x3FFF) << 32;
+  d |= uint64_t(1) << 46;
+  return d;
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void bar_init(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)));
+}
+
+__device__ __forceinline__ void expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// bounded wait for the completion of the phase with parity `parity`
+__device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity) {
+  for (long long it = 0; it < kSpinLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+  for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+
+struct __align__(16) TcShared {
+  uint64_t a_full, slab_done;
+  uint64_t b_full[kTcMaxStages], b_empty[kTcMaxStages];
+  TcGroup grp;
+  uint32_t tmem;
+  int fail, gslab, cnt;
+  int ci[kTcCands], R[kTcCands], C[kTcCands], x0a[kTcCands], delta[kTcCands];
+  float centre[kTcCands];  // window centre value minus the plane offset (exact integer)
+};
+
+// Producer and MMA issue of one tile (warp 0; lane 0 issues the weight copies
+// and the MMAs, all lanes the window transfers).  Returns false when a wait
+// ran out; in-flight copies and MMAs are then drained (bounded) first.
+__device__ bool tc_tile_pipeline(const TcArgs& a, const CUtensorMap* map, TcShared& sh, uint8_t* smem, uint32_t tmem,
+                                 long long& cbase, int& gslab, int lane) {
+  const TcGroup& G = sh.grp;
+  const int S = a.stages, cnt = sh.cnt, kr = G.kr;
+  // K: parts x kw plane columns, then 16 centring columns (filled by the block)
+  const int segs = G.kw / 8, nplane = G.parts * segs, nseg = nplane + 2, K = 8 * nseg, ksteps = K / 16;
+  const uint32_t lbo_a = uint32_t(G.rows_slab) * 16, sbo_a = uint32_t(nseg) * lbo_a;
+  const uint32_t bchunk = uint32_t(G.n) * uint32_t(K) * 2;
+  uint8_t* bbase = smem + size_t(kTcCands) * sbo_a;
+  const int Y = G.rows_slab - 7, nslabs = (kr + Y - 1) / Y;
+  const uint32_t idesc = (1u << 4) | (uint32_t(G.n >> 3) << 17) | (uint32_t(kTcRows >> 4) << 24);
+  bool ok = true;
+  int issued = 0, used = 0;  // weight chunks of this tile loaded / consumed (lane 0)
+  bool a_pending = false;
+  auto issue_b = [&](int i) -> bool {
+    const long long c = cbase + i;
+    const int st = int(c % S);
+    if (c >= S && !bar_wait(&sh.b_empty[st], uint32_t(((c / S) - 1) & 1))) return false;
+    expect_tx(&sh.b_full[st], bchunk);
+    bulk_load(bbase + size_t(st) * bchunk, G.b + size_t(i) * bchunk, bchunk, &sh.b_full[st]);
+    issued = i + 1;
+    return true;
+  };
+  if (lane == 0)
+    for (int i = 0; i < min(S, kr) && ok; ++i) ok = issue_b(i);
+  ok = __shfl_sync(0xffffffffu, ok, 0);
+  for (int sl = 0; sl < nslabs && ok; ++sl) {
+    const int y0 = sl * Y, yn = min(Y, kr - y0);
+    if (lane == 0) {
+      // the previous slab's MMAs have read the window buffer
+      if (gslab > 0) ok = bar_wait(&sh.slab_done, uint32_t((gslab - 1) & 1));
+      if (ok) {
+        expect_tx(&sh.a_full, uint32_t(cnt * nplane) * lbo_a);
+        a_pending = true;
+      }
+    }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    if (!ok) break;
+    for (int it = lane; it < cnt * nplane; it += 32) {
+      const int g = it / nplane, sg = it % nplane, q = sg / segs, s = sg % segs;
+      tma_load_3d(smem + size_t(g) * sbo_a + size_t(sg) * lbo_a, map, sh.x0a[g] + kTcPlaneMargin + 8 * s,
+                  sh.R[g] - 2 + G.rmin + y0,
+                  q * kTcPlaneShifts + sh.delta[g], &sh.a_full);
+    }
+    __syncwarp();
+    if (lane == 0) {
+      ok = bar_wait(&sh.a_full, uint32_t(gslab & 1));
+      if (ok) a_pending = false;
+      const uint32_t a0 = smem_u32(smem);
+      for (int y = y0; y < y0 + yn && ok; ++y) {
+        const long long c = cbase + y;
+        const int st = int(c % S);
+        ok = bar_wait(&sh.b_full[st], uint32_t((c / S) & 1));
+        if (!ok) break;
+        used = y + 1;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t arow = a0 + uint32_t(y - y0) * 16;
+        const uint32_t b0 = smem_u32(bbase + size_t(st) * bchunk);
+        const uint32_t d = tmem + uint32_t((y % a.sets) * a.npad);
+        for (int j = 0; j < ksteps; ++j)
+          mma_f16(d, smem_desc(arow + uint32_t(2 * j) * lbo_a, lbo_a, sbo_a),
+                  smem_desc(b0 + uint32_t(j) * 256, 128, uint32_t(K / 8) * 128), idesc,
+                  (y >= a.sets || j > 0) ? 1u : 0u);
+        mma_commit(&sh.b_empty[st]);
+        // refill the buffer of the previous chunk (its MMAs precede these)
+        if (y >= 1 && y - 1 + S < kr) ok = issue_b(y - 1 + S);
+      }
+      mma_commit(&sh.slab_done);
+      ++gslab;
+    }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    gslab = __shfl_sync(0xffffffffu, gslab, 0);
+  }
+  if (lane == 0) {
+    if (!ok) {
+      // drain: copies in flight, then every MMA issued so far
+      for (int i = used; i < issued; ++i) {
+        const long long c = cbase + i;
+        bar_wait(&sh.b_full[int(c % S)], uint32_t((c / S) & 1));
+      }
+      if (a_pending) bar_wait(&sh.a_full, uint32_t(gslab & 1));
+      mma_commit(&sh.slab_done);
+      bar_wait(&sh.slab_done, uint32_t(gslab & 1));
+      ++gslab;
+    }
+    cbase += kr;
+  }
+  gslab = __shfl_sync(0xffffffffu, gslab, 0);
+  return __shfl_sync(0xffffffffu, ok, 0);
+}
+
+// Persistent: block b takes tiles b, b + gridDim.x, ...
+__global__ void __launch_bounds__(kTcThreads, 1)
+    tc_track_kernel(const __grid_constant__ TcArgs a, const __grid_constant__ CUtensorMap map) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ TcShared sh;
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int ntiles = a.tiles->count;
+  if (int(blockIdx.x) >= ntiles) return;
+  uint8_t* smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
+  if (t == 0) {
+    bar_init(&sh.a_full);
+    bar_init(&sh.slab_done);
+    for (int s = 0; s < kTcMaxStages; ++s) {
+      bar_init(&sh.b_full[s]);
+      bar_init(&sh.b_empty[s]);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    sh.fail = 0;
+    sh.gslab = 0;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh.tmem)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = sh.tmem;
+  long long cbase = 0;  // weight chunks loaded by this block so far (warp 0)
+  int gslab = 0;        // window slabs staged by this block so far (warp 0)
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    // tile set-up: the group into shared memory, one candidate per thread
+    {
+      const int gi = a.tiles->group[tile];
+      const uint32_t* src = reinterpret_cast<const uint32_t*>(a.groups + gi);
+      uint32_t* dst = reinterpret_cast<uint32_t*>(&sh.grp);
+      for (int w = t; w < int(sizeof(TcGroup) / 4); w += kTcThreads) dst[w] = src[w];
+      const int first = a.tiles->first[tile];
+      const int cnt = min(kTcCands, a.tiles->last[tile] - first);
+      if (t == 0) sh.cnt = cnt;
+      if (t < cnt) {
+        const int ci = a.order[first + t];
+        const Cand cd = a.in[ci];
+        int R, C;
+        if (a.exact32) {
+          const float s = float(1.0 / a.step);
+          R = int(roundf(__fmul_rn(__fsub_rn(__fsub_rn(float(cd.row), float(a.crop_row)), float(a.offset)), s)));
+          C = int(roundf(__fmul_rn(__fsub_rn(__fsub_rn(float(cd.col), float(a.crop_col)), float(a.offset)), s)));
+        } else {
+          R = int(round(dsub(dsub(cd.row, a.crop_row), a.offset) / a.step));
+          C = int(round(dsub(dsub(cd.col, a.crop_col), a.offset) / a.step));
+        }
+        sh.ci[t] = ci;
+        sh.R[t] = R;
+        sh.C[t] = C;
+        const int cr = min(max(R, 0), a.lev.h - 1), cc = min(max(C, 0), a.lev.w - 1);
+        sh.centre[t] = a.lev.v[size_t(cr) * a.lev.w + cc] - a.plane_offset;
+        const int x0 = C - 2 + a.groups[gi].cmin;
+        sh.x0a[t] = x0 & ~7;  // floor to a multiple of 8 (16-byte TMA start)
+        sh.delta[t] = x0 - (x0 & ~7);
+      }
+    }
+    __syncthreads();
+    {
+      // centring columns of every staged row: (-c, -c) for one plane, (-c_high,
+      // -c_high, -c_low, -c_low) for a split value, c = c_high 64 + c_low
+      const TcGroup& G = sh.grp;
+      const int nplane = G.parts * (G.kw / 8), nseg = nplane + 2, rows = G.rows_slab;
+      for (int it = t; it < kTcCands * rows; it += kTcThreads) {
+        const int g = it / rows, r = it % rows;
+        const float c = g < sh.cnt ? sh.centre[g] : 0.f;
+        const float ch = G.parts == 2 ? floorf(c * (1.f / 64.f)) : c;
+        const float cl = G.parts == 2 ? c - 64.f * ch : 0.f;
+        const __half2 h = __floats2half2_rn(-ch, -ch), l = __floats2half2_rn(-cl, -cl);
+        uint4 v;
+        v.x = *reinterpret_cast<const uint32_t*>(&h);
+        v.y = *reinterpret_cast<const uint32_t*>(&l);
+        v.z = 0;
+        v.w = 0;
+        uint8_t* row = smem + (size_t(g) * nseg + nplane) * size_t(rows) * 16 + size_t(r) * 16;
+        *reinterpret_cast<uint4*>(row) = v;
+        *reinterpret_cast<uint4*>(row + size_t(rows) * 16) = make_uint4(0, 0, 0, 0);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    if (warp == 0) {
+      const bool ok = tc_tile_pipeline(a, &map, sh, smem, tmem, cbase, gslab, lane);
+      if (lane == 0) {
+        sh.gslab = gslab;
+        if (!ok) {
+          sh.fail = 1;
+          atomicExch(a.error, int32_t(kInternal));
+        }
+      }
+    }
+    __syncthreads();
+    if (sh.fail) break;
+    // all MMAs of the tile are complete once the last slab's commit arrived
+    if (!bar_wait(&sh.slab_done, uint32_t((sh.gslab - 1) & 1))) {
+      atomicExch(&sh.fail, 1);
+      atomicExch(a.error, int32_t(kInternal));
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (sh.fail) break;
+    const TcGroup& G = sh.grp;
+    // accumulators -> shared memory (row t; the operand buffers are free now)
+    float* D = reinterpret_cast<float*>(smem);
+    const int ld = G.n + 1;
+    const int nsets = min(a.sets, G.kr);
+    for (int c0 = 0; c0 < G.n; c0 += 32) {
+      float acc[32];
+      tmem_ld32(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0), acc);
+      for (int set = 1; set < nsets; ++set) {
+        float v[32];
+        tmem_ld32(tmem + (uint32_t(warp * 32) << 16) + uint32_t(set * a.npad + c0), v);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) acc[j] += v[j];
+      }
+#pragma unroll
+      for (int j = 0; j < 32; ++j)
+        if (c0 + j < G.n) D[t * ld + c0 + j] = acc[j];
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    const int g = t >> 3, dr = t & 7;
+    if (g < sh.cnt && dr < 5) {
+      const int ci = sh.ci[g], R = sh.R[g], C = sh.C[g];
+      const float cen = sh.centre[g];
+      const int W = a.lev.w, H = a.lev.h;
+      for (int q = 0; q < G.p; ++q) {
+        float* out = a.dots + size_t(ci) * kTcScoreStride + size_t(G.k_of[q]) * 25 + dr * 5;
+        const int sr = min(max(R + dr - 2 + G.r0[q], 0), H - 1);
+        const float* srow = a.lev.v + size_t(sr) * W;
+        for (int dc = 0; dc < 5; ++dc) {
+          const int n0 = (q * 5 + dc) * 2;
+          // sum w (S - c) with c the centre, as accumulated
+          const float raw = (D[t * ld + n0] + D[t * ld + n0 + 1]) * G.inv_scale;
+          const float s0 = srow[min(max(C + dc - 2 + G.c0[q], 0), W - 1)] - a.plane_offset;
+          // sum w (S - S0) = raw + c (ecorr - weff) + (c - S0) weff: ecorr is
+          // the row-sum total as subtracted, weff the weights' sum
+          out[dc] = raw + (cen * (G.ecorr[q] - G.weff[q]) + (cen - s0) * G.weff[q]);
+        }
+      }
+    }
+    if (t == 0) {
+      atomicAdd(&a.state_rw->tc_macs, (unsigned long long)G.macs * (unsigned long long)sh.cnt);
+      atomicAdd(&a.state_rw->tc_issued, (unsigned long long)kTcRows * G.n * (G.parts * G.kw + 16) * G.kr);
+    }
+    // generic accesses of the buffers before the next tile's async writes
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+  }
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+}
+
+// fp16 planes: thread = 8 consecutive columns of one (shift, row); plane d
+// holds level column x - kTcPlaneMargin + d at column x
+__global__ void tc_planes_kernel(LevelImage lev, __half* planes, int pitch, int parts, float offset) {
+  const int groups = pitch / 8;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long total = (long long)kTcPlaneShifts * lev.h * groups;
+  if (idx >= total) return;
+  const int gx = int(idx % groups);
+  const int y = int((idx / groups) % lev.h);
+  const int d = int(idx / ((long long)groups * lev.h));
+  __align__(16) __half hv[8];
+  __align__(16) __half lv[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int x = gx * 8 + e + d - kTcPlaneMargin;
+    const float v = x >= 0 && x < lev.w ? lev.v[size_t(y) * lev.w + x] - offset : 0.f;
+    if (parts == 2) {
+      const float h = floorf(v * (1.f / 64.f));
+      hv[e] = __float2half_rn(h);
+      lv[e] = __float2half_rn(v - 64.f * h);
+    } else {
+      hv[e] = __float2half_rn(v);
+    }
+  }
+  const size_t plane = size_t(lev.h) * pitch;
+  const size_t at = (size_t(d) * lev.h + y) * pitch + size_t(gx) * 8;
+  *reinterpret_cast<uint4*>(planes + at) = *reinterpret_cast<const uint4*>(hv);
+  if (parts == 2)
+    *reinterpret_cast<uint4*>(planes + size_t(kTcPlaneShifts) * plane + at) = *reinterpret_cast<const uint4*>(lv);
+}
+
+// Grouping of the step's candidates: counts per group, tile list, order.
+__global__ void tc_count_kernel(const Cand* in, const QueryState* state, int slot, const int32_t* group_of_src,
+                                int32_t* counts) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= state->count[slot]) return;
+  const int src = in[i].patch;
+  const int gi = src >= 0 ? group_of_src[src] : -1;
+  if (gi >= 0) atomicAdd(counts + gi, 1);
+}
+
+__global__ void tc_plan_kernel(const int32_t* counts, int ngroups, int32_t* offsets, int32_t* cursor, TcTiles* tiles,
+                               int max_tiles) {
+  if (threadIdx.x != 0) return;
+  int at = 0, nt = 0;
+  for (int gi = 0; gi < ngroups; ++gi) {
+    offsets[gi] = at;
+    cursor[gi] = 0;
+    const int c = counts[gi];
+    for (int f = 0; f < c && nt < max_tiles; f += kTcCands) {
+      tiles->group[nt] = gi;
+      tiles->first[nt] = at + f;
+      tiles->last[nt] = at + min(c, f + kTcCands);
+      ++nt;
+    }
+    at += c;
+  }
+  tiles->count = nt;
+}
+
+__global__ void tc_scatter_kernel(const Cand* in, const QueryState* state, int slot, const int32_t* group_of_src,
+                                  const int32_t* offsets, int32_t* cursor, int32_t* order) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= state->count[slot]) return;
+  const int src = in[i].patch;
+  const int gi = src >= 0 ? group_of_src[src] : -1;
+  if (gi < 0) return;
+  order[offsets[gi] + atomicAdd(cursor + gi, 1)] = i;
+}
+
+}  // namespace
+
+size_t tc_kernel_static_smem() { return sizeof(TcShared); }
+
+cudaError_t launch_tc_planes(const LevelImage& lev, uint16_t* planes, int pitch, int parts, float offset,
+                             cudaStream_t s) {
+  const long long total = (long long)kTcPlaneShifts * lev.h * (pitch / 8);
+  const unsigned blocks = unsigned((total + 255) / 256);
+  tc_planes_kernel<<<blocks, 256, 0, s>>>(lev, reinterpret_cast<__half*>(planes), pitch, parts, offset);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tc_track(const TcArgs& a, const void* map, int ngroups, int32_t* counts, int32_t* offsets,
+                            int32_t* cursor, int max_candidates, size_t smem, int grid, cudaStream_t s) {
+  if (cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int32_t) * size_t(ngroups), s)) return e;
+  const unsigned blocks = unsigned((max_candidates + 255) / 256);
+  tc_count_kernel<<<blocks, 256, 0, s>>>(a.in, a.state, a.in_slot, a.group_of_src, counts);
+  tc_plan_kernel<<<1, 32, 0, s>>>(counts, ngroups, offsets, cursor, a.tiles, kTcMaxTiles);
+  tc_scatter_kernel<<<blocks, 256, 0, s>>>(a.in, a.state, a.in_slot, a.group_of_src, offsets, cursor, a.order);
+  if (cudaError_t e = reserve_dynamic_smem(reinterpret_cast<const void*>(tc_track_kernel), smem)) return e;
+  CUtensorMap m;
+  std::memcpy(&m, map, sizeof(m));
+  tc_track_kernel<<<grid, kTcThreads, smem, s>>>(a, m);
+  return cudaGetLastError();
+}
+
+}  // namespace mvg

@@ -96,7 +96,9 @@ struct QueryState {
   int32_t done;
   int32_t batch_count;             // entries in the refinement batch
   int32_t pad_;
-  unsigned long long track_macs;   // algorithmic MACs of the tracking steps (25 positions x samples per patch)
+  unsigned long long track_macs;   // algorithmic MACs of the CUDA-core tracking (25 positions x samples per patch)
+  unsigned long long tc_macs;      // algorithmic MACs of the tensor-core tracking
+  unsigned long long tc_issued;    // MACs issued to the tensor cores (M x N x K per MMA)
 };
 
 }  // namespace mvg

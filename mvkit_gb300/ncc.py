@@ -352,7 +352,15 @@ class PinnedBuffer:
             pass
 
 
-PROFILE_STAGES = 11
+PROFILE_STAGES = 12
+
+
+def set_correlation_path(path: str) -> None:
+    """'tensor' (default) or 'plain' for this thread's finds."""
+    lib = load()
+    lib.mvg_set_correlation_path.argtypes = [C.c_int32]
+    lib.mvg_set_correlation_path.restype = C.c_int32
+    _check(lib.mvg_set_correlation_path(0 if path == "tensor" else 1), "set_correlation_path")
 
 
 def profile_enable(on: bool = True) -> None:
@@ -377,4 +385,10 @@ def profile_read() -> dict:
         out[name.value.decode()] = dict(ms=ms.value, launches=launches.value, work=work.value)
         finds = nf.value
     out["finds"] = finds
+    issued = C.c_double()
+    lib = load()
+    lib.mvg_profile_tensor_issued.argtypes = [C.POINTER(C.c_double)]
+    lib.mvg_profile_tensor_issued.restype = C.c_int32
+    _check(lib.mvg_profile_tensor_issued(C.byref(issued)), "profile")
+    out["tensor_issued_macs"] = issued.value
     return out

@@ -116,8 +116,16 @@ def pose_set(a):
     return {(float(r[0]), float(r[1]), float(r[2])) for r in np.asarray(a).reshape(-1, 4)}
 
 
+@pytest.fixture
+def path(mg, request):
+    mg.set_correlation_path(request.param)
+    yield request.param
+    mg.set_correlation_path("tensor")
+
+
+@pytest.mark.parametrize("path", ["tensor", "plain"], indirect=True)
 @pytest.mark.parametrize("name", ["cfg1_s1", "rot3_all", "rot_l4_2", "u16_rot", "polarity"])
-def test_candidate_stages_match_oracle(mg, orc, name):
+def test_candidate_stages_match_oracle(mg, orc, name, path):
     case = CASES[name]
     wl, mask = make_inputs(case)
     c, f = case["create"], case["find"]
@@ -151,6 +159,35 @@ def test_candidate_stages_match_oracle(mg, orc, name):
     assert np.all(np.diff(got[:, 3]) <= 0), "sorted by score"
     for r in common:
         assert abs(r[3] - ws[(r[0], r[1], r[2])]) < 1e-4
+
+
+@pytest.mark.parametrize("path", ["plain"], indirect=True)
+@pytest.mark.parametrize("name", ["cfg1_s1", "rot_l4_2", "u16_rot", "polarity", "mask_disc"])
+def test_find_matches_reference_plain_path(mg, name, path):
+    case = CASES[name]
+    wl, mask = make_inputs(case)
+    got = gpu_find(mg, gpu_model(mg, case, wl, mask), wl.image, case)
+    assert_same_matches(got, GOLDEN[name]["matches"], f"{name} plain")
+
+
+def test_tensor_core_tracking_runs(mg):
+    """The default path scores the tracking windows of a u8 search on the
+    tensor cores (the track_tc stage launches), the plain path never does."""
+    case = LARGE["cfg2_s1"]
+    wl, mask = make_inputs(case)
+    model = gpu_model(mg, case, wl, mask)
+    launches = {}
+    for p in ("tensor", "plain"):
+        mg.set_correlation_path(p)
+        mg.profile_enable(True)
+        mg.profile_reset()
+        got = gpu_find(mg, model, wl.image, case)
+        prof = mg.profile_read()
+        mg.profile_enable(False)
+        launches[p] = prof["track_tc"]["launches"]
+        assert_same_matches(got, GOLDEN["cfg2_s1"]["matches"], f"cfg2_s1 {p}")
+    mg.set_correlation_path("tensor")
+    assert launches["tensor"] > 0 and launches["plain"] == 0, launches
 
 
 def test_device_resident_input_and_repeat_calls(mg):
