@@ -66,6 +66,7 @@ struct TcPlan {
   float offset = 0;       // level value subtracted in the planes
   int stages = 2;         // weight-chunk buffers
   int sets = 1, npad = 32;  // accumulator sets, tensor-memory columns per set
+  int stage_bytes = 0, abuf_bytes = 0;  // weight buffer, window buffer
   int rows_slab = 16;     // staged window rows (one TMA box)
   size_t smem = 0;        // dynamic shared memory of the launch
   std::vector<TcGroup> groups;
@@ -415,21 +416,25 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
   }
   plan->npad = (max_n + 31) / 32 * 32;
   plan->sets = std::max(1, std::min(4, 512 / plan->npad));
-  const int stages = int(std::min<size_t>(kTcMaxStages, std::max<size_t>(2, (48 * 1024) / max_chunk)));
-  int rows = std::min(256, (max_kr + 7 + 7) / 8 * 8);
-  for (const Proto& pr : protos) {
-    const size_t chunk = size_t(pr.n) * size_t(parts * pr.kw + 16) * 2;
-    const size_t need = size_t(stages) * chunk + 1024;
-    const size_t per_row = size_t(kTcCands) * size_t(parts * pr.kw / 8 + 2) * 16;
-    const int fit = need < budget ? int((budget - need) / per_row) / 8 * 8 : 0;
-    rows = std::min(rows, fit);
-  }
-  if (rows < 16) {
+  // shared memory: weight ring | two window buffers (rows_slab rows each).
+  // The ring covers the L2 latency (about ten grid rows of MMAs ahead); the
+  // window buffers take the rest, at least 16 rows each.
+  int max_nseg = 0;
+  for (const Proto& pr : protos) max_nseg = std::max(max_nseg, parts * pr.kw / 8 + 2);
+  const size_t per_row = size_t(kTcCands) * size_t(max_nseg) * 16;
+  const size_t min_windows = 2 * per_row * 16 + 1024;
+  if (min_windows + 2 * max_chunk > budget) {
     plan->group_of_src.assign(nsrc, -1);
     return plan;
   }
+  const int stages = int(std::min<size_t>({size_t(kTcMaxStages), size_t(10), (budget - min_windows) / max_chunk}));
+  const size_t ring = size_t(stages) * max_chunk + 1024;
+  const int rows = std::min(std::min(256, (max_kr + 7 + 7) / 8 * 8), int((budget - ring) / 2 / per_row) / 8 * 8);
   plan->stages = stages;
   plan->rows_slab = rows;
+  plan->stage_bytes = int(max_chunk);
+  plan->abuf_bytes = int(per_row * size_t(rows));
+  plan->smem = ring + 2 * per_row * size_t(rows);
   for (const Proto& pr : protos) {
     const int P = int(pr.descs.size()), K = parts * pr.kw + 16, N = pr.n;
     const size_t chunk_elems = size_t(N) * size_t(K);
@@ -526,10 +531,7 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
     check(cudaMemcpy(buf->p, host.data(), host.size() * 2, cudaMemcpyHostToDevice), "tc weights");
     g.b = buf->p;
     plan->weights.push_back(std::move(buf));
-    const size_t abytes = size_t(kTcCands) * size_t(parts * pr.kw / 8 + 2) * size_t(rows) * 16;
-    const size_t bbytes = size_t(stages) * chunk_elems * 2;
-    const size_t dbytes = size_t(128) * size_t(N + 1) * 4;
-    plan->smem = std::max(plan->smem, std::max(abytes + bbytes, dbytes) + 1024);
+    plan->smem = std::max(plan->smem, size_t(128) * size_t(N + 1) * 4 + 1024);  // accumulator staging
     plan->groups.push_back(g);
   }
   return plan;
@@ -1074,6 +1076,8 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
         tca.offset = ta.offset;
         tca.exact32 = exact32;
         tca.stages = P.stages;
+        tca.stage_bytes = P.stage_bytes;
+        tca.abuf_bytes = P.abuf_bytes;
         tca.sets = P.sets;
         tca.npad = P.npad;
         tca.plane_offset = P.offset;

@@ -83,7 +83,7 @@ constexpr int kTcCands = 16;             // candidates per tile (M = 16 x 8 rows
 constexpr int kTcScoreStride = 16 * 25;  // dots per candidate: [selected patch][placement]
 constexpr int kTcMaxGroups = 4096;       // groups of one tracking step
 constexpr int kTcMaxTiles = kMaxCandidates / kTcCands + kTcMaxGroups + 1;
-constexpr int kTcMaxStages = 8;          // weight-chunk buffers
+constexpr int kTcMaxStages = 16;         // weight-chunk buffers
 constexpr int kTcPlaneShifts = 8;        // column-shifted copies of a level plane
 constexpr int kTcPlaneMargin = 8;        // plane columns left of the level
 
@@ -121,6 +121,7 @@ struct TcArgs {
   double crop_row, crop_col, step, offset;
   int exact32;
   int stages;                            // weight-chunk buffers in use
+  int stage_bytes, abuf_bytes;           // bytes per weight buffer / per window buffer
   int sets, npad;                        // accumulator sets (grid row y -> set y mod sets), columns per set
   float plane_offset;                    // level value subtracted in the planes
   int32_t* error;

@@ -24,8 +24,9 @@
 // 16-byte boundary; planes start 8 columns left of the level so that a
 // transfer outside a plane is outside the level too (zero fill).  Weights
 // (fp16 high and low halves of the scaled weights) stream through a ring of
-// shared-memory buffers with bulk copies;
-// one thread issues the MMAs, accumulation is FP32 in tensor memory.  The
+// shared-memory buffers with bulk copies.  The block is warp-specialised: a
+// window-producer warp (two slab buffers), a weight-producer thread and an
+// MMA-issue thread; accumulation is FP32 in tensor memory.  The
 // epilogue writes sum w (S - S0) per placement; track_kernel adds the exact
 // integer window moments and applies the reference's selection rule.
 #include <cuda.h>
@@ -123,110 +124,130 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 
 struct __align__(16) TcShared {
-  uint64_t a_full, slab_done;
+  uint64_t a_full[2], slab_done[2], drain;
   uint64_t b_full[kTcMaxStages], b_empty[kTcMaxStages];
   TcGroup grp;
   uint32_t tmem;
-  int fail, gslab, cnt;
+  int fail, cnt;
+  long long cm, cb;  // weight chunks consumed (MMA thread) / loaded (weight producer)
+  int sm, sa;        // window slabs consumed (MMA thread) / staged (window producer)
   int ci[kTcCands], R[kTcCands], C[kTcCands], x0a[kTcCands], delta[kTcCands];
   float centre[kTcCands];  // window centre value minus the plane offset (exact integer)
 };
 
-// Producer and MMA issue of one tile (warp 0; lane 0 issues the weight copies
-// and the MMAs, all lanes the window transfers).  Returns false when a wait
-// ran out; in-flight copies and MMAs are then drained (bounded) first.
-__device__ bool tc_tile_pipeline(const TcArgs& a, const CUtensorMap* map, TcShared& sh, uint8_t* smem, uint32_t tmem,
-                                 long long& cbase, int& gslab, int lane) {
-  const TcGroup& G = sh.grp;
-  const int S = a.stages, cnt = sh.cnt, kr = G.kr;
-  // K: parts x kw plane columns, then 16 centring columns (filled by the block)
-  const int segs = G.kw / 8, nplane = G.parts * segs, nseg = nplane + 2, K = 8 * nseg, ksteps = K / 16;
-  const uint32_t lbo_a = uint32_t(G.rows_slab) * 16, sbo_a = uint32_t(nseg) * lbo_a;
-  const uint32_t bchunk = uint32_t(G.n) * uint32_t(K) * 2;
-  uint8_t* bbase = smem + size_t(kTcCands) * sbo_a;
-  const int Y = G.rows_slab - 7, nslabs = (kr + Y - 1) / Y;
-  const uint32_t idesc = (1u << 4) | (uint32_t(G.n >> 3) << 17) | (uint32_t(kTcRows >> 4) << 24);
-  bool ok = true;
-  int issued = 0, used = 0;  // weight chunks of this tile loaded / consumed (lane 0)
-  bool a_pending = false;
-  auto issue_b = [&](int i) -> bool {
-    const long long c = cbase + i;
-    const int st = int(c % S);
-    if (c >= S && !bar_wait(&sh.b_empty[st], uint32_t(((c / S) - 1) & 1))) return false;
-    expect_tx(&sh.b_full[st], bchunk);
-    bulk_load(bbase + size_t(st) * bchunk, G.b + size_t(i) * bchunk, bchunk, &sh.b_full[st]);
-    issued = i + 1;
-    return true;
-  };
-  if (lane == 0)
-    for (int i = 0; i < min(S, kr) && ok; ++i) ok = issue_b(i);
-  ok = __shfl_sync(0xffffffffu, ok, 0);
-  for (int sl = 0; sl < nslabs && ok; ++sl) {
-    const int y0 = sl * Y, yn = min(Y, kr - y0);
-    if (lane == 0) {
-      // the previous slab's MMAs have read the window buffer
-      if (gslab > 0) ok = bar_wait(&sh.slab_done, uint32_t((gslab - 1) & 1));
-      if (ok) {
-        expect_tx(&sh.a_full, uint32_t(cnt * nplane) * lbo_a);
-        a_pending = true;
-      }
-    }
-    ok = __shfl_sync(0xffffffffu, ok, 0);
-    if (!ok) break;
-    for (int it = lane; it < cnt * nplane; it += 32) {
-      const int g = it / nplane, sg = it % nplane, q = sg / segs, s = sg % segs;
-      tma_load_3d(smem + size_t(g) * sbo_a + size_t(sg) * lbo_a, map, sh.x0a[g] + kTcPlaneMargin + 8 * s,
-                  sh.R[g] - 2 + G.rmin + y0,
-                  q * kTcPlaneShifts + sh.delta[g], &sh.a_full);
-    }
-    __syncwarp();
-    if (lane == 0) {
-      ok = bar_wait(&sh.a_full, uint32_t(gslab & 1));
-      if (ok) a_pending = false;
-      const uint32_t a0 = smem_u32(smem);
-      for (int y = y0; y < y0 + yn && ok; ++y) {
-        const long long c = cbase + y;
-        const int st = int(c % S);
-        ok = bar_wait(&sh.b_full[st], uint32_t((c / S) & 1));
-        if (!ok) break;
-        used = y + 1;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t arow = a0 + uint32_t(y - y0) * 16;
-        const uint32_t b0 = smem_u32(bbase + size_t(st) * bchunk);
-        const uint32_t d = tmem + uint32_t((y % a.sets) * a.npad);
-        for (int j = 0; j < ksteps; ++j)
-          mma_f16(d, smem_desc(arow + uint32_t(2 * j) * lbo_a, lbo_a, sbo_a),
-                  smem_desc(b0 + uint32_t(j) * 256, 128, uint32_t(K / 8) * 128), idesc,
-                  (y >= a.sets || j > 0) ? 1u : 0u);
-        mma_commit(&sh.b_empty[st]);
-        // refill the buffer of the previous chunk (its MMAs precede these)
-        if (y >= 1 && y - 1 + S < kr) ok = issue_b(y - 1 + S);
-      }
-      mma_commit(&sh.slab_done);
-      ++gslab;
-    }
-    ok = __shfl_sync(0xffffffffu, ok, 0);
-    gslab = __shfl_sync(0xffffffffu, gslab, 0);
+// Shape of one tile's operands.
+struct TcShape {
+  int segs, nplane, nseg, K, ksteps, Y, nslabs;
+  uint32_t lbo, sbo, bchunk;
+  __device__ explicit TcShape(const TcGroup& G) {
+    segs = G.kw / 8;
+    nplane = G.parts * segs;  // plane segments; two centring segments follow
+    nseg = nplane + 2;
+    K = 8 * nseg;
+    ksteps = K / 16;
+    Y = G.rows_slab - 7;  // grid rows per window slab
+    nslabs = (G.kr + Y - 1) / Y;
+    lbo = uint32_t(G.rows_slab) * 16;
+    sbo = uint32_t(nseg) * lbo;
+    bchunk = uint32_t(G.n) * uint32_t(K) * 2;
   }
-  if (lane == 0) {
-    if (!ok) {
-      // drain: copies in flight, then every MMA issued so far
-      for (int i = used; i < issued; ++i) {
-        const long long c = cbase + i;
-        bar_wait(&sh.b_full[int(c % S)], uint32_t((c / S) & 1));
-      }
-      if (a_pending) bar_wait(&sh.a_full, uint32_t(gslab & 1));
-      mma_commit(&sh.slab_done);
-      bar_wait(&sh.slab_done, uint32_t(gslab & 1));
-      ++gslab;
-    }
-    cbase += kr;
-  }
-  gslab = __shfl_sync(0xffffffffu, gslab, 0);
-  return __shfl_sync(0xffffffffu, ok, 0);
+};
+
+__device__ __forceinline__ void tc_fail(const TcArgs& a, TcShared& sh) {
+  atomicExch(&sh.fail, 1);
+  atomicExch(a.error, int32_t(kInternal));
 }
 
-// Persistent: block b takes tiles b, b + gridDim.x, ...
+// MMA issue (one thread): per slab, wait for the windows, then per grid row
+// wait for its weights, issue K/16 MMAs into accumulator set y mod sets and
+// release the weight buffer; release the window buffer after the slab.
+__device__ void tc_mma_role(const TcArgs& a, TcShared& sh, uint8_t* wbase, uint8_t* abase, uint32_t tmem,
+                            long long& cm, int& sm) {
+  const TcGroup& G = sh.grp;
+  const TcShape sp(G);
+  const int S = a.stages;
+  const uint32_t idesc = (1u << 4) | (uint32_t(G.n >> 3) << 17) | (uint32_t(kTcRows >> 4) << 24);
+  for (int sl = 0; sl < sp.nslabs; ++sl) {
+    const int buf = sm & 1;
+    if (!bar_wait(&sh.a_full[buf], uint32_t((sm >> 1) & 1))) {
+      tc_fail(a, sh);
+      return;
+    }
+    const uint32_t a0 = smem_u32(abase + size_t(buf) * a.abuf_bytes);
+    const int y0 = sl * sp.Y, y1 = min(G.kr, y0 + sp.Y);
+    for (int y = y0; y < y1; ++y) {
+      const int st = int(cm % S);
+      if (!bar_wait(&sh.b_full[st], uint32_t((cm / S) & 1))) {
+        tc_fail(a, sh);
+        return;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t arow = a0 + uint32_t(y - y0) * 16;
+      const uint32_t b0 = smem_u32(wbase + size_t(st) * a.stage_bytes);
+      const uint32_t d = tmem + uint32_t((y % a.sets) * a.npad);
+      for (int j = 0; j < sp.ksteps; ++j)
+        mma_f16(d, smem_desc(arow + uint32_t(2 * j) * sp.lbo, sp.lbo, sp.sbo),
+                smem_desc(b0 + uint32_t(j) * 256, 128, uint32_t(sp.K / 8) * 128), idesc,
+                (y >= a.sets || j > 0) ? 1u : 0u);
+      mma_commit(&sh.b_empty[st]);
+      ++cm;
+    }
+    mma_commit(&sh.slab_done[buf]);
+    ++sm;
+  }
+}
+
+// Window producer (one warp): per slab, once the MMAs of the slab that last
+// used the buffer are done, one TMA box (8 columns x rows_slab rows) per
+// candidate and plane segment.
+__device__ void tc_window_role(const TcArgs& a, const CUtensorMap* map, TcShared& sh, uint8_t* abase, int& sa,
+                               int lane) {
+  const TcGroup& G = sh.grp;
+  const TcShape sp(G);
+  const int cnt = sh.cnt;
+  for (int sl = 0; sl < sp.nslabs; ++sl) {
+    const int buf = sa & 1;
+    int ok = 1;
+    if (lane == 0) {
+      if (sa >= 2) ok = bar_wait(&sh.slab_done[buf], uint32_t(((sa >> 1) - 1) & 1));
+      if (ok) expect_tx(&sh.a_full[buf], uint32_t(cnt * sp.nplane) * sp.lbo);
+      else tc_fail(a, sh);
+    }
+    if (!__shfl_sync(0xffffffffu, ok, 0)) return;
+    uint8_t* dst = abase + size_t(buf) * a.abuf_bytes;
+    const int y0 = sl * sp.Y;
+    for (int it = lane; it < cnt * sp.nplane; it += 32) {
+      const int g = it / sp.nplane, sg = it % sp.nplane, q = sg / sp.segs, s = sg % sp.segs;
+      tma_load_3d(dst + size_t(g) * sp.sbo + size_t(sg) * sp.lbo, map, sh.x0a[g] + kTcPlaneMargin + 8 * s,
+                  sh.R[g] - 2 + G.rmin + y0, q * kTcPlaneShifts + sh.delta[g], &sh.a_full[buf]);
+    }
+    __syncwarp();
+    ++sa;
+  }
+}
+
+// Weight producer (one thread): the tile's grid-row chunks through the ring,
+// as far ahead as the ring allows.
+__device__ void tc_weight_role(const TcArgs& a, TcShared& sh, uint8_t* wbase, long long& cb) {
+  const TcGroup& G = sh.grp;
+  const TcShape sp(G);
+  const int S = a.stages;
+  for (int i = 0; i < G.kr; ++i) {
+    const int st = int(cb % S);
+    if (cb >= S && !bar_wait(&sh.b_empty[st], uint32_t(((cb / S) - 1) & 1))) {
+      tc_fail(a, sh);
+      return;
+    }
+    expect_tx(&sh.b_full[st], sp.bchunk);
+    bulk_load(wbase + size_t(st) * a.stage_bytes, G.b + size_t(i) * sp.bchunk, sp.bchunk, &sh.b_full[st]);
+    ++cb;
+  }
+}
+
+// Persistent and warp-specialised: block b takes tiles b, b + gridDim.x, ...;
+// per tile warp 0 issues the MMAs, warp 1 stages windows, warp 2 streams
+// weights, and all four warps run the set-up and the epilogue.  Shared
+// memory: weight ring (stages x stage_bytes) | two window buffers.
 __global__ void __launch_bounds__(kTcThreads, 1)
     tc_track_kernel(const __grid_constant__ TcArgs a, const __grid_constant__ CUtensorMap map) {
   extern __shared__ uint8_t smem_raw[];
@@ -235,16 +256,22 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const int ntiles = a.tiles->count;
   if (int(blockIdx.x) >= ntiles) return;
   uint8_t* smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
+  uint8_t* wbase = smem;
+  uint8_t* abase = smem + size_t(a.stages) * a.stage_bytes;
   if (t == 0) {
-    bar_init(&sh.a_full);
-    bar_init(&sh.slab_done);
+    bar_init(&sh.a_full[0]);
+    bar_init(&sh.a_full[1]);
+    bar_init(&sh.slab_done[0]);
+    bar_init(&sh.slab_done[1]);
+    bar_init(&sh.drain);
     for (int s = 0; s < kTcMaxStages; ++s) {
       bar_init(&sh.b_full[s]);
       bar_init(&sh.b_empty[s]);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     sh.fail = 0;
-    sh.gslab = 0;
+    sh.cm = sh.cb = 0;
+    sh.sm = sh.sa = 0;
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh.tmem)),
@@ -255,8 +282,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = sh.tmem;
-  long long cbase = 0;  // weight chunks loaded by this block so far (warp 0)
-  int gslab = 0;        // window slabs staged by this block so far (warp 0)
+  long long cm = 0, cb = 0;  // role-local counters (MMA thread, weight producer)
+  int sm = 0, sa = 0;        // role-local counters (MMA thread, window producer)
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     // tile set-up: the group into shared memory, one candidate per thread
     {
@@ -291,12 +318,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     __syncthreads();
     {
-      // centring columns of every staged row: (-c, -c) for one plane, (-c_high,
-      // -c_high, -c_low, -c_low) for a split value, c = c_high 64 + c_low
+      // centring columns of every staged row of both window buffers: (-c, -c)
+      // for one plane, (-c_high, -c_high, -c_low, -c_low) for a split value,
+      // c = 64 c_high + c_low
       const TcGroup& G = sh.grp;
-      const int nplane = G.parts * (G.kw / 8), nseg = nplane + 2, rows = G.rows_slab;
-      for (int it = t; it < kTcCands * rows; it += kTcThreads) {
-        const int g = it / rows, r = it % rows;
+      const TcShape sp(G);
+      const int rows = G.rows_slab;
+      for (int it = t; it < 2 * kTcCands * rows; it += kTcThreads) {
+        const int buf = it / (kTcCands * rows), g = (it / rows) % kTcCands, r = it % rows;
         const float c = g < sh.cnt ? sh.centre[g] : 0.f;
         const float ch = G.parts == 2 ? floorf(c * (1.f / 64.f)) : c;
         const float cl = G.parts == 2 ? c - 64.f * ch : 0.f;
@@ -306,33 +335,51 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         v.y = *reinterpret_cast<const uint32_t*>(&l);
         v.z = 0;
         v.w = 0;
-        uint8_t* row = smem + (size_t(g) * nseg + nplane) * size_t(rows) * 16 + size_t(r) * 16;
+        uint8_t* row = abase + size_t(buf) * a.abuf_bytes + size_t(g) * sp.sbo + size_t(sp.nplane) * sp.lbo +
+                       size_t(r) * 16;
         *reinterpret_cast<uint4*>(row) = v;
-        *reinterpret_cast<uint4*>(row + size_t(rows) * 16) = make_uint4(0, 0, 0, 0);
+        *reinterpret_cast<uint4*>(row + sp.lbo) = make_uint4(0, 0, 0, 0);
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     __syncthreads();
     if (warp == 0) {
-      const bool ok = tc_tile_pipeline(a, &map, sh, smem, tmem, cbase, gslab, lane);
       if (lane == 0) {
-        sh.gslab = gslab;
-        if (!ok) {
-          sh.fail = 1;
-          atomicExch(a.error, int32_t(kInternal));
-        }
+        tc_mma_role(a, sh, wbase, abase, tmem, cm, sm);
+        sh.cm = cm;
+        sh.sm = sm;
       }
+      __syncwarp();
+    } else if (warp == 1) {
+      tc_window_role(a, &map, sh, abase, sa, lane);
+      if (lane == 0) sh.sa = sa;
+    } else if (warp == 2) {
+      if (lane == 0) {
+        tc_weight_role(a, sh, wbase, cb);
+        sh.cb = cb;
+      }
+      __syncwarp();
     }
     __syncthreads();
-    if (sh.fail) break;
-    // all MMAs of the tile are complete once the last slab's commit arrived
-    if (!bar_wait(&sh.slab_done, uint32_t((sh.gslab - 1) & 1))) {
-      atomicExch(&sh.fail, 1);
-      atomicExch(a.error, int32_t(kInternal));
+    if (!sh.fail) {
+      // all MMAs of the tile are complete once the last slab's commit arrived
+      const int last = sh.sm - 1;
+      if (!bar_wait(&sh.slab_done[last & 1], uint32_t((last >> 1) & 1))) tc_fail(a, sh);
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     __syncthreads();
-    if (sh.fail) break;
+    if (sh.fail) {
+      // drain in-flight copies and MMAs (bounded) before leaving
+      if (t == 0) {
+        for (long long c = sh.cm; c < sh.cb; ++c)
+          bar_wait(&sh.b_full[int(c % a.stages)], uint32_t((c / a.stages) & 1));
+        for (int sl = sh.sm; sl < sh.sa; ++sl) bar_wait(&sh.a_full[sl & 1], uint32_t((sl >> 1) & 1));
+        mma_commit(&sh.drain);
+        bar_wait(&sh.drain, 0);
+      }
+      __syncthreads();
+      break;
+    }
     const TcGroup& G = sh.grp;
     // accumulators -> shared memory (row t; the operand buffers are free now)
     float* D = reinterpret_cast<float*>(smem);
