@@ -308,6 +308,20 @@ def main():
     prof = aggregate()
     host_ms = timed(pinned, True, args.steps)
 
+    # the same finds one at a time (untimed): per-kernel event times without
+    # other streams' kernels interleaved
+    def isolated():
+        mg.set_correlation_path(args.path)
+        mg.profile_reset()
+        mg.profile_enable(True)
+        st = streams[0]
+        for im in dev:
+            mg.find_ncc_model(im, model, *ctl, stream=st.cuda_stream)
+        mg.profile_enable(False)
+        return mg.profile_read()
+
+    iso = pool.submit(isolated).result()
+
     def maxed(x):
         if world == 1:
             return x
@@ -338,11 +352,17 @@ def main():
     rstage = "track_tc" if args.path == "tensor" and stages.get("track_tc", {}).get("ms") else "track"
     d = stages[rstage]
     achieved = 2.0 * d["work"] / (d["ms"] / 1e3) / 1e12 if d["ms"] else None
+    di = iso[rstage]
+    achieved_iso = 2.0 * di["work"] / (di["ms"] / 1e3) / 1e12 if di["ms"] else None
     roof = {"bound": "tensor", "achieved": achieved, "peak": pk["tflops_sustained"], "unit": "TFLOP/s",
             "frac": achieved / pk["tflops_sustained"] if achieved else None,
             "traffic": traffic_from_profiles(kernel_names[rstage]),
             "kernel": kernel_names[rstage],
             "stage_share": d["ms"] / sum(v["ms"] for v in stages.values()),
+            "isolated": {"achieved": achieved_iso,
+                         "frac": achieved_iso / pk["tflops_sustained"] if achieved_iso else None,
+                         "ms_per_launch": di["ms"] / max(1, di["launches"]),
+                         "note": "same finds one at a time on one stream (untimed pass)"},
             "note": f"algorithmic correlation FLOPs (2 x MACs) over the stage's event time; peak = {pk['source']} "
                     f"dense bf16 sustained; " + (
                         f"fp16 operands (exact integer halves), FP32 accumulation in tensor memory; issued/"
@@ -366,6 +386,8 @@ def main():
         "gpu_launches": int(launches_total),
         "clocks": clocks.summary(),
         "stages_ms_per_find": {k: round(v["ms"] / max(1, prof["finds"]), 4) for k, v in stages.items()},
+        "stages_ms_per_find_isolated": {k: round(v["ms"] / max(1, iso["finds"]), 4) for k, v in iso.items()
+                                        if isinstance(v, dict)},
         "matches_per_scene": matches,
     }
     if other is not None:

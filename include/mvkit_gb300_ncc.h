@@ -132,9 +132,10 @@ MVG_API const char* mvg_last_error(void);
 MVG_API int32_t mvg_set_correlation_path(int32_t path);
 
 /* Per-thread stage profile of finds on this thread: CUDA events recorded on
- * the find's stream around each kernel group while enabled.  Stages 0..11:
+ * the find's stream around each kernel group while enabled.  Stages 0..12:
  * upload, pyramid, prefix, coarse, nms, track, dedup, score, sort, select,
- * refine, track_tc.  ms: summed event time; launches: kernels launched (counted also
+ * refine, track_tc (the tensor-core correlation kernel), tc_prep (its fp16
+ * planes and candidate grouping).  ms: summed event time; launches: kernels launched (counted also
  * while disabled); work: algorithmic multiply-adds (coarse, track) or
  * bilinear taps (score); finds: completed finds since the last reset. */
 MVG_API int32_t mvg_profile_enable(int32_t on);

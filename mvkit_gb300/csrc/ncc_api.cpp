@@ -4,7 +4,6 @@
 //   prepare  src/ncc_matching/matcher.cpp:343-851
 //   find     src/ncc_matching/matcher.cpp:1063-1076
 //   C API    src/c_api/ncc_matching_api.cpp:29-203
-#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -229,32 +228,6 @@ const OrigDev& coarse_original(mvg_ncc_model_s& m, size_t level) {
     m.coarse_original[level] = std::move(o);
   }
   return *m.coarse_original[level];
-}
-
-using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-// 3-D TMA descriptor of the fp16 planes (x, row, plane): boxes of 8 columns x
-// `rows` rows of one plane, zero fill outside.
-void encode_planes_map(CUtensorMap* map, const uint16_t* planes, int pitch, int height, int parts, int rows) {
-  static const EncodeTiledFn fn = [] {
-    void* f = nullptr;
-    cudaDriverEntryPointQueryResult q{};
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
-        q != cudaDriverEntryPointSuccess)
-      f = nullptr;
-    return reinterpret_cast<EncodeTiledFn>(f);
-  }();
-  if (!fn) raise(kInternal, "cuTensorMapEncodeTiled is not available from the driver");
-  const cuuint64_t dims[3] = {cuuint64_t(pitch), cuuint64_t(height), cuuint64_t(kTcPlaneShifts * parts)};
-  const cuuint64_t strides[2] = {cuuint64_t(pitch) * 2, cuuint64_t(pitch) * 2 * cuuint64_t(height)};
-  const cuuint32_t box[3] = {8, cuuint32_t(rows), 1};
-  const cuuint32_t elem[3] = {1, 1, 1};
-  const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, const_cast<uint16_t*>(planes), dims, strides, box,
-                        elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                        CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) raise(kInternal, "cuTensorMapEncodeTiled failed (" + std::to_string(int(r)) + ")");
 }
 
 // Correlation path of this thread's finds: tensor cores where applicable
@@ -620,9 +593,9 @@ Workspace& workspace() {
 // Per-thread stage profile: CUDA events on the find's stream around each
 // kernel group (only while enabled), launch counts and algorithmic work.
 enum Stage { kStUpload, kStPyramid, kStPrefix, kStCoarse, kStNms, kStTrack, kStDedup, kStScore, kStSort, kStSelect,
-             kStRefine, kStTrackTc, kStages };
-const char* const kStageNames[kStages] = {"upload", "pyramid", "prefix", "coarse", "nms", "track",
-                                          "dedup", "score", "sort", "select", "refine", "track_tc"};
+             kStRefine, kStTrackTc, kStTcPrep, kStages };
+const char* const kStageNames[kStages] = {"upload", "pyramid", "prefix", "coarse",   "nms",      "track",  "dedup",
+                                          "score",  "sort",    "select", "refine",   "track_tc", "tc_prep"};
 struct Profiler {
   bool on = false;
   struct Mark {
@@ -1057,8 +1030,6 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
         ws.tc_offsets.reserve(size_t(ng));
         ws.tc_cursor.reserve(size_t(ng));
         ws.tc_tiles.reserve(1);
-        CUtensorMap map;
-        encode_planes_map(&map, ws.tc_planes.p, pitch, lev[t].h, P.parts, P.rows_slab);
         TcArgs tca;
         tca.lev = lev[t];
         tca.in = cur;
@@ -1081,15 +1052,22 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
         tca.sets = P.sets;
         tca.npad = P.npad;
         tca.plane_offset = P.offset;
+        tca.planes = ws.tc_planes.p;
+        tca.plane_pitch = pitch;
         tca.error = &st->error;
-        Span spt(kStTrackTc, s, 5);
-        check(launch_tc_planes(lev[t], ws.tc_planes.p, pitch, P.parts, P.offset, s), "tc planes");
-        // more than half an SM's shared memory: one block per SM, which owns
-        // all 512 tensor-memory columns
-        const size_t smem = std::max(P.smem, ws.smem_optin / 2 + 1024);
-        check(launch_tc_track(tca, &map, ng, ws.tc_counts.p, ws.tc_offsets.p, ws.tc_cursor.p, kMaxCandidates, smem,
-                              std::min(kTcMaxTiles, ws.sm_count), s),
-              "tc track");
+        {
+          Span spp(kStTcPrep, s, 4);
+          check(launch_tc_planes(lev[t], ws.tc_planes.p, pitch, P.parts, P.offset, s), "tc planes");
+          check(launch_tc_group(tca, ng, ws.tc_counts.p, ws.tc_offsets.p, ws.tc_cursor.p, kMaxCandidates, s),
+                "tc group");
+        }
+        {
+          // more than half an SM's shared memory: one block per SM, which
+          // owns all 512 tensor-memory columns
+          const size_t smem = std::max(P.smem, ws.smem_optin / 2 + 1024);
+          Span spt(kStTrackTc, s);
+          check(launch_tc_track(tca, smem, std::min(kTcMaxTiles, ws.sm_count), s), "tc track");
+        }
         ta.tc_dots = ws.tc_dots.p;
         ta.tc_group_of_src = d_tc_gsrc[t];
       }

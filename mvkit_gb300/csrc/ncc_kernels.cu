@@ -688,70 +688,77 @@ __global__ void __launch_bounds__(128) score_kernel(ScoreArgs a) {
 }
 
 // --------------------------------------------------------------------- sort
-// Candidates by score (descending), then row, column, angle ascending
-// (src/ncc_matching/matcher.cpp:824-827).  One block, bitonic on 64-bit
-// order-preserving keys; exact score ties fall back to the pose.
+// 64-bit keys ordering scores descending (order-preserving bit transform).
 __device__ __forceinline__ unsigned long long desc_key(double s) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(s);
   const unsigned long long asc = (b >> 63) ? ~b : (b | 0x8000000000000000ULL);
   return ~asc;
 }
 
-__device__ __forceinline__ bool before(const Cand* c, const unsigned long long* key, const int* idx, int a, int b) {
-  const int ia = idx[a], ib = idx[b];
-  if (ia < 0) return false;
-  if (ib < 0) return true;
-  const unsigned long long ka = key[a], kb = key[b];
-  if (ka != kb) return ka < kb;
-  const Cand x = c[ia], y = c[ib];
-  if (x.row != y.row) return x.row < y.row;
-  if (x.col != y.col) return x.col < y.col;
-  return x.angle < y.angle;
-}
-
-__global__ void __launch_bounds__(1024) sort_kernel(SortArgs a) {
-  extern __shared__ unsigned char smem[];
+// Rank sort: the output position of a candidate is the number of candidates
+// before it in the reference's order (score descending, then row, column,
+// angle; matcher.cpp:824-827).  Poses are unique after the merge, so the
+// ranks are a permutation.  A block ranks 64 candidates, four threads each
+// counting over a quarter of every 2048-key tile of the list in shared
+// memory; pose ties (equal keys) read the poses from global memory.
+constexpr int kSortPer = 64;
+__global__ void __launch_bounds__(256) sort_kernel(SortArgs a) {
+  __shared__ unsigned long long s_key[2048];
+  __shared__ int s_finite;
   const int n = a.state->count[a.slot];
-  int P = 1;
-  while (P < n) P <<= 1;
-  unsigned long long* key = reinterpret_cast<unsigned long long*>(smem);
-  int* idx = reinterpret_cast<int*>(key + P);
-  for (int t = threadIdx.x; t < P; t += blockDim.x) {
-    idx[t] = t < n ? t : -1;
-    key[t] = t < n ? desc_key(a.in[t].score) : ~0ULL;
+  if (int(blockIdx.x) * kSortPer >= n) return;
+  const int lane4 = threadIdx.x & 3;
+  const int i = blockIdx.x * kSortPer + (threadIdx.x >> 2);
+  Cand me{};
+  unsigned long long key = ~0ULL;
+  if (i < n) {
+    me = a.in[i];
+    key = desc_key(me.score);
   }
-  __syncthreads();
-  for (int k = 2; k <= P; k <<= 1)
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      for (int t = threadIdx.x; t < P; t += blockDim.x) {
-        const int l = t ^ j;
-        if (l > t) {
-          const bool up = (t & k) == 0;
-          const bool swap = up ? before(a.in, key, idx, l, t) : before(a.in, key, idx, t, l);
-          if (swap) {
-            const unsigned long long tk = key[t];
-            key[t] = key[l];
-            key[l] = tk;
-            const int ti = idx[t];
-            idx[t] = idx[l];
-            idx[l] = ti;
+  if (threadIdx.x == 0) s_finite = 0;
+  int rank = 0;
+  for (int base = 0; base < n; base += 2048) {
+    const int m = min(2048, n - base);
+    __syncthreads();
+    for (int k = threadIdx.x; k < m; k += 256) s_key[k] = desc_key(a.in[base + k].score);
+    __syncthreads();
+    if (i < n) {
+      int r0 = 0, r1 = 0;
+      int k = lane4;
+      for (; k + 4 < m; k += 8) {
+        const unsigned long long k0 = s_key[k], k1 = s_key[k + 4];
+        r0 += k0 < key;
+        r1 += k1 < key;
+        if (k0 == key || k1 == key) {
+          for (int q = 0; q < 2; ++q) {
+            const int kk = k + 4 * q;
+            if (s_key[kk] != key) continue;
+            const Cand c = a.in[base + kk];
+            if (c.row < me.row || (c.row == me.row && (c.col < me.col || (c.col == me.col && c.angle < me.angle))))
+              ++r0;
           }
         }
       }
-      __syncthreads();
+      for (; k < m; k += 4) {
+        const unsigned long long k0 = s_key[k];
+        r0 += k0 < key;
+        if (k0 == key) {
+          const Cand c = a.in[base + k];
+          if (c.row < me.row || (c.row == me.row && (c.col < me.col || (c.col == me.col && c.angle < me.angle))))
+            ++r0;
+        }
+      }
+      rank += r0 + r1;
     }
-  __shared__ int finite_count;
-  if (threadIdx.x == 0) finite_count = 0;
-  __syncthreads();
-  int local = 0;
-  for (int t = threadIdx.x; t < n; t += blockDim.x) {
-    const Cand c = a.in[idx[t]];
-    a.out[t] = c;
-    local += isfinite(c.score) ? 1 : 0;
   }
-  atomicAdd(&finite_count, local);
+  rank += __shfl_xor_sync(0xffffffffu, rank, 1);
+  rank += __shfl_xor_sync(0xffffffffu, rank, 2);
+  if (i < n && lane4 == 0) {
+    a.out[rank] = me;
+    if (isfinite(me.score)) atomicAdd(&s_finite, 1);
+  }
   __syncthreads();
-  if (threadIdx.x == 0) a.state->sorted_count = finite_count;
+  if (threadIdx.x == 0 && s_finite) atomicAdd(&a.state->sorted_count, s_finite);
 }
 
 // ----------------------------------------------------------------- overlap
@@ -1526,9 +1533,7 @@ cudaError_t launch_score(const ScoreArgs& a, int max_candidates, cudaStream_t s)
 }
 
 cudaError_t launch_sort(const SortArgs& a, cudaStream_t s) {
-  const size_t smem = 16384 * (sizeof(unsigned long long) + sizeof(int));
-  if (const cudaError_t e = reserve_dynamic_smem(reinterpret_cast<const void*>(sort_kernel), smem)) return e;
-  sort_kernel<<<1, 1024, smem, s>>>(a);
+  sort_kernel<<<(kMaxCandidates + kSortPer - 1) / kSortPer, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -124,6 +124,8 @@ struct TcArgs {
   int stage_bytes, abuf_bytes;           // bytes per weight buffer / per window buffer
   int sets, npad;                        // accumulator sets (grid row y -> set y mod sets), columns per set
   float plane_offset;                    // level value subtracted in the planes
+  const uint16_t* planes;                // fp16 planes (launch_tc_planes)
+  int plane_pitch;                       // elements per plane row
   int32_t* error;
 };
 
@@ -133,9 +135,10 @@ struct TcArgs {
 cudaError_t launch_tc_planes(const LevelImage& lev, uint16_t* planes, int pitch, int parts, float offset,
                              cudaStream_t s);
 size_t tc_kernel_static_smem();
-// `map` is the 3-D TMA descriptor (x, row, plane) of the planes (128 bytes).
-cudaError_t launch_tc_track(const TcArgs& a, const void* map, int ngroups, int32_t* counts, int32_t* offsets,
-                            int32_t* cursor, int max_candidates, size_t smem, int grid, cudaStream_t s);
+// Groups the step's candidates into tiles (counts, tile list, order).
+cudaError_t launch_tc_group(const TcArgs& a, int ngroups, int32_t* counts, int32_t* offsets, int32_t* cursor,
+                            int max_candidates, cudaStream_t s);
+cudaError_t launch_tc_track(const TcArgs& a, size_t smem, int grid, cudaStream_t s);
 
 struct DedupArgs {
   const Cand* in;

@@ -17,31 +17,29 @@
 // accumulator sets in tensor memory, summed in FP32 by the epilogue.
 // Windows come straight from fp16 copies of the level ("planes", exact
 // integers: the level minus a constant, split into a high and a low plane
-// when a level's values exceed fp16's integer range) by TMA, one 16-byte
-// column strip per transfer, into the canonical no-swizzle K-major layout
-// whose row pitch is 16 bytes, so grid row y is the same tiles started y rows
-// later.  Eight column-shifted copies of each plane keep every TMA start on a
-// 16-byte boundary; planes start 8 columns left of the level so that a
-// transfer outside a plane is outside the level too (zero fill).  Weights
-// (fp16 high and low halves of the scaled weights) stream through a ring of
-// shared-memory buffers with bulk copies.  The block is warp-specialised: a
-// window-producer warp (two slab buffers), a weight-producer thread and an
-// MMA-issue thread; accumulation is FP32 in tensor memory.  The
+// when a level's values exceed fp16's integer range), 16 bytes per cp.async,
+// into the canonical no-swizzle K-major layout whose row pitch is 16 bytes,
+// so grid row y is the same tiles started y rows later.  Eight
+// column-shifted copies of each plane keep every copy on a 16-byte boundary;
+// planes start 8 columns left of the level.  Weights (fp16 high and low
+// halves of the scaled weights) stream through a ring of shared-memory
+// buffers with bulk copies (TMA engine).  The block is warp-specialised:
+// four window-producer warps (two slab buffers), a weight-producer thread
+// and an MMA-issue thread; accumulation is FP32 in tensor memory.  The
 // epilogue writes sum w (S - S0) per placement; track_kernel adds the exact
 // integer window moments and applies the reference's selection rule.
-#include <cuda.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
-#include <cstring>
 
 #include "ncc_kernels.h"
 
 namespace mvg {
 namespace {
 
-constexpr int kTcThreads = 128;
+constexpr int kTcThreads = 192;     // warp 0 MMA, warp 1 weights, warps 2-5 windows
+constexpr int kTcWindowThreads = 128;
 constexpr int kTcRows = 128;                  // MMA M
 constexpr uint32_t kTmemCols = 512;           // accumulator sets x columns per set
 constexpr long long kSpinLimit = 1ll << 22;   // mbarrier polls before giving up
@@ -69,8 +67,12 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
                : "memory");
 }
 
-__device__ __forceinline__ void bar_init(uint64_t* bar) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)));
+__device__ __forceinline__ void bar_init(uint64_t* bar, uint32_t count = 1) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void bar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 __device__ __forceinline__ void expect_tx(uint64_t* bar, uint32_t bytes) {
@@ -98,12 +100,10 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
                : "memory");
 }
 
-__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-      "[%5];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
-      : "memory");
+// 16 bytes global -> shared, zero-filled when `valid` is false
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, bool valid) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(valid ? 16 : 0)
+               : "memory");
 }
 
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
@@ -173,8 +173,14 @@ __device__ void tc_mma_role(const TcArgs& a, TcShared& sh, uint8_t* wbase, uint8
       tc_fail(a, sh);
       return;
     }
-    const uint32_t a0 = smem_u32(abase + size_t(buf) * a.abuf_bytes);
+    // descriptors advance by plain adds of the 16-byte address units: one row
+    // per grid row, two segments (2 lbo) per K step; weights 256 bytes per K step
+    const uint64_t a_desc0 = smem_desc(smem_u32(abase + size_t(buf) * a.abuf_bytes), sp.lbo, sp.sbo);
+    const uint64_t a_kstep = uint64_t(2 * sp.lbo) >> 4;
+    const uint64_t b_desc0 = smem_desc(smem_u32(wbase), 128, uint32_t(sp.K / 8) * 128);
+    const uint64_t b_stage = uint64_t(a.stage_bytes) >> 4;
     const int y0 = sl * sp.Y, y1 = min(G.kr, y0 + sp.Y);
+    int set = y0 % a.sets;
     for (int y = y0; y < y1; ++y) {
       const int st = int(cm % S);
       if (!bar_wait(&sh.b_full[st], uint32_t((cm / S) & 1))) {
@@ -182,46 +188,60 @@ __device__ void tc_mma_role(const TcArgs& a, TcShared& sh, uint8_t* wbase, uint8
         return;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t arow = a0 + uint32_t(y - y0) * 16;
-      const uint32_t b0 = smem_u32(wbase + size_t(st) * a.stage_bytes);
-      const uint32_t d = tmem + uint32_t((y % a.sets) * a.npad);
-      for (int j = 0; j < sp.ksteps; ++j)
-        mma_f16(d, smem_desc(arow + uint32_t(2 * j) * sp.lbo, sp.lbo, sp.sbo),
-                smem_desc(b0 + uint32_t(j) * 256, 128, uint32_t(sp.K / 8) * 128), idesc,
-                (y >= a.sets || j > 0) ? 1u : 0u);
+      uint64_t ad = a_desc0 + uint64_t(y - y0), bd = b_desc0 + uint64_t(st) * b_stage;
+      const uint32_t d = tmem + uint32_t(set * a.npad);
+      mma_f16(d, ad, bd, idesc, y >= a.sets ? 1u : 0u);
+      for (int j = 1; j < sp.ksteps; ++j) {
+        ad += a_kstep;
+        bd += 16;
+        mma_f16(d, ad, bd, idesc, 1u);
+      }
       mma_commit(&sh.b_empty[st]);
       ++cm;
+      if (++set == a.sets) set = 0;
     }
     mma_commit(&sh.slab_done[buf]);
     ++sm;
   }
 }
 
-// Window producer (one warp): per slab, once the MMAs of the slab that last
-// used the buffer are done, one TMA box (8 columns x rows_slab rows) per
-// candidate and plane segment.
-__device__ void tc_window_role(const TcArgs& a, const CUtensorMap* map, TcShared& sh, uint8_t* abase, int& sa,
-                               int lane) {
+// Window producers (four warps): per slab, once the MMAs of the slab that
+// last used the buffer are done, 16-byte cp.async copies from the planes
+// (zero outside them); a warp's copies are 8 rows x 4 segments, so its global
+// reads are 64-byte row pieces and its shared writes 128-byte row runs.
+// Each thread waits for its own copies, orders them for the tensor cores
+// (proxy fence) and arrives on the buffer's barrier (128 arrivals).
+__device__ void tc_window_role(const TcArgs& a, TcShared& sh, uint8_t* abase, int& sa, int pt) {
   const TcGroup& G = sh.grp;
   const TcShape sp(G);
-  const int cnt = sh.cnt;
+  const int cnt = sh.cnt, rows = G.rows_slab, H = a.lev.h, pitch = a.plane_pitch;
+  const size_t plane = size_t(H) * size_t(pitch);
+  const int lane = pt & 31, wp = pt >> 5;
+  const int rblocks = rows / 8, sblocks = (sp.nplane + 3) / 4;
+  const int items = cnt * rblocks * sblocks;  // one per warp-iteration
   for (int sl = 0; sl < sp.nslabs; ++sl) {
     const int buf = sa & 1;
-    int ok = 1;
-    if (lane == 0) {
-      if (sa >= 2) ok = bar_wait(&sh.slab_done[buf], uint32_t(((sa >> 1) - 1) & 1));
-      if (ok) expect_tx(&sh.a_full[buf], uint32_t(cnt * sp.nplane) * sp.lbo);
-      else tc_fail(a, sh);
+    if (sa >= 2 && !bar_wait(&sh.slab_done[buf], uint32_t(((sa >> 1) - 1) & 1))) {
+      tc_fail(a, sh);
+      return;
     }
-    if (!__shfl_sync(0xffffffffu, ok, 0)) return;
-    uint8_t* dst = abase + size_t(buf) * a.abuf_bytes;
+    uint8_t* dst0 = abase + size_t(buf) * a.abuf_bytes;
     const int y0 = sl * sp.Y;
-    for (int it = lane; it < cnt * sp.nplane; it += 32) {
-      const int g = it / sp.nplane, sg = it % sp.nplane, q = sg / sp.segs, s = sg % sp.segs;
-      tma_load_3d(dst + size_t(g) * sp.sbo + size_t(sg) * sp.lbo, map, sh.x0a[g] + kTcPlaneMargin + 8 * s,
-                  sh.R[g] - 2 + G.rmin + y0, q * kTcPlaneShifts + sh.delta[g], &sh.a_full[buf]);
+    for (int it = wp; it < items; it += kTcWindowThreads / 32) {
+      const int g = it / (rblocks * sblocks), rem = it % (rblocks * sblocks);
+      const int r = (rem / sblocks) * 8 + (lane & 7), sg = (rem % sblocks) * 4 + (lane >> 3);
+      if (sg >= sp.nplane) continue;
+      const int q = sg / sp.segs, s = sg % sp.segs;
+      const int row = sh.R[g] - 2 + G.rmin + y0 + r;
+      const int x = sh.x0a[g] + kTcPlaneMargin + 8 * s;
+      const bool valid = row >= 0 && row < H && x >= 0 && x + 8 <= pitch;
+      const uint16_t* src =
+          a.planes + size_t(q * kTcPlaneShifts + sh.delta[g]) * plane + (valid ? size_t(row) * pitch + x : 0);
+      cp_async16(dst0 + size_t(g) * sp.sbo + size_t(sg) * sp.lbo + size_t(r) * 16, src, valid);
     }
-    __syncwarp();
+    asm volatile("cp.async.commit_group;\n cp.async.wait_group 0;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    bar_arrive(&sh.a_full[buf]);
     ++sa;
   }
 }
@@ -245,11 +265,11 @@ __device__ void tc_weight_role(const TcArgs& a, TcShared& sh, uint8_t* wbase, lo
 }
 
 // Persistent and warp-specialised: block b takes tiles b, b + gridDim.x, ...;
-// per tile warp 0 issues the MMAs, warp 1 stages windows, warp 2 streams
-// weights, and all four warps run the set-up and the epilogue.  Shared
+// per tile warp 0 issues the MMAs, warp 1 streams weights, warps 2-5 stage
+// windows, and all six warps run the set-up and the epilogue.  Shared
 // memory: weight ring (stages x stage_bytes) | two window buffers.
 __global__ void __launch_bounds__(kTcThreads, 1)
-    tc_track_kernel(const __grid_constant__ TcArgs a, const __grid_constant__ CUtensorMap map) {
+    tc_track_kernel(const __grid_constant__ TcArgs a) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ TcShared sh;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
@@ -259,8 +279,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   uint8_t* wbase = smem;
   uint8_t* abase = smem + size_t(a.stages) * a.stage_bytes;
   if (t == 0) {
-    bar_init(&sh.a_full[0]);
-    bar_init(&sh.a_full[1]);
+    bar_init(&sh.a_full[0], kTcWindowThreads);
+    bar_init(&sh.a_full[1], kTcWindowThreads);
     bar_init(&sh.slab_done[0]);
     bar_init(&sh.slab_done[1]);
     bar_init(&sh.drain);
@@ -351,14 +371,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
       __syncwarp();
     } else if (warp == 1) {
-      tc_window_role(a, &map, sh, abase, sa, lane);
-      if (lane == 0) sh.sa = sa;
-    } else if (warp == 2) {
       if (lane == 0) {
         tc_weight_role(a, sh, wbase, cb);
         sh.cb = cb;
       }
       __syncwarp();
+    } else {
+      tc_window_role(a, sh, abase, sa, t - 64);
+      if (t == 64) sh.sa = sa;
     }
     __syncthreads();
     if (!sh.fail) {
@@ -373,7 +393,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       if (t == 0) {
         for (long long c = sh.cm; c < sh.cb; ++c)
           bar_wait(&sh.b_full[int(c % a.stages)], uint32_t((c / a.stages) & 1));
-        for (int sl = sh.sm; sl < sh.sa; ++sl) bar_wait(&sh.a_full[sl & 1], uint32_t((sl >> 1) & 1));
         mma_commit(&sh.drain);
         bar_wait(&sh.drain, 0);
       }
@@ -385,39 +404,40 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     float* D = reinterpret_cast<float*>(smem);
     const int ld = G.n + 1;
     const int nsets = min(a.sets, G.kr);
-    for (int c0 = 0; c0 < G.n; c0 += 32) {
-      float acc[32];
-      tmem_ld32(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0), acc);
-      for (int set = 1; set < nsets; ++set) {
-        float v[32];
-        tmem_ld32(tmem + (uint32_t(warp * 32) << 16) + uint32_t(set * a.npad + c0), v);
+    if (warp < 4)  // warp w reads tensor-memory lanes 32w..32w+31
+      for (int c0 = 0; c0 < G.n; c0 += 32) {
+        float acc[32];
+        tmem_ld32(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0), acc);
+        for (int set = 1; set < nsets; ++set) {
+          float v[32];
+          tmem_ld32(tmem + (uint32_t(warp * 32) << 16) + uint32_t(set * a.npad + c0), v);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) acc[j] += v[j];
+          for (int j = 0; j < 32; ++j) acc[j] += v[j];
+        }
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          if (c0 + j < G.n) D[t * ld + c0 + j] = acc[j];
       }
-#pragma unroll
-      for (int j = 0; j < 32; ++j)
-        if (c0 + j < G.n) D[t * ld + c0 + j] = acc[j];
-    }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    const int g = t >> 3, dr = t & 7;
-    if (g < sh.cnt && dr < 5) {
+    // one item = (candidate, row placement, patch): five column placements
+    for (int it = t; it < sh.cnt * 5 * G.p; it += kTcThreads) {
+      const int g = it / (5 * G.p), dr = (it / G.p) % 5, q = it % G.p;
+      const int m = g * 8 + dr;  // accumulator row
       const int ci = sh.ci[g], R = sh.R[g], C = sh.C[g];
       const float cen = sh.centre[g];
       const int W = a.lev.w, H = a.lev.h;
-      for (int q = 0; q < G.p; ++q) {
-        float* out = a.dots + size_t(ci) * kTcScoreStride + size_t(G.k_of[q]) * 25 + dr * 5;
-        const int sr = min(max(R + dr - 2 + G.r0[q], 0), H - 1);
-        const float* srow = a.lev.v + size_t(sr) * W;
-        for (int dc = 0; dc < 5; ++dc) {
-          const int n0 = (q * 5 + dc) * 2;
-          // sum w (S - c) with c the centre, as accumulated
-          const float raw = (D[t * ld + n0] + D[t * ld + n0 + 1]) * G.inv_scale;
-          const float s0 = srow[min(max(C + dc - 2 + G.c0[q], 0), W - 1)] - a.plane_offset;
-          // sum w (S - S0) = raw + c (ecorr - weff) + (c - S0) weff: ecorr is
-          // the row-sum total as subtracted, weff the weights' sum
-          out[dc] = raw + (cen * (G.ecorr[q] - G.weff[q]) + (cen - s0) * G.weff[q]);
-        }
+      float* out = a.dots + size_t(ci) * kTcScoreStride + size_t(G.k_of[q]) * 25 + dr * 5;
+      const int sr = min(max(R + dr - 2 + G.r0[q], 0), H - 1);
+      const float* srow = a.lev.v + size_t(sr) * W;
+      for (int dc = 0; dc < 5; ++dc) {
+        const int n0 = (q * 5 + dc) * 2;
+        // sum w (S - c) with c the centre, as accumulated
+        const float raw = (D[m * ld + n0] + D[m * ld + n0 + 1]) * G.inv_scale;
+        const float s0 = srow[min(max(C + dc - 2 + G.c0[q], 0), W - 1)] - a.plane_offset;
+        // sum w (S - S0) = raw + c (ecorr - weff) + (c - S0) weff: ecorr is
+        // the row-sum total as subtracted, weff the weights' sum
+        out[dc] = raw + (cen * (G.ecorr[q] - G.weff[q]) + (cen - s0) * G.weff[q]);
       }
     }
     if (t == 0) {
@@ -473,23 +493,42 @@ __global__ void tc_count_kernel(const Cand* in, const QueryState* state, int slo
   if (gi >= 0) atomicAdd(counts + gi, 1);
 }
 
-__global__ void tc_plan_kernel(const int32_t* counts, int ngroups, int32_t* offsets, int32_t* cursor, TcTiles* tiles,
-                               int max_tiles) {
-  if (threadIdx.x != 0) return;
-  int at = 0, nt = 0;
-  for (int gi = 0; gi < ngroups; ++gi) {
-    offsets[gi] = at;
-    cursor[gi] = 0;
-    const int c = counts[gi];
-    for (int f = 0; f < c && nt < max_tiles; f += kTcCands) {
-      tiles->group[nt] = gi;
-      tiles->first[nt] = at + f;
-      tiles->last[nt] = at + min(c, f + kTcCands);
-      ++nt;
-    }
-    at += c;
+// Tile list: per group, tiles of up to 16 candidates in order (block-wide
+// scan of the per-group candidate and tile counts, 1024 threads).
+__global__ void __launch_bounds__(1024) tc_plan_kernel(const int32_t* counts, int ngroups, int32_t* offsets,
+                                                       int32_t* cursor, TcTiles* tiles, int max_tiles) {
+  __shared__ int s_cand[1024], s_tile[1024];
+  const int t = threadIdx.x, per = (ngroups + 1023) / 1024;
+  const int g0 = min(ngroups, t * per), g1 = min(ngroups, g0 + per);
+  int c = 0, n = 0;
+  for (int g = g0; g < g1; ++g) {
+    c += counts[g];
+    n += (counts[g] + kTcCands - 1) / kTcCands;
   }
-  tiles->count = nt;
+  s_cand[t] = c;
+  s_tile[t] = n;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    const int a = t >= off ? s_cand[t - off] : 0, b = t >= off ? s_tile[t - off] : 0;
+    __syncthreads();
+    s_cand[t] += a;
+    s_tile[t] += b;
+    __syncthreads();
+  }
+  int at = s_cand[t] - c, nt = s_tile[t] - n;
+  for (int g = g0; g < g1; ++g) {
+    offsets[g] = at;
+    cursor[g] = 0;
+    const int cg = counts[g];
+    for (int f = 0; f < cg; f += kTcCands, ++nt) {
+      if (nt >= max_tiles) continue;
+      tiles->group[nt] = g;
+      tiles->first[nt] = at + f;
+      tiles->last[nt] = at + min(cg, f + kTcCands);
+    }
+    at += cg;
+  }
+  if (t == 1023) tiles->count = min(s_tile[1023], max_tiles);
 }
 
 __global__ void tc_scatter_kernel(const Cand* in, const QueryState* state, int slot, const int32_t* group_of_src,
@@ -514,17 +553,19 @@ cudaError_t launch_tc_planes(const LevelImage& lev, uint16_t* planes, int pitch,
   return cudaGetLastError();
 }
 
-cudaError_t launch_tc_track(const TcArgs& a, const void* map, int ngroups, int32_t* counts, int32_t* offsets,
-                            int32_t* cursor, int max_candidates, size_t smem, int grid, cudaStream_t s) {
+cudaError_t launch_tc_group(const TcArgs& a, int ngroups, int32_t* counts, int32_t* offsets, int32_t* cursor,
+                            int max_candidates, cudaStream_t s) {
   if (cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int32_t) * size_t(ngroups), s)) return e;
   const unsigned blocks = unsigned((max_candidates + 255) / 256);
   tc_count_kernel<<<blocks, 256, 0, s>>>(a.in, a.state, a.in_slot, a.group_of_src, counts);
-  tc_plan_kernel<<<1, 32, 0, s>>>(counts, ngroups, offsets, cursor, a.tiles, kTcMaxTiles);
+  tc_plan_kernel<<<1, 1024, 0, s>>>(counts, ngroups, offsets, cursor, a.tiles, kTcMaxTiles);
   tc_scatter_kernel<<<blocks, 256, 0, s>>>(a.in, a.state, a.in_slot, a.group_of_src, offsets, cursor, a.order);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tc_track(const TcArgs& a, size_t smem, int grid, cudaStream_t s) {
   if (cudaError_t e = reserve_dynamic_smem(reinterpret_cast<const void*>(tc_track_kernel), smem)) return e;
-  CUtensorMap m;
-  std::memcpy(&m, map, sizeof(m));
-  tc_track_kernel<<<grid, kTcThreads, smem, s>>>(a, m);
+  tc_track_kernel<<<grid, kTcThreads, smem, s>>>(a);
   return cudaGetLastError();
 }
 

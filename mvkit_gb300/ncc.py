@@ -352,7 +352,7 @@ class PinnedBuffer:
             pass
 
 
-PROFILE_STAGES = 12
+PROFILE_STAGES = 13
 
 
 def set_correlation_path(path: str) -> None:
