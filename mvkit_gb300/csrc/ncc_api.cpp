@@ -173,21 +173,34 @@ struct DevLevel {
 
 struct OrigDev {
   DevBuf<float> dr, dc, w;
+  DevBuf<float4> dcw;
+  float box[4] = {0, 0, 0, 0};
   int32_t n = 0;
   void set(const Raster& r, double orow, double ocol) {
     std::vector<float> a(r.size()), b(r.size()), c(r.size());
+    std::vector<float4> packed(r.size());
+    box[0] = box[2] = INFINITY;
+    box[1] = box[3] = -INFINITY;
     for (size_t i = 0; i < r.size(); ++i) {
       a[i] = float(double(r.rows[i]) - orow);
       b[i] = float(double(r.cols[i]) - ocol);
       c[i] = float(r.w[i]);
+      packed[i] = make_float4(a[i], b[i], c[i], 0.f);
+      box[0] = std::min(box[0], a[i]);
+      box[1] = std::max(box[1], a[i]);
+      box[2] = std::min(box[2], b[i]);
+      box[3] = std::max(box[3], b[i]);
     }
     dr.upload(a, nullptr);
     dc.upload(b, nullptr);
     w.upload(c, nullptr);
+    dcw.upload(packed, nullptr);
     n = int32_t(r.size());
     check(cudaDeviceSynchronize(), "model upload");
   }
-  OriginalView view() const { return OriginalView{dr.p, dc.p, w.p, n}; }
+  OriginalView view() const {
+    return OriginalView{dr.p, dc.p, w.p, dcw.p, box[0], box[1], box[2], box[3], n};
+  }
 };
 
 }  // namespace
@@ -820,6 +833,10 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
       const PatchDesc& d = m.levels[li]->desc[size_t(p)];
       if (!lattice_exact32(d.orow) || !lattice_exact32(d.ocol)) exact32 = false;
     }
+  // longest run of any patch per level (bounds a run's moment sums)
+  int max_run[kMaxLevels] = {};
+  for (size_t li = 0; li < level_count; ++li)
+    for (const PatchDesc& d : m.levels[li]->desc) max_run[li] = std::max(max_run[li], d.cmax - d.cmin + 1);
   // tensor-core plans of the tracking steps (cached per target level)
   std::vector<std::shared_ptr<const TcPlan>> tc(level_count);
   if (t_path == 0) {
@@ -927,6 +944,10 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     if (!need) continue;
     ws.lev_p[l].reserve(size_t(lw[l] + 1) * size_t(lh[l]));
     lev[l].prefix = ws.lev_p[l].p;
+    // 8-byte prefixes (uint32 modulo 2^32) when a run's sum of S^2 fits
+    const double maxv = (type == 1 ? 65535.0 : 255.0) * std::ldexp(1., int(2 * l));
+    lev[l].prefix32 =
+        double(max_run[l]) * maxv * maxv < 4294967296.0 ? reinterpret_cast<uint2*>(ws.lev_p[l].p) : nullptr;
     Span sp(kStPrefix, s);
     check(launch_prefix(lev[l], s), "prefix");
   }

@@ -93,12 +93,30 @@ __device__ __forceinline__ float window_score(float dot, long long s1, long long
   return absolute ? fabsf(s) : s;
 }
 
-__device__ __forceinline__ void window_moments(const longlong2* __restrict__ P, int pitch, int r, int c,
+// Window moments {sum S, sum S^2} of a patch at (r, c) from the level's row
+// prefixes: runs first, first + step, ... (step > 1 splits the runs over
+// threads; the caller adds the parts).
+__device__ __forceinline__ void window_moments(const LevelImage& lev, int pitch, int r, int c,
                                                const int32_t* __restrict__ runs, const int32_t* __restrict__ ends,
-                                               int nruns, long long& s1, long long& s2) {
+                                               int nruns, long long& s1, long long& s2, int first = 0,
+                                               int step = 1) {
   s1 = 0;
   s2 = 0;
-  for (int j = 0; j < nruns; ++j) {
+  if (lev.prefix32) {
+    const uint2* __restrict__ P = lev.prefix32;
+    for (int j = first; j < nruns; j += step) {
+      const int32_t rb = __ldg(runs + j);
+      const int e = __ldg(ends + j);
+      const size_t base = size_t(r + run_row(rb)) * pitch + c;
+      const uint2 hi = P[base + e + 1];
+      const uint2 lo = P[base + run_begin(rb)];
+      s1 += (long long)(hi.x - lo.x);
+      s2 += (long long)(hi.y - lo.y);
+    }
+    return;
+  }
+  const longlong2* __restrict__ P = lev.prefix;
+  for (int j = first; j < nruns; j += step) {
     const int32_t rb = __ldg(runs + j);
     const int e = __ldg(ends + j);
     const size_t base = size_t(r + run_row(rb)) * pitch + c;
@@ -144,7 +162,13 @@ __global__ void prefix_kernel(LevelImage lev) {
   if (warp >= lev.h) return;
   const float* row = lev.v + size_t(warp) * lev.w;
   longlong2* out = lev.prefix + size_t(warp) * (lev.w + 1);
-  if (lane == 0) out[0] = make_longlong2(0, 0);
+  uint2* out32 = lev.prefix32 ? lev.prefix32 + size_t(warp) * (lev.w + 1) : nullptr;
+  if (lane == 0) {
+    if (out32)
+      out32[0] = make_uint2(0, 0);
+    else
+      out[0] = make_longlong2(0, 0);
+  }
   long long c1 = 0, c2 = 0;
   for (int base = 0; base < lev.w; base += 32) {
     const int c = base + lane;
@@ -158,7 +182,12 @@ __global__ void prefix_kernel(LevelImage lev) {
         b += ub;
       }
     }
-    if (c < lev.w) out[c + 1] = make_longlong2(c1 + a, c2 + b);
+    if (c < lev.w) {
+      if (out32)
+        out32[c + 1] = make_uint2(uint32_t(c1 + a), uint32_t(c2 + b));
+      else
+        out[c + 1] = make_longlong2(c1 + a, c2 + b);
+    }
     c1 += __shfl_sync(0xffffffffu, a, 31);
     c2 += __shfl_sync(0xffffffffu, b, 31);
   }
@@ -208,7 +237,7 @@ __global__ void __launch_bounds__(256) coarse_kernel(CoarseArgs a) {
       acc0 = fmaf(__int_as_float(x.y), base[off_row(x.x) * TW + off_col(x.x)] - s0, acc0);
     }
     long long s1, s2;
-    window_moments(a.lev.prefix, w + 1, r, c, a.view.runs + pd.run_off, a.view.runs_end + pd.run_off, pd.nruns, s1, s2);
+    window_moments(a.lev, w + 1, r, c, a.view.runs + pd.run_off, a.view.runs_end + pd.run_off, pd.nruns, s1, s2);
     score = window_score(acc0 + acc1, s1, s2, pd.n, a.absolute);
   }
   a.planes[(size_t(p) * h + r) * w + c] = score;
@@ -265,7 +294,7 @@ __global__ void nms_kernel(NmsArgs a) {
 constexpr int kTrackThreads = 256;
 constexpr int kTrackMaxSel = 64;
 
-__global__ void __launch_bounds__(kTrackThreads) track_kernel(TrackArgs a) {
+__global__ void __launch_bounds__(kTrackThreads, 5) track_kernel(TrackArgs a) {
   extern __shared__ float win[];
   const int i = blockIdx.x;
   if (i >= a.state->count[a.in_slot]) return;
@@ -275,6 +304,9 @@ __global__ void __launch_bounds__(kTrackThreads) track_kernel(TrackArgs a) {
   __shared__ int s_n, s_split, s_wr0, s_wc0, s_wh, s_wcols, s_staged;
   __shared__ float s_centre;
   __shared__ float s_part[kTrackThreads];
+  // moment partials of the slices (launches with tensor-core items only)
+  long long* s_m1 = a.split_off >= 0 ? reinterpret_cast<long long*>(win + a.split_off) : nullptr;
+  long long* s_m2 = s_m1 ? s_m1 + kTrackThreads : nullptr;
   __shared__ float s_wbest[kTrackThreads / 32];
   __shared__ int s_word[kTrackThreads / 32];
   const Cand cd = a.in[i];
@@ -410,9 +442,19 @@ __global__ void __launch_bounds__(kTrackThreads) track_kernel(TrackArgs a) {
       }
       acc += acc1;
     }
-    // combine the sample slices of one item (threads item + q * items)
+    // window moments: with scratch, the runs split over the item's slices
+    // like the samples; otherwise in slice 0
+    long long s1 = 0, s2 = 0;
+    if (valid && (s_m1 || part == 0))
+      window_moments(a.lev, pitch + 1, r, c, a.view.runs + pd.run_off, a.view.runs_end + pd.run_off, pd.nruns, s1,
+                     s2, s_m1 ? part : 0, s_m1 ? split : 1);
+    // combine the slices of one item (threads item + q * items)
     if (split > 1) {
       s_part[threadIdx.x] = acc;
+      if (s_m1) {
+        s_m1[threadIdx.x] = s1;
+        s_m2[threadIdx.x] = s2;
+      }
       __syncthreads();
     }
     if (part == 0 && valid) {
@@ -425,9 +467,11 @@ __global__ void __launch_bounds__(kTrackThreads) track_kernel(TrackArgs a) {
         // sum w (S - S0) = sum w (S - centre) - (S0 - centre) sum w
         if (staged) dot = fmaf(-x0, pd.wsum, dot);
       }
-      long long s1, s2;
-      window_moments(a.lev.prefix, pitch + 1, r, c, a.view.runs + pd.run_off, a.view.runs_end + pd.run_off,
-                     pd.nruns, s1, s2);
+      if (s_m1)
+        for (int q = 1; q < split; ++q) {
+          s1 += s_m1[threadIdx.x + q * items];
+          s2 += s_m2[threadIdx.x + q * items];
+        }
       const float sc = window_score(dot, s1, s2, pd.n, a.absolute);
       if (better(sc, item, best, border)) {
         best = sc;
@@ -605,6 +649,28 @@ __device__ __forceinline__ LocalPose make_local(double row, double col, double a
   return l;
 }
 
+// True when every sample of the rotated original lies inside the image by a
+// margin: the sample positions are affine in (dr, dc), so the corners of the
+// offset box bound them (the margin covers FP32 rounding of the per-sample
+// expressions).  Inside, the passes drop their per-sample bounds tests.
+__device__ __forceinline__ bool samples_inside(const LocalPose& L, const OriginalView& o, float hmin, float hmax,
+                                               float wmin, float wmax) {
+  float y0 = INFINITY, y1 = -INFINITY, x0 = INFINITY, x1 = -INFINITY;
+  const float drs[2] = {o.dr_min, o.dr_max}, dcs[2] = {o.dc_min, o.dc_max};
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const float y = L.fr + (L.ca * drs[i] - L.sa * dcs[j]), x = L.fc + (L.sa * drs[i] + L.ca * dcs[j]);
+      y0 = fminf(y0, y);
+      y1 = fmaxf(y1, y);
+      x0 = fminf(x0, x);
+      x1 = fmaxf(x1, x);
+    }
+  const float m = 1e-2f;
+  return y0 >= hmin + m && x0 >= wmin + m && y1 <= hmax - 1.f - m && x1 <= wmax - 1.f - m;
+}
+
 // Shared state of a block working on one pose at a time.
 struct PoseShared {
   LocalPose lp;
@@ -651,6 +717,23 @@ __device__ void continuous_pass(const ImageView& img, const OriginalView& orig, 
     }
   }
   float acc[4] = {0.f, 0.f, 0.f, 0.f};  // sum q, sum q^2, sum w q, out-of-image flag
+  if (samples_inside(L, orig, hmin, hmax, wmin, wmax)) {
+    // every sample and its 2x2 neighbourhood is inside: no tests, 32-bit offsets
+    const float* base = img.v + (size_t(L.R0) * img.w + L.C0);
+    const int w = img.w;
+    for (int s = threadIdx.x; s < orig.n; s += blockDim.x) {
+      const float4 p = __ldg(orig.dcw + s);
+      const float y = L.fr + (L.ca * p.x - L.sa * p.y), x = L.fc + (L.sa * p.x + L.ca * p.y);
+      const int iy = __float2int_rd(y), ix = __float2int_rd(x);
+      const float fy = y - float(iy), fx = x - float(ix);
+      const float* v = base + (iy * w + ix);
+      const float q = (1 - fy) * ((1 - fx) * __ldg(v) + fx * __ldg(v + 1)) +
+                      fy * ((1 - fx) * __ldg(v + w) + fx * __ldg(v + w + 1)) - offset;
+      acc[0] += q;
+      acc[1] = fmaf(q, q, acc[1]);
+      acc[2] = fmaf(p.z, q, acc[2]);
+    }
+  } else
   for (int s = threadIdx.x; s < orig.n; s += blockDim.x) {
     const float dr = __ldg(orig.dr + s), dc = __ldg(orig.dc + s), w = __ldg(orig.w + s);
     const float y = L.fr + (L.ca * dr - L.sa * dc), x = L.fc + (L.sa * dr + L.ca * dc);
@@ -1056,16 +1139,19 @@ __device__ void gn_pass(const ImageView& img, const OriginalView& orig, double r
   float acc[19];
 #pragma unroll
   for (int k = 0; k < 19; ++k) acc[k] = 0.f;
+  const bool inside = samples_inside(L, orig, hmin, hmax, wmin, wmax);
+  const float* base = img.v + (size_t(L.R0) * img.w + L.C0);
   for (int s = threadIdx.x; s < orig.n; s += blockDim.x) {
-    const float dr = __ldg(orig.dr + s), dc = __ldg(orig.dc + s), w = __ldg(orig.w + s);
+    const float4 p = __ldg(orig.dcw + s);
+    const float dr = p.x, dc = p.y, w = p.z;
     const float y = L.fr + (L.ca * dr - L.sa * dc), x = L.fc + (L.sa * dr + L.ca * dc);
-    if (!(y >= hmin && x >= wmin && y < hmax && x < wmax)) {
+    if (!inside && !(y >= hmin && x >= wmin && y < hmax && x < wmax)) {
       acc[18] = 1.f;
       continue;
     }
-    const float fy0 = floorf(y), fx0 = floorf(x);
-    const float fy = y - fy0, fx = x - fx0;
-    const float* v = img.v + size_t(L.R0 + int(fy0)) * img.w + (L.C0 + int(fx0));
+    const int iy = __float2int_rd(y), ix = __float2int_rd(x);
+    const float fy = y - float(iy), fx = x - float(ix);
+    const float* v = base + (iy * img.w + ix);
     const float va = __ldg(v), vb = __ldg(v + 1), vd = __ldg(v + img.w), ve = __ldg(v + img.w + 1);
     const float q = (1 - fy) * ((1 - fx) * va + fx * vb) + fy * ((1 - fx) * vd + fx * ve) - offset;
     const float gy = (1 - fx) * (vd - va) + fx * (ve - vb), gx = (1 - fy) * (vb - va) + fy * (ve - vd);
@@ -1509,11 +1595,21 @@ cudaError_t launch_track(const TrackArgs& a, int max_candidates, cudaStream_t s,
   TrackArgs b = a;
   size_t smem = size_t(a.view.lin_pitch) * size_t(a.view.lin_rows) * sizeof(float);
   const size_t fixed = 8 * 1024;  // static shared memory of the kernel
-  if (smem + fixed > smem_limit || smem > 160 * 1024) {
+  const size_t scratch = a.tc_dots ? 2 * kTrackThreads * sizeof(long long) : 0;
+  if (smem + scratch + fixed > smem_limit || smem > 160 * 1024) {
     b.staged_ok = 0;
     smem = 0;
   } else {
     b.staged_ok = 1;
+  }
+  // tensor-core items leave the sample slices idle: they split the runs
+  // instead, through a scratch after the window
+  if (scratch) {
+    smem = (smem + 15) & ~size_t(15);  // 8-byte entries: start on a 16-byte boundary
+    b.split_off = int(smem / sizeof(float));
+    smem += scratch;
+  } else {
+    b.split_off = -1;
   }
   if (const cudaError_t e = reserve_dynamic_smem(reinterpret_cast<const void*>(track_kernel), smem)) return e;
   track_kernel<<<max_candidates, kTrackThreads, smem, s>>>(b);

@@ -13,8 +13,11 @@ namespace mvg {
 struct LevelImage {
   float* v = nullptr;
   int w = 0, h = 0;
-  // row prefix moments of the level: (w+1) x h pairs {sum S, sum S^2}
+  // row prefix moments of the level: (w+1) x h pairs {sum S, sum S^2}, as
+  // int64 (prefix) or, when every run sum of S^2 is below 2^32, as uint32
+  // modulo 2^32 (prefix32; differences of two entries are then exact)
   longlong2* prefix = nullptr;
+  uint2* prefix32 = nullptr;
 };
 
 // Valid-position interval of a patch on a level: the intersection of the
@@ -63,6 +66,8 @@ struct TrackArgs {
   int exact32;              // lattice arithmetic is exact in FP32 (host-checked)
   int absolute;
   int staged_ok;            // set by the launcher: dynamic shared memory holds the window
+  int split_off;            // set by the launcher: float offset of the moment-split scratch in
+                            // dynamic shared memory (-1: no scratch, moments in one slice)
   // sum w (S - S0) of the rotated patches of tensor-core groups (nullable),
   // kTcScoreStride per candidate
   const float* tc_dots;

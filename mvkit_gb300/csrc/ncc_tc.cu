@@ -161,8 +161,23 @@ __device__ __forceinline__ void tc_fail(const TcArgs& a, TcShared& sh) {
 // MMA issue (one thread): per slab, wait for the windows, then per grid row
 // wait for its weights, issue K/16 MMAs into accumulator set y mod sets and
 // release the weight buffer; release the window buffer after the slab.
+// Position in the weight ring: buffer index and phase parity of chunk count,
+// advanced incrementally (no division on the issue path).
+struct RingPos {
+  long long count = 0;
+  int stage = 0;
+  uint32_t phase = 0;
+  __device__ void advance(int stages) {
+    ++count;
+    if (++stage == stages) {
+      stage = 0;
+      phase ^= 1u;
+    }
+  }
+};
+
 __device__ void tc_mma_role(const TcArgs& a, TcShared& sh, uint8_t* wbase, uint8_t* abase, uint32_t tmem,
-                            long long& cm, int& sm) {
+                            RingPos& cm, int& sm) {
   const TcGroup& G = sh.grp;
   const TcShape sp(G);
   const int S = a.stages;
@@ -181,24 +196,26 @@ __device__ void tc_mma_role(const TcArgs& a, TcShared& sh, uint8_t* wbase, uint8
     const uint64_t b_stage = uint64_t(a.stage_bytes) >> 4;
     const int y0 = sl * sp.Y, y1 = min(G.kr, y0 + sp.Y);
     int set = y0 % a.sets;
+    uint32_t d = tmem + uint32_t(set * a.npad);
+    const uint32_t d_end = tmem + uint32_t(a.sets * a.npad);
     for (int y = y0; y < y1; ++y) {
-      const int st = int(cm % S);
-      if (!bar_wait(&sh.b_full[st], uint32_t((cm / S) & 1))) {
+      if (!bar_wait(&sh.b_full[cm.stage], cm.phase)) {
         tc_fail(a, sh);
         return;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      uint64_t ad = a_desc0 + uint64_t(y - y0), bd = b_desc0 + uint64_t(st) * b_stage;
-      const uint32_t d = tmem + uint32_t(set * a.npad);
+      uint64_t ad = a_desc0 + uint64_t(y - y0), bd = b_desc0 + uint64_t(cm.stage) * b_stage;
       mma_f16(d, ad, bd, idesc, y >= a.sets ? 1u : 0u);
+#pragma unroll 4
       for (int j = 1; j < sp.ksteps; ++j) {
         ad += a_kstep;
         bd += 16;
         mma_f16(d, ad, bd, idesc, 1u);
       }
-      mma_commit(&sh.b_empty[st]);
-      ++cm;
-      if (++set == a.sets) set = 0;
+      mma_commit(&sh.b_empty[cm.stage]);
+      cm.advance(S);
+      d += uint32_t(a.npad);
+      if (d == d_end) d = tmem;
     }
     mma_commit(&sh.slab_done[buf]);
     ++sm;
@@ -217,8 +234,8 @@ __device__ void tc_window_role(const TcArgs& a, TcShared& sh, uint8_t* abase, in
   const int cnt = sh.cnt, rows = G.rows_slab, H = a.lev.h, pitch = a.plane_pitch;
   const size_t plane = size_t(H) * size_t(pitch);
   const int lane = pt & 31, wp = pt >> 5;
-  const int rblocks = rows / 8, sblocks = (sp.nplane + 3) / 4;
-  const int items = cnt * rblocks * sblocks;  // one per warp-iteration
+  const int rblocks = rows / 8;
+  const size_t part_stride = size_t(kTcPlaneShifts) * plane;  // high plane -> low plane
   for (int sl = 0; sl < sp.nslabs; ++sl) {
     const int buf = sa & 1;
     if (sa >= 2 && !bar_wait(&sh.slab_done[buf], uint32_t(((sa >> 1) - 1) & 1))) {
@@ -227,17 +244,24 @@ __device__ void tc_window_role(const TcArgs& a, TcShared& sh, uint8_t* abase, in
     }
     uint8_t* dst0 = abase + size_t(buf) * a.abuf_bytes;
     const int y0 = sl * sp.Y;
-    for (int it = wp; it < items; it += kTcWindowThreads / 32) {
-      const int g = it / (rblocks * sblocks), rem = it % (rblocks * sblocks);
-      const int r = (rem / sblocks) * 8 + (lane & 7), sg = (rem % sblocks) * 4 + (lane >> 3);
-      if (sg >= sp.nplane) continue;
-      const int q = sg / sp.segs, s = sg % sp.segs;
-      const int row = sh.R[g] - 2 + G.rmin + y0 + r;
-      const int x = sh.x0a[g] + kTcPlaneMargin + 8 * s;
-      const bool valid = row >= 0 && row < H && x >= 0 && x + 8 <= pitch;
-      const uint16_t* src =
-          a.planes + size_t(q * kTcPlaneShifts + sh.delta[g]) * plane + (valid ? size_t(row) * pitch + x : 0);
-      cp_async16(dst0 + size_t(g) * sp.sbo + size_t(sg) * sp.lbo + size_t(r) * 16, src, valid);
+    // warp wp stages candidates wp, wp + 4, ...; lane = (row in an 8-row block,
+    // segment in a 4-segment block)
+    for (int g = wp; g < cnt; g += kTcWindowThreads / 32) {
+      const int row0 = sh.R[g] - 2 + G.rmin + y0 + (lane & 7);
+      const int x0 = sh.x0a[g] + kTcPlaneMargin;
+      const uint16_t* pbase = a.planes + size_t(sh.delta[g]) * plane;
+      uint8_t* dg = dst0 + size_t(g) * sp.sbo + size_t(lane & 7) * 16;
+      for (int rb = 0; rb < rblocks; ++rb) {
+        const int row = row0 + rb * 8;
+        const bool rok = row >= 0 && row < H;
+        for (int sg = lane >> 3; sg < sp.nplane; sg += 4) {
+          const int q = sg >= sp.segs ? 1 : 0;
+          const int x = x0 + 8 * (sg - q * sp.segs);
+          const bool valid = rok && x >= 0 && x + 8 <= pitch;
+          const uint16_t* src = pbase + (q ? part_stride : 0) + (valid ? size_t(row) * pitch + x : 0);
+          cp_async16(dg + size_t(sg) * sp.lbo + size_t(rb) * 128, src, valid);
+        }
+      }
     }
     asm volatile("cp.async.commit_group;\n cp.async.wait_group 0;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -248,19 +272,21 @@ __device__ void tc_window_role(const TcArgs& a, TcShared& sh, uint8_t* abase, in
 
 // Weight producer (one thread): the tile's grid-row chunks through the ring,
 // as far ahead as the ring allows.
-__device__ void tc_weight_role(const TcArgs& a, TcShared& sh, uint8_t* wbase, long long& cb) {
+__device__ void tc_weight_role(const TcArgs& a, TcShared& sh, uint8_t* wbase, RingPos& cb) {
   const TcGroup& G = sh.grp;
   const TcShape sp(G);
   const int S = a.stages;
+  const uint8_t* src = G.b;
   for (int i = 0; i < G.kr; ++i) {
-    const int st = int(cb % S);
-    if (cb >= S && !bar_wait(&sh.b_empty[st], uint32_t(((cb / S) - 1) & 1))) {
+    // the buffer's previous chunk (count - S) has been consumed
+    if (cb.count >= S && !bar_wait(&sh.b_empty[cb.stage], cb.phase ^ 1u)) {
       tc_fail(a, sh);
       return;
     }
-    expect_tx(&sh.b_full[st], sp.bchunk);
-    bulk_load(wbase + size_t(st) * a.stage_bytes, G.b + size_t(i) * sp.bchunk, sp.bchunk, &sh.b_full[st]);
-    ++cb;
+    expect_tx(&sh.b_full[cb.stage], sp.bchunk);
+    bulk_load(wbase + size_t(cb.stage) * a.stage_bytes, src, sp.bchunk, &sh.b_full[cb.stage]);
+    src += sp.bchunk;
+    cb.advance(S);
   }
 }
 
@@ -302,7 +328,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = sh.tmem;
-  long long cm = 0, cb = 0;  // role-local counters (MMA thread, weight producer)
+  RingPos cm, cb;            // role-local ring positions (MMA thread, weight producer)
   int sm = 0, sa = 0;        // role-local counters (MMA thread, window producer)
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     // tile set-up: the group into shared memory, one candidate per thread
@@ -366,14 +392,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     if (warp == 0) {
       if (lane == 0) {
         tc_mma_role(a, sh, wbase, abase, tmem, cm, sm);
-        sh.cm = cm;
+        sh.cm = cm.count;
         sh.sm = sm;
       }
       __syncwarp();
     } else if (warp == 1) {
       if (lane == 0) {
         tc_weight_role(a, sh, wbase, cb);
-        sh.cb = cb;
+        sh.cb = cb.count;
       }
       __syncwarp();
     } else {

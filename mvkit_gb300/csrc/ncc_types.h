@@ -57,6 +57,8 @@ struct OriginalView {
   const float* dr;              // sample row - level origin row
   const float* dc;              // sample column - level origin column
   const float* w;
+  const float4* dcw;            // the same samples packed {dr, dc, w, 0}
+  float dr_min, dr_max, dc_min, dc_max;  // sample offset box
   int32_t n;
 };
 
