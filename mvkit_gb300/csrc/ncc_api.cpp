@@ -355,7 +355,7 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
   struct Proto {
     std::vector<int32_t> ks, descs;
     int rmin = INT32_MAX, rmax = INT32_MIN, cmin = INT32_MAX, cmax = INT32_MIN;
-    int kr = 0, kw = 0, n = 0;
+    int kr = 0, kw = 0, rg = 1, n = 0;
   };
   std::vector<Proto> protos;
   std::map<std::vector<int32_t>, int> by_key;
@@ -384,7 +384,12 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
     }
     pr.kr = pr.rmax - pr.rmin + 1;
     pr.kw = (pr.cmax - pr.cmin + 1 + 4 + 15) / 16 * 16;
-    pr.n = (10 * int(pr.descs.size()) + 15) / 16 * 16;
+    // grid rows per chunk: as many as keep N <= 256 (and <= 4, so that
+    // placement row + chunk row stays within the 8 rows of a candidate)
+    const int P = int(pr.descs.size());
+    pr.rg = 4;
+    while (pr.rg > 1 && (10 * P * pr.rg + 15) / 16 * 16 > 256) --pr.rg;
+    pr.n = (10 * P * pr.rg + 15) / 16 * 16;
     by_key[key] = int(protos.size());
     plan->group_of_src[src] = int(protos.size());
     protos.push_back(std::move(pr));
@@ -395,7 +400,9 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
   size_t max_chunk = 0;
   int max_kr = 0;
   int max_n = 0;
+  int min_rg = 4;
   for (const Proto& pr : protos) {
+    min_rg = std::min(min_rg, pr.rg);
     max_chunk = std::max(max_chunk, size_t(pr.n) * size_t(parts * pr.kw + 16) * 2);
     max_kr = std::max(max_kr, pr.kr);
     max_n = std::max(max_n, pr.n);
@@ -403,8 +410,8 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
   plan->npad = (max_n + 31) / 32 * 32;
   plan->sets = std::max(1, std::min(4, 512 / plan->npad));
   // shared memory: weight ring | two window buffers (rows_slab rows each).
-  // The ring covers the L2 latency (about ten grid rows of MMAs ahead); the
-  // window buffers take the rest, at least 16 rows each.
+  // The ring holds about eight grid rows of weights ahead of the MMAs (the L2
+  // latency); the window buffers take the rest, at least 16 rows each.
   int max_nseg = 0;
   for (const Proto& pr : protos) max_nseg = std::max(max_nseg, parts * pr.kw / 8 + 2);
   const size_t per_row = size_t(kTcCands) * size_t(max_nseg) * 16;
@@ -413,7 +420,8 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
     plan->group_of_src.assign(nsrc, -1);
     return plan;
   }
-  const int stages = int(std::min<size_t>({size_t(kTcMaxStages), size_t(10), (budget - min_windows) / max_chunk}));
+  const int stages = int(std::min<size_t>({size_t(kTcMaxStages), size_t(std::max(2, (8 + min_rg - 1) / min_rg)),
+                                           (budget - min_windows) / max_chunk}));
   const size_t ring = size_t(stages) * max_chunk + 1024;
   const int rows = std::min(std::min(256, (max_kr + 7 + 7) / 8 * 8), int((budget - ring) / 2 / per_row) / 8 * 8);
   plan->stages = stages;
@@ -440,7 +448,8 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
     const double m64 = parts == 2 ? 64.0 : 1.0;
     const double limit = std::min(maxw > 0 ? 16384.0 / (maxw * m64) : 1e30, maxrow > 0 ? 16384.0 / (maxrow * m64) : 1e30);
     const double sigma = limit < 1e30 ? std::ldexp(1., int(std::floor(std::log2(limit)))) : 1.0;
-    std::vector<uint16_t> host(size_t(pr.kr) * chunk_elems, 0);
+    const int rg = pr.rg, chunks = (pr.kr + rg - 1) / rg;
+    std::vector<uint16_t> host(size_t(chunks) * chunk_elems, 0);
     TcGroup g{};
     g.kr = pr.kr;
     g.kw = pr.kw;
@@ -448,13 +457,17 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
     g.rmin = pr.rmin;
     g.cmin = pr.cmin;
     g.p = P;
+    g.rg = rg;
     g.n = N;
     g.rows_slab = rows;
     g.inv_scale = float(1.0 / sigma);
     g.macs = 0;
-    auto at = [&](size_t y, int n, int k) {
-      return y * chunk_elems + size_t(n / 8) * size_t(K / 8) * 64 + size_t(k / 8) * 64 + size_t(n % 8) * 8 +
-             size_t(k % 8);
+    // element of grid row y, column (patch q, placement dc, half), K index k:
+    // chunk y / rg, N column ((y mod rg) P + q) 5 + dc) 2 + half
+    auto at = [&](size_t y, int q, int dc, int half, int k) {
+      const int n = ((int(y % size_t(rg)) * P + q) * 5 + dc) * 2 + half;
+      return (y / size_t(rg)) * chunk_elems + size_t(n / 8) * size_t(K / 8) * 64 + size_t(k / 8) * 64 +
+             size_t(n % 8) * 8 + size_t(k % 8);
     };
     for (int q = 0; q < P; ++q) {
       const PatchDesc& d = T.desc[size_t(pr.descs[size_t(q)])];
@@ -478,7 +491,7 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
             const double mult = (parts == 2 && part == 0) ? 64.0 : 1.0;
             const int k = part * pr.kw + x;
             for (int half = 0; half < 2; ++half)
-              host[at(y, (q * 5 + dc) * 2 + half, k)] = half_bits((half ? lv : hv) * mult);
+              host[at(y, q, dc, half, k)] = half_bits((half ? lv : hv) * mult);
           }
         }
       }
@@ -492,15 +505,14 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
           const uint16_t f2 = half_bits(r - half_value(f1));
           ecorr += half_value(f1) + half_value(f2);
           for (int dc = 0; dc < 5; ++dc) {
-            const int n = (q * 5 + dc) * 2 + half;
             if (parts == 2) {
-              host[at(y, n, kc0)] = half_bits(64.0 * half_value(f1));
-              host[at(y, n, kc0 + 1)] = half_bits(64.0 * half_value(f2));
-              host[at(y, n, kc0 + 2)] = f1;
-              host[at(y, n, kc0 + 3)] = f2;
+              host[at(y, q, dc, half, kc0)] = half_bits(64.0 * half_value(f1));
+              host[at(y, q, dc, half, kc0 + 1)] = half_bits(64.0 * half_value(f2));
+              host[at(y, q, dc, half, kc0 + 2)] = f1;
+              host[at(y, q, dc, half, kc0 + 3)] = f2;
             } else {
-              host[at(y, n, kc0)] = f1;
-              host[at(y, n, kc0 + 1)] = f2;
+              host[at(y, q, dc, half, kc0)] = f1;
+              host[at(y, q, dc, half, kc0 + 1)] = f2;
             }
           }
         }

@@ -80,9 +80,9 @@ cudaError_t reserve_dynamic_smem(const void* kernel, size_t bytes);
 
 // Tensor-core tracking (ncc_tc.cu).  A tile is up to 16 candidates of one
 // group (candidates found with the same source patch search the same target
-// patches); MMA rows are (candidate, row placement), MMA columns (patch,
-// column placement, weight half); K runs over the window columns of one
-// grid row, and the grid rows accumulate in tensor memory.
+// patches); MMA rows are (candidate, window row offset), MMA columns (grid
+// row in the chunk, patch, column placement, weight half); K runs over the
+// window columns, and the chunks of grid rows accumulate in tensor memory.
 constexpr int kTcMaxP = 16;              // patches of one group (N = 10 P <= 160)
 constexpr int kTcCands = 16;             // candidates per tile (M = 16 x 8 rows)
 constexpr int kTcScoreStride = 16 * 25;  // dots per candidate: [selected patch][placement]
@@ -93,12 +93,13 @@ constexpr int kTcPlaneShifts = 8;        // column-shifted copies of a level pla
 constexpr int kTcPlaneMargin = 8;        // plane columns left of the level
 
 struct TcGroup {
-  const uint8_t* b;                      // kr chunks: N x (parts kw) fp16 weights, canonical K-major
+  const uint8_t* b;                      // ceil(kr / rg) chunks: N x K fp16 weights, canonical K-major
   long long macs;                        // algorithmic MACs per candidate (25 x samples of all patches)
   int kr, kw;                            // grid rows; window columns per part (multiple of 16)
   int parts;                             // planes per value: 1, or 2 (64 x high part, low part)
   int rmin, cmin;                        // grid origin relative to the placement centre
-  int p, n;                              // patches; MMA N (10 p rounded up to 16)
+  int p, rg, n;                          // patches; grid rows per chunk (N columns side by side);
+                                         // MMA N (10 p rg rounded up to 16)
   int rows_slab;                         // window rows per staged slab (multiple of 8, >= 16)
   float inv_scale;                       // 1 / weight scale
   int k_of[kTcMaxP];                     // index in the candidate's selected list

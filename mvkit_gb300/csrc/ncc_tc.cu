@@ -4,16 +4,20 @@
 // found with: all candidates of a group search the same target patches (the
 // reference's angle window, src/ncc_matching/matcher.cpp:680-697), so the
 // group shares one weight matrix per grid row.  A tile is up to 16
-// candidates of a group and one MMA computes, for one grid row y of the
-// patches' union grid,
+// candidates of a group and one MMA computes, for a chunk of rg grid rows
+// y .. y + rg - 1 of the patches' union grid (k < rg),
 //
-//   D[(candidate g, row placement dr)][(patch p, column placement dc, half)]
-//     += sum_x window_g(y + dr, x) * w_{p,half}(y, x - dc)
+//   D[(candidate g, row m)][(k, patch p, column placement dc, half)]
+//     += sum_x window_g(y + m, x) * w_{p,half}(y + k, x - dc)
 //
-// with M = 16 x 8 rows (dr = 0..4 used), N = 10 P, K = the window columns
+// Window row y + m is placement m at grid row y and placement m - k at grid
+// row y + k, so the dot product of placement dr is the sum over k of
+// D_k[(g, dr + k)] (dr + k <= 7 for dr < 5, rg <= 4).  One window tile thus
+// serves rg grid rows: the MMAs are bound by fetching that tile, so rg
+// divides their count.  M = 16 x 8 rows, N = 10 P rg, K = the window columns
 // plus one 16-column step that subtracts the candidate's centre value times
 // the row sum of each weight column (centred accumulation, as the CUDA-core
-// path's window centring).  Grid rows accumulate round-robin into up to four
+// path's window centring).  Chunks accumulate round-robin into up to four
 // accumulator sets in tensor memory, summed in FP32 by the epilogue.
 // Windows come straight from fp16 copies of the level ("planes", exact
 // integers: the level minus a constant, split into a high and a low plane
@@ -137,7 +141,7 @@ struct __align__(16) TcShared {
 
 // Shape of one tile's operands.
 struct TcShape {
-  int segs, nplane, nseg, K, ksteps, Y, nslabs;
+  int segs, nplane, nseg, K, ksteps, Y, nslabs, chunks;
   uint32_t lbo, sbo, bchunk;
   __device__ explicit TcShape(const TcGroup& G) {
     segs = G.kw / 8;
@@ -145,8 +149,9 @@ struct TcShape {
     nseg = nplane + 2;
     K = 8 * nseg;
     ksteps = K / 16;
-    Y = G.rows_slab - 7;  // grid rows per window slab
+    Y = (G.rows_slab - 7) / G.rg * G.rg;  // grid rows per window slab (whole chunks)
     nslabs = (G.kr + Y - 1) / Y;
+    chunks = (G.kr + G.rg - 1) / G.rg;
     lbo = uint32_t(G.rows_slab) * 16;
     sbo = uint32_t(nseg) * lbo;
     bchunk = uint32_t(G.n) * uint32_t(K) * 2;
@@ -195,17 +200,17 @@ __device__ void tc_mma_role(const TcArgs& a, TcShared& sh, uint8_t* wbase, uint8
     const uint64_t b_desc0 = smem_desc(smem_u32(wbase), 128, uint32_t(sp.K / 8) * 128);
     const uint64_t b_stage = uint64_t(a.stage_bytes) >> 4;
     const int y0 = sl * sp.Y, y1 = min(G.kr, y0 + sp.Y);
-    int set = y0 % a.sets;
-    uint32_t d = tmem + uint32_t(set * a.npad);
+    int chunk = y0 / G.rg;
+    uint32_t d = tmem + uint32_t((chunk % a.sets) * a.npad);
     const uint32_t d_end = tmem + uint32_t(a.sets * a.npad);
-    for (int y = y0; y < y1; ++y) {
+    for (int y = y0; y < y1; y += G.rg, ++chunk) {
       if (!bar_wait(&sh.b_full[cm.stage], cm.phase)) {
         tc_fail(a, sh);
         return;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       uint64_t ad = a_desc0 + uint64_t(y - y0), bd = b_desc0 + uint64_t(cm.stage) * b_stage;
-      mma_f16(d, ad, bd, idesc, y >= a.sets ? 1u : 0u);
+      mma_f16(d, ad, bd, idesc, chunk >= a.sets ? 1u : 0u);
 #pragma unroll 4
       for (int j = 1; j < sp.ksteps; ++j) {
         ad += a_kstep;
@@ -277,7 +282,7 @@ __device__ void tc_weight_role(const TcArgs& a, TcShared& sh, uint8_t* wbase, Ri
   const TcShape sp(G);
   const int S = a.stages;
   const uint8_t* src = G.b;
-  for (int i = 0; i < G.kr; ++i) {
+  for (int i = 0; i < sp.chunks; ++i) {
     // the buffer's previous chunk (count - S) has been consumed
     if (cb.count >= S && !bar_wait(&sh.b_empty[cb.stage], cb.phase ^ 1u)) {
       tc_fail(a, sh);
@@ -429,7 +434,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     // accumulators -> shared memory (row t; the operand buffers are free now)
     float* D = reinterpret_cast<float*>(smem);
     const int ld = G.n + 1;
-    const int nsets = min(a.sets, G.kr);
+    const int nsets = min(a.sets, (G.kr + G.rg - 1) / G.rg);
     if (warp < 4)  // warp w reads tensor-memory lanes 32w..32w+31
       for (int c0 = 0; c0 < G.n; c0 += 32) {
         float acc[32];
@@ -456,11 +461,21 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       float* out = a.dots + size_t(ci) * kTcScoreStride + size_t(G.k_of[q]) * 25 + dr * 5;
       const int sr = min(max(R + dr - 2 + G.r0[q], 0), H - 1);
       const float* srow = a.lev.v + size_t(sr) * W;
+      // first samples of the five placements, loaded before any store
+      float s0v[5];
+#pragma unroll
+      for (int dc = 0; dc < 5; ++dc) s0v[dc] = __ldg(srow + min(max(C + dc - 2 + G.c0[q], 0), W - 1));
+#pragma unroll
       for (int dc = 0; dc < 5; ++dc) {
-        const int n0 = (q * 5 + dc) * 2;
-        // sum w (S - c) with c the centre, as accumulated
-        const float raw = (D[m * ld + n0] + D[m * ld + n0 + 1]) * G.inv_scale;
-        const float s0 = srow[min(max(C + dc - 2 + G.c0[q], 0), W - 1)] - a.plane_offset;
+        // sum w (S - c) with c the centre, as accumulated: accumulator row
+        // m + k of grid-row slot k holds this placement's grid rows y + k
+        float sum = 0.f;
+        for (int k = 0; k < G.rg; ++k) {
+          const int n0 = ((k * G.p + q) * 5 + dc) * 2;
+          sum += D[(m + k) * ld + n0] + D[(m + k) * ld + n0 + 1];
+        }
+        const float raw = sum * G.inv_scale;
+        const float s0 = s0v[dc] - a.plane_offset;
         // sum w (S - S0) = raw + c (ecorr - weff) + (c - S0) weff: ecorr is
         // the row-sum total as subtracted, weff the weights' sum
         out[dc] = raw + (cen * (G.ecorr[q] - G.weff[q]) + (cen - s0) * G.weff[q]);
@@ -468,7 +483,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     if (t == 0) {
       atomicAdd(&a.state_rw->tc_macs, (unsigned long long)G.macs * (unsigned long long)sh.cnt);
-      atomicAdd(&a.state_rw->tc_issued, (unsigned long long)kTcRows * G.n * (G.parts * G.kw + 16) * G.kr);
+      atomicAdd(&a.state_rw->tc_issued,
+                (unsigned long long)kTcRows * G.n * (G.parts * G.kw + 16) * ((G.kr + G.rg - 1) / G.rg));
     }
     // generic accesses of the buffers before the next tile's async writes
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
