@@ -311,50 +311,77 @@ __global__ void __launch_bounds__(kTrackThreads, 5) track_kernel(TrackArgs a) {
   __shared__ int s_word[kTrackThreads / 32];
   const Cand cd = a.in[i];
   const int WW = a.view.lin_pitch;
+  __shared__ int s_b, s_tc, s_bound[2][4];
+  __shared__ float s_xr32, s_xc32;
+  __shared__ double s_xr, s_xc;
   if (threadIdx.x == 0) {
     const int src = cd.patch;
     const int b = src >= 0 ? a.sel_off[src] : 0, e = src >= 0 ? a.sel_off[src + 1] : 0;
-    const int n = min(e - b, kTrackMaxSel);
+    s_b = b;
+    s_n = min(e - b, kTrackMaxSel);
     // rotated patches of a tensor-core group were scored by tc_track_kernel
-    const bool tc = a.tc_dots && src >= 0 && a.tc_group_of_src[src] >= 0;
-    int wr0 = INT32_MAX, wc0 = INT32_MAX, wr1 = INT32_MIN, wc1 = INT32_MIN;
+    s_tc = a.tc_dots && src >= 0 && a.tc_group_of_src[src] >= 0;
     // window centres: round((pose - crop - offset) / step - origin)
-    double xr = 0, xc = 0;
-    float xr32 = 0, xc32 = 0;
     if (a.exact32) {
-      xr32 = __fmul_rn(__fsub_rn(__fsub_rn(float(cd.row), float(a.crop_row)), float(a.offset)), float(1.0 / a.step));
-      xc32 = __fmul_rn(__fsub_rn(__fsub_rn(float(cd.col), float(a.crop_col)), float(a.offset)), float(1.0 / a.step));
+      s_xr32 = __fmul_rn(__fsub_rn(__fsub_rn(float(cd.row), float(a.crop_row)), float(a.offset)), float(1.0 / a.step));
+      s_xc32 = __fmul_rn(__fsub_rn(__fsub_rn(float(cd.col), float(a.crop_col)), float(a.offset)), float(1.0 / a.step));
     } else {
-      xr = dsub(dsub(cd.row, a.crop_row), a.offset) / a.step;
-      xc = dsub(dsub(cd.col, a.crop_col), a.offset) / a.step;
+      s_xr = dsub(dsub(cd.row, a.crop_row), a.offset) / a.step;
+      s_xc = dsub(dsub(cd.col, a.crop_col), a.offset) / a.step;
     }
-    for (int k = 0; k < n; ++k) {
-      const int j = a.sel_idx[b + k];
+  }
+  __syncthreads();
+  {
+    // one thread per selected patch (at most 64: warps 0 and 1)
+    int wr0 = INT32_MAX, wc0 = INT32_MAX, wr1 = INT32_MIN, wc1 = INT32_MIN;
+    const int k = threadIdx.x;
+    if (k < s_n) {
+      const int j = a.sel_idx[s_b + k];
       s_sel[k] = j;
       const PatchDesc pd = a.view.patches[a.plist[j]];
       int row, col;
       if (a.exact32) {
-        row = int(roundf(__fsub_rn(xr32, float(pd.orow))));
-        col = int(roundf(__fsub_rn(xc32, float(pd.ocol))));
+        row = int(roundf(__fsub_rn(s_xr32, float(pd.orow))));
+        col = int(roundf(__fsub_rn(s_xc32, float(pd.ocol))));
       } else {
-        row = int(round(dsub(xr, pd.orow)));
-        col = int(round(dsub(xc, pd.ocol)));
+        row = int(round(dsub(s_xr, pd.orow)));
+        col = int(round(dsub(s_xc, pd.ocol)));
       }
       s_row[k] = row;
       s_col[k] = col;
-      s_istc[k] = tc && pd.orow == 0 && pd.ocol == 0 && k < 16;
+      const bool istc = s_tc && pd.orow == 0 && pd.ocol == 0 && k < 16;
+      s_istc[k] = istc;
       const PosRange rg = a.ranges[j];
       // only placements scored here need image data
       const int r_lo = max(row - 2, rg.r0), r_hi = min(row + 2, rg.r1 - 1);
       const int c_lo = max(col - 2, rg.c0), c_hi = min(col + 2, rg.c1 - 1);
-      if (!s_istc[k] && r_lo <= r_hi && c_lo <= c_hi) {
-        wr0 = min(wr0, r_lo + pd.rmin);
-        wr1 = max(wr1, r_hi + pd.rmax);
-        wc0 = min(wc0, c_lo + pd.cmin);
-        wc1 = max(wc1, c_hi + pd.cmax);
+      if (!istc && r_lo <= r_hi && c_lo <= c_hi) {
+        wr0 = r_lo + pd.rmin;
+        wr1 = r_hi + pd.rmax;
+        wc0 = c_lo + pd.cmin;
+        wc1 = c_hi + pd.cmax;
       }
     }
-    s_n = n;
+    if (threadIdx.x < 64) {
+      for (int o = 16; o > 0; o >>= 1) {
+        wr0 = min(wr0, __shfl_xor_sync(0xffffffffu, wr0, o));
+        wc0 = min(wc0, __shfl_xor_sync(0xffffffffu, wc0, o));
+        wr1 = max(wr1, __shfl_xor_sync(0xffffffffu, wr1, o));
+        wc1 = max(wc1, __shfl_xor_sync(0xffffffffu, wc1, o));
+      }
+      if ((threadIdx.x & 31) == 0) {
+        s_bound[threadIdx.x >> 5][0] = wr0;
+        s_bound[threadIdx.x >> 5][1] = wr1;
+        s_bound[threadIdx.x >> 5][2] = wc0;
+        s_bound[threadIdx.x >> 5][3] = wc1;
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int n = s_n;
+    const int wr0 = min(s_bound[0][0], s_bound[1][0]), wr1 = max(s_bound[0][1], s_bound[1][1]);
+    const int wc0 = min(s_bound[0][2], s_bound[1][2]), wc1 = max(s_bound[0][3], s_bound[1][3]);
     const int items = n * 25;
     s_split = items > 0 ? max(1, min(8, kTrackThreads / items)) : 1;
     const bool any = wr0 <= wr1;
