@@ -551,7 +551,10 @@ struct Workspace {
   DevBuf<Refined> refined;
   DevBuf<int32_t> refined_flag, batch;
   DevBuf<QueryState> state;
-  DevBuf<float> tc_dots;
+  DevBuf<float> tc_dots, coarse_dots;
+  DevBuf<Cand> coarse_cand;
+  DevBuf<int2> coarse_rc;
+  DevBuf<uint32_t> pairs;            // fp16 pairs of the finest level
   DevBuf<uint16_t> tc_planes;
   DevBuf<int32_t> tc_order, tc_counts, tc_offsets, tc_cursor;
   DevBuf<TcTiles> tc_tiles;
@@ -871,6 +874,62 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
       if (!it->second->groups.empty()) tc[t] = it->second;
     }
   }
+  // tensor-core coarse scan: the kept coarse patches with their origin on the
+  // lattice, 16 per virtual source; a lattice of pseudo-candidates at stride
+  // 5 covers every top-level position (the rest stays on coarse_kernel)
+  std::shared_ptr<const TcPlan> tc_coarse;
+  std::vector<int32_t> vsel_off, vsel_idx;
+  std::vector<uint8_t> coarse_skip(plan[top].plist.size(), 0);
+  std::vector<int32_t> co_src(plan[top].plist.size(), -1), co_k(plan[top].plist.size(), 0);
+  const int lat_r = (lh[top] + 4) / 5, lat_c = (lw[top] + 4) / 5;
+  int coarse_nsrc = 0;
+  if (t_path == 0) {
+    float offset = 0;
+    const int parts = tc_parts(type, top, &offset);
+    DevLevel& T = *m.levels[top];
+    std::vector<int32_t> elig;
+    for (size_t j = 0; j < plan[top].plist.size(); ++j) {
+      const PatchDesc& d = T.desc[size_t(plan[top].plist[j])];
+      if (d.orow == 0 && d.ocol == 0) elig.push_back(int32_t(j));
+    }
+    vsel_off.push_back(0);
+    for (size_t i = 0; i < elig.size(); i += kTcMaxP) {
+      for (size_t k = i; k < std::min(elig.size(), i + kTcMaxP); ++k) vsel_idx.push_back(elig[k]);
+      vsel_off.push_back(int32_t(vsel_idx.size()));
+    }
+    const size_t nsrc = vsel_off.size() - 1;
+    const size_t ncand = nsrc * size_t(lat_r) * size_t(lat_c);
+    if (parts && nsrc > 0 && ncand / kTcCands + nsrc + 1 <= size_t(kTcMaxTiles)) {
+      LevelPlan vp;
+      vp.plist = plan[top].plist;
+      vp.sel_off = vsel_off;
+      vp.sel_idx = vsel_idx;
+      std::vector<int32_t> key{-1, int32_t(parts), int32_t(nsrc)};
+      key.insert(key.end(), vp.plist.begin(), vp.plist.end());
+      key.insert(key.end(), vsel_off.begin(), vsel_off.end());
+      key.insert(key.end(), vsel_idx.begin(), vsel_idx.end());
+      const size_t budget = ws.smem_optin - tc_kernel_static_smem() - 1024;
+      auto it = T.tc_plans.find(key);
+      if (it == T.tc_plans.end()) {
+        if (T.tc_plans.size() >= 32) T.tc_plans.clear();
+        it = T.tc_plans.emplace(std::move(key), build_tc_plan(T, nsrc, vp, parts, offset, budget)).first;
+      }
+      // every virtual source must have its group: the lattice covers them all
+      bool all = !it->second->groups.empty();
+      for (int32_t g : it->second->group_of_src) all = all && g >= 0;
+      if (all) {
+        tc_coarse = it->second;
+        coarse_nsrc = int(nsrc);
+        for (size_t v = 0; v + 1 < vsel_off.size(); ++v)
+          for (int32_t q = vsel_off[v]; q < vsel_off[v + 1]; ++q) {
+            const size_t j = size_t(vsel_idx[size_t(q)]);
+            coarse_skip[j] = 1;
+            co_src[j] = int32_t(v);
+            co_k[j] = q - vsel_off[v];
+          }
+      }
+    }
+  }
   const size_t finest_level = finest;
   const OriginalView orig = finest_level ? coarse_original(m, finest_level).view() : m.original.view();
   for (size_t li = 0; li < level_count; ++li) views[li] = m.levels[li]->view();
@@ -893,6 +952,9 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   const int32_t* d_sel_idx[kMaxLevels];
   const TcGroup* d_tc_groups[kMaxLevels];
   const int32_t* d_tc_gsrc[kMaxLevels];
+  const int32_t *d_co_src = nullptr, *d_co_k = nullptr, *d_co_gsrc = nullptr;
+  const TcGroup* d_co_groups = nullptr;
+  const uint8_t* d_co_skip = nullptr;
   {
     size_t total = 0;
     std::vector<size_t> at(4 * level_count);
@@ -913,7 +975,30 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
       tc_at[2 * li + 1] = total;
       total += tc[li] ? (tc[li]->group_of_src.size() * sizeof(int32_t) + 15) & ~size_t(15) : 0;
     }
+    // tensor-core coarse scan: virtual sources, groups, skip flags
+    size_t co_at[5] = {0, 0, 0, 0, 0};
+    if (tc_coarse) {
+      const size_t sizes[5] = {co_src.size() * sizeof(int32_t), co_k.size() * sizeof(int32_t),
+                               tc_coarse->groups.size() * sizeof(TcGroup),
+                               tc_coarse->group_of_src.size() * sizeof(int32_t), coarse_skip.size()};
+      for (int q = 0; q < 5; ++q) {
+        co_at[q] = total;
+        total += (sizes[q] + 15) & ~size_t(15);
+      }
+    }
     uint8_t* h = ws.stage_tables(std::max<size_t>(total, 16));
+    if (tc_coarse) {
+      std::memcpy(h + co_at[0], co_src.data(), co_src.size() * sizeof(int32_t));
+      std::memcpy(h + co_at[1], co_k.data(), co_k.size() * sizeof(int32_t));
+      std::memcpy(h + co_at[2], tc_coarse->groups.data(), tc_coarse->groups.size() * sizeof(TcGroup));
+      std::memcpy(h + co_at[3], tc_coarse->group_of_src.data(), tc_coarse->group_of_src.size() * sizeof(int32_t));
+      std::memcpy(h + co_at[4], coarse_skip.data(), coarse_skip.size());
+      d_co_src = reinterpret_cast<const int32_t*>(ws.tables.p + co_at[0]);
+      d_co_k = reinterpret_cast<const int32_t*>(ws.tables.p + co_at[1]);
+      d_co_groups = reinterpret_cast<const TcGroup*>(ws.tables.p + co_at[2]);
+      d_co_gsrc = reinterpret_cast<const int32_t*>(ws.tables.p + co_at[3]);
+      d_co_skip = reinterpret_cast<const uint8_t*>(ws.tables.p + co_at[4]);
+    }
     for (size_t li = 0; li < level_count; ++li) {
       std::memcpy(h + at[4 * li], plan[li].plist.data(), plan[li].plist.size() * sizeof(int32_t));
       std::memcpy(h + at[4 * li + 1], plan[li].ranges.data(), plan[li].ranges.size() * sizeof(PosRange));
@@ -973,6 +1058,70 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     max_bw = std::max(max_bw, top_desc[size_t(p)].cmax - top_desc[size_t(p)].cmin);
   }
   ws.planes.reserve(size_t(std::max(nplist, 1)) * size_t(lw[top]) * size_t(lh[top]));
+  if (tc_coarse) {
+    // tensor-core scan of the rotated coarse patches into their planes
+    const TcPlan& P = *tc_coarse;
+    const int ncand = coarse_nsrc * lat_r * lat_c;
+    const int pitch = (lw[top] + kTcPlaneMargin + 7) & ~7;
+    const int slot_c = kMaxLevels + 1;
+    ws.coarse_cand.reserve(size_t(ncand));
+    ws.coarse_rc.reserve(size_t(ncand));
+    ws.coarse_dots.reserve(size_t(ncand) * kTcScoreStride);
+    ws.tc_planes.reserve(size_t(P.parts) * kTcPlaneShifts * size_t(lh[top]) * size_t(pitch));
+    ws.tc_order.reserve(std::max(size_t(ncand), size_t(kMaxCandidates)));
+    ws.tc_tiles.reserve(1);
+    TcArgs tca{};
+    tca.lev = lev[top];
+    tca.in = ws.coarse_cand.p;
+    tca.state = st;
+    tca.state_rw = st;
+    tca.in_slot = slot_c;
+    tca.groups = d_co_groups;
+    tca.group_of_src = d_co_gsrc;
+    tca.tiles = ws.tc_tiles.p;
+    tca.order = ws.tc_order.p;
+    tca.dots = ws.coarse_dots.p;
+    tca.step = scale;
+    tca.offset = phase;
+    tca.exact32 = 0;
+    tca.stages = P.stages;
+    tca.stage_bytes = P.stage_bytes;
+    tca.abuf_bytes = P.abuf_bytes;
+    tca.sets = P.sets;
+    tca.npad = P.npad;
+    tca.plane_offset = P.offset;
+    tca.planes = ws.tc_planes.p;
+    tca.plane_pitch = pitch;
+    tca.rc = ws.coarse_rc.p;
+    tca.error = &st->error;
+    {
+      Span spp(kStTcPrep, s, 2);
+      check(launch_tc_planes(lev[top], ws.tc_planes.p, pitch, P.parts, P.offset, s), "tc planes");
+      check(launch_coarse_lattice(ws.coarse_cand.p, ws.coarse_rc.p, coarse_nsrc, lat_r, lat_c, d_co_gsrc,
+                                  ws.tc_order.p, ws.tc_tiles.p, st, slot_c, s),
+            "coarse lattice");
+    }
+    {
+      const size_t smem = std::max(P.smem, ws.smem_optin / 2 + 1024);
+      Span spt(kStTrackTc, s);
+      check(launch_tc_track(tca, smem, std::min(kTcMaxTiles, ws.sm_count), s), "tc coarse");
+    }
+    CoarseTcArgs cs;
+    cs.lev = lev[top];
+    cs.view = views[top];
+    cs.plist = d_plist[top];
+    cs.ranges = d_ranges[top];
+    cs.nplist = nplist;
+    cs.src_of = d_co_src;
+    cs.k_of = d_co_k;
+    cs.lat_r = lat_r;
+    cs.lat_c = lat_c;
+    cs.dots = ws.coarse_dots.p;
+    cs.planes = ws.planes.p;
+    cs.absolute = hm.params.ignore_polarity;
+    Span sp(kStCoarse, s);
+    check(launch_coarse_tc_score(cs, s), "coarse tc score");
+  }
   if (nplist > 0) {
     CoarseArgs ca;
     ca.lev = lev[top];
@@ -982,6 +1131,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     ca.nplist = nplist;
     ca.planes = ws.planes.p;
     ca.absolute = hm.params.ignore_polarity;
+    ca.skip = d_co_skip;
     {
       Span sp(kStCoarse, s);
       const cudaError_t e = launch_coarse(ca, max_bh, max_bw, s, ws.smem_optin);
@@ -989,6 +1139,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
       check(e, "coarse");
     }
     for (int k = 0; k < nplist; ++k) {
+      if (coarse_skip[size_t(k)]) continue;  // counted with the tensor-core work
       const PosRange& rg = plan[top].ranges[size_t(k)];
       t_prof.work[kStCoarse] += double(std::max(0, rg.r1 - rg.r0)) * double(std::max(0, rg.c1 - rg.c0)) *
                                 double(top_desc[size_t(plan[top].plist[size_t(k)])].n);
@@ -1087,6 +1238,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
         tca.plane_offset = P.offset;
         tca.planes = ws.tc_planes.p;
         tca.plane_pitch = pitch;
+        tca.rc = nullptr;
         tca.error = &st->error;
         {
           Span spp(kStTcPrep, s, 4);
@@ -1136,6 +1288,14 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   // full-resolution score (matcher.cpp:813-822) and sort (824-827)
   const double fscale = std::ldexp(1., int(finest)), fphase = (fscale - 1) * .5;
   ImageView fine{lev[finest].v, lw[finest], lh[finest]};
+  if ((type == 1 ? 65535.0 : 255.0) * std::ldexp(1., int(2 * finest)) <= 2048.0) {
+    // fp16-exact level: half2 pairs halve the bilinear loads of the
+    // continuous score and the Gauss-Newton passes
+    ws.pairs.reserve(size_t(lw[finest]) * size_t(lh[finest]));
+    Span sp(kStScore, s, 1);
+    check(launch_pairs(lev[finest].v, lw[finest], lh[finest], ws.pairs.p, s), "pairs");
+    fine.pairs = ws.pairs.p;
+  }
   {
     ScoreArgs sa;
     sa.img = fine;

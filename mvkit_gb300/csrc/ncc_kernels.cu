@@ -13,8 +13,10 @@
 // only where the reference's decisions need it: pose lattice arithmetic (or
 // an FP32 form the host proved exact), the normal-equation solve, and the
 // rectangle overlap of the MaxOverlap rule.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
@@ -202,6 +204,7 @@ constexpr int kTileW = 32, kTileH = 8;
 __global__ void __launch_bounds__(256) coarse_kernel(CoarseArgs a) {
   extern __shared__ float tile[];
   const int p = blockIdx.z;
+  if (a.skip && a.skip[p]) return;  // plane written by the tensor-core scan
   const PatchDesc pd = a.view.patches[a.plist[p]];
   const PosRange rg = a.ranges[p];
   const int R0 = blockIdx.y * kTileH, C0 = blockIdx.x * kTileW;
@@ -241,6 +244,57 @@ __global__ void __launch_bounds__(256) coarse_kernel(CoarseArgs a) {
     score = window_score(acc0 + acc1, s1, s2, pd.n, a.absolute);
   }
   a.planes[(size_t(p) * h + r) * w + c] = score;
+}
+
+// Pseudo-candidates of the tensor-core coarse scan: per virtual source, one
+// per 5x5 block of top-level positions, centred in the block; they are
+// already grouped by source, so the order is the identity and a source's
+// tiles are runs of 16 consecutive candidates.
+__global__ void coarse_lattice_kernel(Cand* cand, int2* rc, int nsrc, int nbr, int nbc, const int32_t* group_of_src,
+                                      int32_t* order, TcTiles* tiles, QueryState* state, int slot) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nb = nbr * nbc, tps = (nb + kTcCands - 1) / kTcCands;  // tiles per source
+  if (i == 0) {
+    state->count[slot] = nsrc * nb;
+    tiles->count = nsrc * tps;
+  }
+  if (i < nsrc * tps) {
+    const int src = i / tps, u = i % tps;
+    tiles->group[i] = group_of_src[src];
+    tiles->first[i] = src * nb + u * kTcCands;
+    tiles->last[i] = src * nb + min(nb, (u + 1) * kTcCands);
+  }
+  if (i >= nsrc * nb) return;
+  const int b = i % nb;
+  Cand c{};
+  c.patch = i / nb;
+  cand[i] = c;
+  order[i] = i;
+  rc[i] = make_int2(5 * (b / nbc) + 2, 5 * (b % nbc) + 2);
+}
+
+// Score planes of the patches the tensor cores correlated: one thread per
+// plane position (consecutive threads, consecutive columns: coalesced moment
+// loads); exact moments and the score as coarse_kernel computes them.
+__global__ void coarse_tc_score_kernel(CoarseTcArgs a) {
+  const int w = a.lev.w, h = a.lev.h;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)a.nplist * h * w) return;
+  const int j = int(idx / ((long long)h * w)), rem = int(idx % ((long long)h * w));
+  const int src = a.src_of[j];
+  if (src < 0) return;  // coarse_kernel's plane
+  const int r = rem / w, c = rem % w;
+  const PosRange rg = a.ranges[j];
+  float score = -INFINITY;
+  if (r >= rg.r0 && r < rg.r1 && c >= rg.c0 && c < rg.c1) {
+    const PatchDesc pd = a.view.patches[a.plist[j]];
+    const int ci = (src * a.lat_r + r / 5) * a.lat_c + c / 5;
+    const int pos = (r % 5) * 5 + c % 5;
+    long long s1, s2;
+    window_moments(a.lev, w + 1, r, c, a.view.runs + pd.run_off, a.view.runs_end + pd.run_off, pd.nruns, s1, s2);
+    score = window_score(a.dots[size_t(ci) * kTcScoreStride + a.k_of[j] * 25 + pos], s1, s2, pd.n, a.absolute);
+  }
+  a.planes[idx] = score;
 }
 
 // 3x3 local maxima >= 0.4*MinScore with the reference's tie rule, compacted
@@ -747,18 +801,50 @@ __device__ void continuous_pass(const ImageView& img, const OriginalView& orig, 
   if (samples_inside(L, orig, hmin, hmax, wmin, wmax)) {
     // every sample and its 2x2 neighbourhood is inside: no tests, 32-bit offsets
     const float* base = img.v + (size_t(L.R0) * img.w + L.C0);
+    const uint32_t* pbase = img.pairs ? img.pairs + (size_t(L.R0) * img.w + L.C0) : nullptr;
     const int w = img.w;
-    for (int s = threadIdx.x; s < orig.n; s += blockDim.x) {
-      const float4 p = __ldg(orig.dcw + s);
-      const float y = L.fr + (L.ca * p.x - L.sa * p.y), x = L.fc + (L.sa * p.x + L.ca * p.y);
-      const int iy = __float2int_rd(y), ix = __float2int_rd(x);
-      const float fy = y - float(iy), fx = x - float(ix);
-      const float* v = base + (iy * w + ix);
-      const float q = (1 - fy) * ((1 - fx) * __ldg(v) + fx * __ldg(v + 1)) +
-                      fy * ((1 - fx) * __ldg(v + w) + fx * __ldg(v + w + 1)) - offset;
-      acc[0] += q;
-      acc[1] = fmaf(q, q, acc[1]);
-      acc[2] = fmaf(p.z, q, acc[2]);
+    // four samples per step, all loads issued before the arithmetic; each
+    // thread still adds its samples in order s, s + blockDim.x, ...
+    constexpr int U = 4;
+    const int stride = blockDim.x;
+    for (int s0 = threadIdx.x; s0 < orig.n; s0 += U * stride) {
+      float4 p[U];
+      float fy[U], fx[U], va[U], vb[U], vd[U], ve[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int s = s0 + u * stride;
+        p[u] = s < orig.n ? __ldg(orig.dcw + s) : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const float y = L.fr + (L.ca * p[u].x - L.sa * p[u].y), x = L.fc + (L.sa * p[u].x + L.ca * p[u].y);
+        const int iy = __float2int_rd(y), ix = __float2int_rd(x);
+        fy[u] = y - float(iy);
+        fx[u] = x - float(ix);
+        if (pbase) {
+          const uint32_t* pp = pbase + (iy * w + ix);
+          const uint32_t aq = __ldg(pp), bq = __ldg(pp + w);
+          va[u] = __half2float(__ushort_as_half(aq & 0xffff));
+          vb[u] = __half2float(__ushort_as_half(aq >> 16));
+          vd[u] = __half2float(__ushort_as_half(bq & 0xffff));
+          ve[u] = __half2float(__ushort_as_half(bq >> 16));
+        } else {
+          const float* v = base + (iy * w + ix);
+          va[u] = __ldg(v);
+          vb[u] = __ldg(v + 1);
+          vd[u] = __ldg(v + w);
+          ve[u] = __ldg(v + w + 1);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (s0 + u * stride >= orig.n) break;
+        const float q = (1 - fy[u]) * ((1 - fx[u]) * va[u] + fx[u] * vb[u]) +
+                        fy[u] * ((1 - fx[u]) * vd[u] + fx[u] * ve[u]) - offset;
+        acc[0] += q;
+        acc[1] = fmaf(q, q, acc[1]);
+        acc[2] = fmaf(p[u].z, q, acc[2]);
+      }
     }
   } else
   for (int s = threadIdx.x; s < orig.n; s += blockDim.x) {
@@ -798,6 +884,15 @@ __global__ void __launch_bounds__(128) score_kernel(ScoreArgs a) {
 }
 
 // --------------------------------------------------------------------- sort
+// fp16 pairs (v[x], v[x+1]) of an fp16-exact level (last column repeats).
+__global__ void pairs_kernel(const float* __restrict__ v, int w, int h, uint32_t* __restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)w * h) return;
+  const int x = int(i % w);
+  const __half a = __float2half_rn(v[i]), b = __float2half_rn(v[x + 1 < w ? i + 1 : i]);
+  out[i] = uint32_t(__half_as_ushort(a)) | (uint32_t(__half_as_ushort(b)) << 16);
+}
+
 // 64-bit keys ordering scores descending (order-preserving bit transform).
 __device__ __forceinline__ unsigned long long desc_key(double s) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(s);
@@ -1178,8 +1273,21 @@ __device__ void gn_pass(const ImageView& img, const OriginalView& orig, double r
     }
     const int iy = __float2int_rd(y), ix = __float2int_rd(x);
     const float fy = y - float(iy), fx = x - float(ix);
-    const float* v = base + (iy * img.w + ix);
-    const float va = __ldg(v), vb = __ldg(v + 1), vd = __ldg(v + img.w), ve = __ldg(v + img.w + 1);
+    float va, vb, vd, ve;
+    if (inside && img.pairs) {
+      const uint32_t* pp = img.pairs + (size_t(L.R0) * img.w + L.C0) + (iy * img.w + ix);
+      const uint32_t aq = __ldg(pp), bq = __ldg(pp + img.w);
+      va = __half2float(__ushort_as_half(aq & 0xffff));
+      vb = __half2float(__ushort_as_half(aq >> 16));
+      vd = __half2float(__ushort_as_half(bq & 0xffff));
+      ve = __half2float(__ushort_as_half(bq >> 16));
+    } else {
+      const float* v = base + (iy * img.w + ix);
+      va = __ldg(v);
+      vb = __ldg(v + 1);
+      vd = __ldg(v + img.w);
+      ve = __ldg(v + img.w + 1);
+    }
     const float q = (1 - fy) * ((1 - fx) * va + fx * vb) + fy * ((1 - fx) * vd + fx * ve) - offset;
     const float gy = (1 - fx) * (vd - va) + fx * (ve - vb), gx = (1 - fy) * (vb - va) + fy * (ve - vd);
     const float g2 = gy * (-L.sa * dr - L.ca * dc) + gx * (L.ca * dr - L.sa * dc);
@@ -1652,6 +1760,26 @@ cudaError_t launch_dedup(const DedupArgs& a, int max_candidates, cudaStream_t s)
 
 cudaError_t launch_score(const ScoreArgs& a, int max_candidates, cudaStream_t s) {
   score_kernel<<<max_candidates, 128, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_coarse_lattice(Cand* cand, int2* rc, int nsrc, int nbr, int nbc, const int32_t* group_of_src,
+                                  int32_t* order, TcTiles* tiles, QueryState* state, int slot, cudaStream_t s) {
+  const int n = std::max(1, nsrc * nbr * nbc);
+  coarse_lattice_kernel<<<(n + 255) / 256, 256, 0, s>>>(cand, rc, nsrc, nbr, nbc, group_of_src, order, tiles, state,
+                                                        slot);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_coarse_tc_score(const CoarseTcArgs& a, cudaStream_t s) {
+  const long long n = (long long)a.nplist * a.lev.h * a.lev.w;
+  coarse_tc_score_kernel<<<unsigned((n + 255) / 256), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pairs(const float* v, int w, int h, uint32_t* pairs, cudaStream_t s) {
+  const long long n = (long long)w * h;
+  pairs_kernel<<<unsigned((n + 255) / 256), 256, 0, s>>>(v, w, h, pairs);
   return cudaGetLastError();
 }
 

@@ -34,6 +34,25 @@ struct CoarseArgs {
   int nplist;
   float* planes;            // nplist x h x w scores
   int absolute;
+  const uint8_t* skip;      // per kept patch: 1 = plane written by the tensor-core scan (nullable)
+};
+
+// Tensor-core coarse scan: a lattice of pseudo-candidates at stride 5 (each
+// covers a 5x5 block of positions) per virtual source (up to 16 kept coarse
+// patches), scored by tc_track_kernel; coarse_tc_score_kernel turns the dots
+// into score planes.
+struct CoarseTcArgs {
+  LevelImage lev;
+  LevelView view;
+  const int32_t* plist;
+  const PosRange* ranges;
+  int nplist;
+  const int32_t* src_of;    // per kept patch: its virtual source (-1: coarse_kernel's)
+  const int32_t* k_of;      // per kept patch: index in the virtual source's list
+  int lat_r, lat_c;         // lattice blocks per column / row
+  const float* dots;        // kTcScoreStride per pseudo-candidate
+  float* planes;
+  int absolute;
 };
 
 struct NmsArgs {
@@ -132,6 +151,7 @@ struct TcArgs {
   float plane_offset;                    // level value subtracted in the planes
   const uint16_t* planes;                // fp16 planes (launch_tc_planes)
   int plane_pitch;                       // elements per plane row
+  const int2* rc;                        // candidate lattice positions given directly (nullable)
   int32_t* error;
 };
 
@@ -145,6 +165,16 @@ size_t tc_kernel_static_smem();
 cudaError_t launch_tc_group(const TcArgs& a, int ngroups, int32_t* counts, int32_t* offsets, int32_t* cursor,
                             int max_candidates, cudaStream_t s);
 cudaError_t launch_tc_track(const TcArgs& a, size_t smem, int grid, cudaStream_t s);
+
+// Pseudo-candidates in source order, their lattice centres, the identity
+// order and the tile list (16 consecutive candidates of one source per tile).
+cudaError_t launch_coarse_lattice(Cand* cand, int2* rc, int nsrc, int nbr, int nbc, const int32_t* group_of_src,
+                                  int32_t* order, TcTiles* tiles, QueryState* state, int slot, cudaStream_t s);
+cudaError_t launch_coarse_tc_score(const CoarseTcArgs& a, cudaStream_t s);
+
+// half2 pairs (v[x], v[min(x + 1, w - 1)]) of a level whose values are exact
+// in fp16, w x h entries.
+cudaError_t launch_pairs(const float* v, int w, int h, uint32_t* pairs, cudaStream_t s);
 
 struct DedupArgs {
   const Cand* in;
@@ -160,6 +190,9 @@ struct DedupArgs {
 struct ImageView {
   const float* v;           // finest level (float of pixel sums)
   int w, h;
+  // optional: per pixel the fp16 pair (v[x], v[x+1]) as half2 bits, for
+  // levels whose values are exact in fp16 (two loads per bilinear tap)
+  const uint32_t* pairs = nullptr;
 };
 
 struct ScoreArgs {

@@ -349,7 +349,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const int ci = a.order[first + t];
         const Cand cd = a.in[ci];
         int R, C;
-        if (a.exact32) {
+        if (a.rc) {
+          R = a.rc[ci].x;
+          C = a.rc[ci].y;
+        } else if (a.exact32) {
           const float s = float(1.0 / a.step);
           R = int(roundf(__fmul_rn(__fsub_rn(__fsub_rn(float(cd.row), float(a.crop_row)), float(a.offset)), s)));
           C = int(roundf(__fmul_rn(__fsub_rn(__fsub_rn(float(cd.col), float(a.crop_col)), float(a.offset)), s)));
