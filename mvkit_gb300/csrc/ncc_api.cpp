@@ -243,6 +243,19 @@ const OrigDev& coarse_original(mvg_ncc_model_s& m, size_t level) {
   return *m.coarse_original[level];
 }
 
+// Dynamic shared memory one tensor-core block may use: kTcBlocksPerSm blocks
+// share an SM (228 KB, each with its static part and 1 KB reserved).
+size_t tc_smem_budget(size_t optin) {
+  const size_t per_sm = 228 * 1024;
+  const size_t share = per_sm / kTcBlocksPerSm - tc_kernel_static_smem() - 1024;
+  return std::min(share, optin - tc_kernel_static_smem()) - 1024;
+}
+// Launch size of a plan: with one block per SM, more than half the SM's
+// shared memory keeps a second block (and its tensor-memory allocation) off.
+size_t tc_launch_smem(const TcPlan& P, size_t optin) {
+  return kTcBlocksPerSm == 1 ? std::max(P.smem, optin / 2 + 1024) : P.smem;
+}
+
 // Correlation path of this thread's finds: tensor cores where applicable
 // (0) or FP32 CUDA cores only (1).
 thread_local int t_path = 0;
@@ -408,7 +421,7 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
     max_n = std::max(max_n, pr.n);
   }
   plan->npad = (max_n + 31) / 32 * 32;
-  plan->sets = std::max(1, std::min(4, 512 / plan->npad));
+  plan->sets = std::max(1, std::min(4, 512 / kTcBlocksPerSm / plan->npad));
   // shared memory: weight ring | two window buffers (rows_slab rows each).
   // The ring holds about eight grid rows of weights ahead of the MMAs (the L2
   // latency); the window buffers take the rest, at least 16 rows each.
@@ -522,6 +535,7 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
       g.r0[q] = o0 >> 16;
       g.c0[q] = int(int16_t(o0 & 0xffff));
       g.weff[q] = float(sum / sigma);
+      g.weff_k[pr.ks[size_t(q)]] = g.weff[q];
       g.macs += 25ll * d.n;
     }
     auto buf = std::make_unique<DevBuf<uint8_t>>();
@@ -855,7 +869,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   // tensor-core plans of the tracking steps (cached per target level)
   std::vector<std::shared_ptr<const TcPlan>> tc(level_count);
   if (t_path == 0) {
-    const size_t budget = ws.smem_optin - tc_kernel_static_smem() - 1024;
+    const size_t budget = tc_smem_budget(ws.smem_optin);
     for (size_t t = std::max(finest, size_t(opt.subpixel ? 1 : 0)); t + 1 < level_count; ++t) {
       float offset = 0;
       const int parts = tc_parts(type, t, &offset);
@@ -908,7 +922,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
       key.insert(key.end(), vp.plist.begin(), vp.plist.end());
       key.insert(key.end(), vsel_off.begin(), vsel_off.end());
       key.insert(key.end(), vsel_idx.begin(), vsel_idx.end());
-      const size_t budget = ws.smem_optin - tc_kernel_static_smem() - 1024;
+      const size_t budget = tc_smem_budget(ws.smem_optin);
       auto it = T.tc_plans.find(key);
       if (it == T.tc_plans.end()) {
         if (T.tc_plans.size() >= 32) T.tc_plans.clear();
@@ -1102,9 +1116,10 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
             "coarse lattice");
     }
     {
-      const size_t smem = std::max(P.smem, ws.smem_optin / 2 + 1024);
       Span spt(kStTrackTc, s);
-      check(launch_tc_track(tca, smem, std::min(kTcMaxTiles, ws.sm_count), s), "tc coarse");
+      check(launch_tc_track(tca, tc_launch_smem(P, ws.smem_optin), std::min(kTcMaxTiles, ws.sm_count * kTcBlocksPerSm),
+                            s),
+            "tc coarse");
     }
     CoarseTcArgs cs;
     cs.lev = lev[top];
@@ -1117,6 +1132,8 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     cs.lat_r = lat_r;
     cs.lat_c = lat_c;
     cs.dots = ws.coarse_dots.p;
+    cs.groups = d_co_groups;
+    cs.group_of_src = d_co_gsrc;
     cs.planes = ws.planes.p;
     cs.absolute = hm.params.ignore_polarity;
     Span sp(kStCoarse, s);
@@ -1203,6 +1220,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
       ta.absolute = hm.params.ignore_polarity;
       ta.tc_dots = nullptr;
       ta.tc_group_of_src = nullptr;
+      ta.tc_groups = nullptr;
       if (tc[t]) {
         const TcPlan& P = *tc[t];
         const int ng = int(P.groups.size());
@@ -1247,14 +1265,14 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
                 "tc group");
         }
         {
-          // more than half an SM's shared memory: one block per SM, which
-          // owns all 512 tensor-memory columns
-          const size_t smem = std::max(P.smem, ws.smem_optin / 2 + 1024);
           Span spt(kStTrackTc, s);
-          check(launch_tc_track(tca, smem, std::min(kTcMaxTiles, ws.sm_count), s), "tc track");
+          check(launch_tc_track(tca, tc_launch_smem(P, ws.smem_optin),
+                                std::min(kTcMaxTiles, ws.sm_count * kTcBlocksPerSm), s),
+                "tc track");
         }
         ta.tc_dots = ws.tc_dots.p;
         ta.tc_group_of_src = d_tc_gsrc[t];
+        ta.tc_groups = d_tc_groups[t];
       }
       Span sp(kStTrack, s);
       check(launch_track(ta, kMaxCandidates, s, ws.smem_optin), "track");

@@ -289,10 +289,14 @@ __global__ void coarse_tc_score_kernel(CoarseTcArgs a) {
   if (r >= rg.r0 && r < rg.r1 && c >= rg.c0 && c < rg.c1) {
     const PatchDesc pd = a.view.patches[a.plist[j]];
     const int ci = (src * a.lat_r + r / 5) * a.lat_c + c / 5;
-    const int pos = (r % 5) * 5 + c % 5;
+    const int pos = (r % 5) * 5 + c % 5, k = a.k_of[j];
     long long s1, s2;
     window_moments(a.lev, w + 1, r, c, a.view.runs + pd.run_off, a.view.runs_end + pd.run_off, pd.nruns, s1, s2);
-    score = window_score(a.dots[size_t(ci) * kTcScoreStride + a.k_of[j] * 25 + pos], s1, s2, pd.n, a.absolute);
+    // sum w (S - S0) = sum w S - S0 sum w (first sample S0)
+    const int2 f0 = __ldg(a.view.sw + pd.sample_off);
+    const float s0 = a.lev.v[size_t(r + off_row(f0.x)) * w + c + off_col(f0.x)];
+    const float dot = fmaf(-s0, a.groups[a.group_of_src[src]].weff_k[k], a.dots[size_t(ci) * kTcScoreStride + k * 25 + pos]);
+    score = window_score(dot, s1, s2, pd.n, a.absolute);
   }
   a.planes[idx] = score;
 }
@@ -541,7 +545,12 @@ __global__ void __launch_bounds__(kTrackThreads, 5) track_kernel(TrackArgs a) {
     if (part == 0 && valid) {
       float dot;
       if (is_tc) {
-        dot = a.tc_dots[size_t(i) * kTcScoreStride + item];
+        // sum w (S - S0) = sum w S - S0 sum w (first sample S0)
+        const int k = item / 25;
+        const int2 f0 = __ldg(a.view.sw + pd.sample_off);
+        const float s0 = a.lev.v[size_t(r + off_row(f0.x)) * pitch + c + off_col(f0.x)];
+        dot = fmaf(-s0, a.tc_groups[a.tc_group_of_src[cd.patch]].weff_k[k],
+                   a.tc_dots[size_t(i) * kTcScoreStride + item]);
       } else {
         dot = acc;
         for (int q = 1; q < split; ++q) dot += s_part[threadIdx.x + q * items];

@@ -8,6 +8,8 @@
 
 namespace mvg {
 
+struct TcGroup;  // tensor-core group (below)
+
 // Integer-valued pyramid levels held as float (exact: every level value is an
 // integer sum of 4^k input pixels, < 2^24).  Level 0 is the crop itself.
 struct LevelImage {
@@ -50,7 +52,9 @@ struct CoarseTcArgs {
   const int32_t* src_of;    // per kept patch: its virtual source (-1: coarse_kernel's)
   const int32_t* k_of;      // per kept patch: index in the virtual source's list
   int lat_r, lat_c;         // lattice blocks per column / row
-  const float* dots;        // kTcScoreStride per pseudo-candidate
+  const float* dots;        // kTcScoreStride per pseudo-candidate: sum w S
+  const TcGroup* groups;    // by virtual source (weff_k for the first-sample shift)
+  const int32_t* group_of_src;
   float* planes;
   int absolute;
 };
@@ -87,10 +91,11 @@ struct TrackArgs {
   int staged_ok;            // set by the launcher: dynamic shared memory holds the window
   int split_off;            // set by the launcher: float offset of the moment-split scratch in
                             // dynamic shared memory (-1: no scratch, moments in one slice)
-  // sum w (S - S0) of the rotated patches of tensor-core groups (nullable),
-  // kTcScoreStride per candidate
+  // sum w S of the rotated patches of tensor-core groups (nullable),
+  // kTcScoreStride per candidate, and their groups (for weff_k)
   const float* tc_dots;
   const int32_t* tc_group_of_src;
+  const TcGroup* tc_groups;
 };
 
 // Raises a kernel's dynamic shared-memory limit on the current device to at
@@ -110,6 +115,7 @@ constexpr int kTcMaxTiles = kMaxCandidates / kTcCands + kTcMaxGroups + 1;
 constexpr int kTcMaxStages = 16;         // weight-chunk buffers
 constexpr int kTcPlaneShifts = 8;        // column-shifted copies of a level plane
 constexpr int kTcPlaneMargin = 8;        // plane columns left of the level
+constexpr int kTcBlocksPerSm = 1;        // resident tensor-core blocks per SM (512 / this TMEM columns each)
 
 struct TcGroup {
   const uint8_t* b;                      // ceil(kr / rg) chunks: N x K fp16 weights, canonical K-major
@@ -125,6 +131,7 @@ struct TcGroup {
   int r0[kTcMaxP], c0[kTcMaxP];          // first sample offset of each patch
   float weff[kTcMaxP];                   // sum of the fp16 weights / scale
   float ecorr[kTcMaxP];                  // sum over grid rows of the centring row sums / scale
+  float weff_k[kTcMaxP];                 // weff by index in the selected list (0: not in the group)
 };
 
 struct TcTiles {
@@ -142,7 +149,8 @@ struct TcArgs {
   const int32_t* group_of_src;           // source patch -> group (-1: CUDA-core path)
   TcTiles* tiles;
   int32_t* order;
-  float* dots;                           // kTcScoreStride per candidate: sum w (S - S0)
+  float* dots;                           // kTcScoreStride per candidate: sum w S (consumers
+                                         // subtract S0 weff_k, S0 the first sample)
   double crop_row, crop_col, step, offset;
   int exact32;
   int stages;                            // weight-chunk buffers in use

@@ -45,7 +45,7 @@ namespace {
 constexpr int kTcThreads = 192;     // warp 0 MMA, warp 1 weights, warps 2-5 windows
 constexpr int kTcWindowThreads = 128;
 constexpr int kTcRows = 128;                  // MMA M
-constexpr uint32_t kTmemCols = 512;           // accumulator sets x columns per set
+constexpr uint32_t kTmemCols = 512 / kTcBlocksPerSm;  // accumulator sets x columns per set
 constexpr long long kSpinLimit = 1ll << 22;   // mbarrier polls before giving up
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
@@ -458,16 +458,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     for (int it = t; it < sh.cnt * 5 * G.p; it += kTcThreads) {
       const int g = it / (5 * G.p), dr = (it / G.p) % 5, q = it % G.p;
       const int m = g * 8 + dr;  // accumulator row
-      const int ci = sh.ci[g], R = sh.R[g], C = sh.C[g];
+      const int ci = sh.ci[g];
       const float cen = sh.centre[g];
-      const int W = a.lev.w, H = a.lev.h;
       float* out = a.dots + size_t(ci) * kTcScoreStride + size_t(G.k_of[q]) * 25 + dr * 5;
-      const int sr = min(max(R + dr - 2 + G.r0[q], 0), H - 1);
-      const float* srow = a.lev.v + size_t(sr) * W;
-      // first samples of the five placements, loaded before any store
-      float s0v[5];
-#pragma unroll
-      for (int dc = 0; dc < 5; ++dc) s0v[dc] = __ldg(srow + min(max(C + dc - 2 + G.c0[q], 0), W - 1));
+      // sum w S = sum w (S' - c) + c ecorr + offset weff, S' = S - offset:
+      // the consumers subtract S0 weff (first sample S0) themselves
+      const float shift = cen * G.ecorr[q] + a.plane_offset * G.weff[q];
 #pragma unroll
       for (int dc = 0; dc < 5; ++dc) {
         // sum w (S - c) with c the centre, as accumulated: accumulator row
@@ -477,11 +473,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           const int n0 = ((k * G.p + q) * 5 + dc) * 2;
           sum += D[(m + k) * ld + n0] + D[(m + k) * ld + n0 + 1];
         }
-        const float raw = sum * G.inv_scale;
-        const float s0 = s0v[dc] - a.plane_offset;
-        // sum w (S - S0) = raw + c (ecorr - weff) + (c - S0) weff: ecorr is
-        // the row-sum total as subtracted, weff the weights' sum
-        out[dc] = raw + (cen * (G.ecorr[q] - G.weff[q]) + (cen - s0) * G.weff[q]);
+        out[dc] = sum * G.inv_scale + shift;
       }
     }
     if (t == 0) {
