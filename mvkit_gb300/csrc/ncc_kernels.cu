@@ -355,7 +355,7 @@ constexpr int kTrackMaxSel = 64;
 __global__ void __launch_bounds__(kTrackThreads, 5) track_kernel(TrackArgs a) {
   extern __shared__ float win[];
   const int i = blockIdx.x;
-  if (i >= a.state->count[a.in_slot]) return;
+  if (i >= live_count(a.state, a.in_slot)) return;
   __shared__ int s_sel[kTrackMaxSel];
   __shared__ int s_row[kTrackMaxSel], s_col[kTrackMaxSel];
   __shared__ unsigned char s_istc[kTrackMaxSel];
@@ -656,7 +656,7 @@ __device__ void snap_pose(Cand& p, double height, double width) {
 
 __global__ void snap_kernel(Cand* c, const QueryState* state, int slot, double height, double width) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= state->count[slot]) return;
+  if (i >= live_count(state, slot)) return;
   Cand p = c[i];
   snap_pose(p, height, width);
   c[i] = p;
@@ -667,7 +667,7 @@ __global__ void snap_kernel(Cand* c, const QueryState* state, int slot, double h
 // and scores below the threshold; order is irrelevant downstream.
 __global__ void dedup_kernel(DedupArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.state->count[a.in_slot]) return;
+  if (i >= live_count(a.state, a.in_slot)) return;
   const Cand p = a.in[i];
   if (!isfinite(p.score) || p.score < a.threshold) return;
   const unsigned long long kr = __double_as_longlong(p.row), kc = __double_as_longlong(p.col),
@@ -883,7 +883,7 @@ __device__ void continuous_pass(const ImageView& img, const OriginalView& orig, 
 __global__ void __launch_bounds__(128) score_kernel(ScoreArgs a) {
   __shared__ PoseShared sh;
   const int i = blockIdx.x;
-  if (i >= a.state->count[a.slot]) return;
+  if (i >= live_count(a.state, a.slot)) return;
   const Cand c = a.cand[i];
   if (!isfinite(c.score)) return;
   const double row = (c.row - a.crop_row - a.phase) / a.scale;
@@ -919,7 +919,7 @@ constexpr int kSortPer = 64;
 __global__ void __launch_bounds__(256) sort_kernel(SortArgs a) {
   __shared__ unsigned long long s_key[2048];
   __shared__ int s_finite;
-  const int n = a.state->count[a.slot];
+  const int n = live_count(a.state, a.slot);
   if (int(blockIdx.x) * kSortPer >= n) return;
   const int lane4 = threadIdx.x & 3;
   const int i = blockIdx.x * kSortPer + (threadIdx.x >> 2);

@@ -10,6 +10,15 @@ namespace mvg {
 
 struct TcGroup;  // tensor-core group (below)
 
+// Entries of a candidate list that exist: a list's counter keeps counting
+// past the kMaxCandidates-entry buffers when the coarse budget overflows
+// (the find then ends with LimitExceeded), so readers clamp it.
+#ifdef __CUDACC__
+__device__ __forceinline__ int live_count(const QueryState* s, int slot) {
+  return min(s->count[slot], kMaxCandidates);
+}
+#endif
+
 // Integer-valued pyramid levels held as float (exact: every level value is an
 // integer sum of 4^k input pixels, < 2^24).  Level 0 is the crop itself.
 struct LevelImage {

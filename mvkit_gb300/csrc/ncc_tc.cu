@@ -454,27 +454,24 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    // one item = (candidate, row placement, patch): five column placements
-    for (int it = t; it < sh.cnt * 5 * G.p; it += kTcThreads) {
-      const int g = it / (5 * G.p), dr = (it / G.p) % 5, q = it % G.p;
-      const int m = g * 8 + dr;  // accumulator row
-      const int ci = sh.ci[g];
-      const float cen = sh.centre[g];
-      float* out = a.dots + size_t(ci) * kTcScoreStride + size_t(G.k_of[q]) * 25 + dr * 5;
-      // sum w S = sum w (S' - c) + c ecorr + offset weff, S' = S - offset:
-      // the consumers subtract S0 weff (first sample S0) themselves
-      const float shift = cen * G.ecorr[q] + a.plane_offset * G.weff[q];
-#pragma unroll
-      for (int dc = 0; dc < 5; ++dc) {
-        // sum w (S - c) with c the centre, as accumulated: accumulator row
-        // m + k of grid-row slot k holds this placement's grid rows y + k
-        float sum = 0.f;
-        for (int k = 0; k < G.rg; ++k) {
-          const int n0 = ((k * G.p + q) * 5 + dc) * 2;
-          sum += D[(m + k) * ld + n0] + D[(m + k) * ld + n0 + 1];
-        }
-        out[dc] = sum * G.inv_scale + shift;
+    // one output per thread, consecutive threads on consecutive dots of a
+    // candidate ([selected patch][row placement][column placement])
+    const int per = 25 * G.p;
+    for (int it = t; it < sh.cnt * per; it += kTcThreads) {
+      const int g = it / per, e = it - g * per;
+      const int q = e / 25, pos = e - q * 25, dr = pos / 5, dc = pos - dr * 5;
+      const int m = g * 8 + dr;  // accumulator row of grid-row slot 0
+      // sum w (S' - c) over the chunk's grid-row slots: slot k holds this
+      // placement's grid rows y + k in accumulator row m + k
+      float sum = 0.f;
+      for (int k = 0; k < G.rg; ++k) {
+        const int n0 = ((k * G.p + q) * 5 + dc) * 2;
+        sum += D[(m + k) * ld + n0] + D[(m + k) * ld + n0 + 1];
       }
+      // sum w S = sum w (S' - c) + c ecorr + offset weff (S' = S - offset);
+      // the consumers subtract S0 weff (first sample S0) themselves
+      a.dots[size_t(sh.ci[g]) * kTcScoreStride + size_t(G.k_of[q]) * 25 + pos] =
+          sum * G.inv_scale + (sh.centre[g] * G.ecorr[q] + a.plane_offset * G.weff[q]);
     }
     if (t == 0) {
       atomicAdd(&a.state_rw->tc_macs, (unsigned long long)G.macs * (unsigned long long)sh.cnt);
@@ -524,7 +521,7 @@ __global__ void tc_planes_kernel(LevelImage lev, __half* planes, int pitch, int 
 __global__ void tc_count_kernel(const Cand* in, const QueryState* state, int slot, const int32_t* group_of_src,
                                 int32_t* counts) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= state->count[slot]) return;
+  if (i >= live_count(state, slot)) return;
   const int src = in[i].patch;
   const int gi = src >= 0 ? group_of_src[src] : -1;
   if (gi >= 0) atomicAdd(counts + gi, 1);
@@ -571,7 +568,7 @@ __global__ void __launch_bounds__(1024) tc_plan_kernel(const int32_t* counts, in
 __global__ void tc_scatter_kernel(const Cand* in, const QueryState* state, int slot, const int32_t* group_of_src,
                                   const int32_t* offsets, int32_t* cursor, int32_t* order) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= state->count[slot]) return;
+  if (i >= live_count(state, slot)) return;
   const int src = in[i].patch;
   const int gi = src >= 0 ? group_of_src[src] : -1;
   if (gi < 0) return;

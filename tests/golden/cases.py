@@ -72,6 +72,43 @@ CASES = {
                           create=dict(levels=3, angle_start=-D(5), angle_extent=D(10)),
                           find=dict(angle_start=-D(5), angle_extent=D(10), min_score=0.5, num_matches=0,
                                     max_overlap=0.0, subpixel=True, highest=3, lowest=1)),
+    # full-circle models: the angle list wraps, coarse stride and windows span it
+    "full_circle": dict(gen=dict(seed=22, height=480, width=640, tsize=64, n_poses=3,
+                                 angle_range=(-math.pi, math.pi)),
+                        create=dict(levels=4, angle_start=-math.pi, angle_extent=2 * math.pi),
+                        find=dict(angle_start=-math.pi, angle_extent=2 * math.pi, min_score=0.7, num_matches=3,
+                                  max_overlap=0.5, subpixel=True, highest=4, lowest=1)),
+    "full_circle_72": dict(gen=dict(seed=28, height=480, width=640, tsize=72, n_poses=3,
+                                    angle_range=(-math.pi, math.pi)),
+                           create=dict(levels=4, angle_start=-math.pi, angle_extent=2 * math.pi),
+                           find=dict(angle_start=-math.pi, angle_extent=2 * math.pi, min_score=0.7, num_matches=0,
+                                     max_overlap=0.5, subpixel=True, highest=4, lowest=1)),
+    # automatic levels on a full circle: the reference exceeds its coarse
+    # candidate budget and returns LimitExceeded (-103)
+    "budget_360": dict(gen=dict(seed=22, height=480, width=640, tsize=48, n_poses=3,
+                                angle_range=(-math.pi, math.pi)),
+                       create=dict(levels=0, angle_start=-math.pi, angle_extent=2 * math.pi),
+                       find=dict(angle_start=-math.pi, angle_extent=2 * math.pi, min_score=0.7, num_matches=3,
+                                 max_overlap=0.5, subpixel=True, highest=0, lowest=1)),
+    # query range wider than the trained range (clipped to it)
+    "query_clip": dict(gen=dict(seed=24, height=480, width=640, tsize=56, n_poses=2, angle_range=(-D(18), D(18))),
+                       create=dict(levels=3, angle_start=-D(20), angle_extent=D(40)),
+                       find=dict(angle_start=-D(40), angle_extent=D(100), min_score=0.7, num_matches=2,
+                                 max_overlap=0.5, subpixel=True, highest=3, lowest=1)),
+    # 12-bit data in uint16 (the large-image configuration's format), wide angles
+    "u16_12bit": dict(gen=dict(seed=25, height=480, width=640, tsize=64, n_poses=2, angle_range=(-D(45), D(45)),
+                               maxval=4095, noise_sigma=20),
+                      create=dict(levels=3, angle_start=-D(45), angle_extent=D(90)),
+                      find=dict(angle_start=-D(45), angle_extent=D(90), min_score=0.6, num_matches=2,
+                                max_overlap=0.5, subpixel=True, highest=3, lowest=1)),
+    "tiny16": dict(gen=dict(seed=26, height=240, width=320, tsize=16, n_poses=2, angle_range=(-D(10), D(10))),
+                   create=dict(levels=2, angle_start=-D(10), angle_extent=D(20)),
+                   find=dict(angle_start=-D(10), angle_extent=D(20), min_score=0.7, num_matches=2, max_overlap=0.5,
+                             subpixel=True, highest=2, lowest=1)),
+    "big160": dict(gen=dict(seed=27, height=720, width=960, tsize=160, n_poses=2, angle_range=(-D(12), D(12))),
+                   create=dict(levels=4, angle_start=-D(12), angle_extent=D(24)),
+                   find=dict(angle_start=-D(12), angle_extent=D(24), min_score=0.7, num_matches=2, max_overlap=0.5,
+                             subpixel=True, highest=4, lowest=1)),
 }
 
 # Large single-GPU throughput case, checked against the oracle at full size.

@@ -42,7 +42,15 @@ def main():
     out = {"source": "reference mvkit matcher compiled from its sources (scalar build)", "cases": {}}
     for name, case in {**CASES, **LARGE}.items():
         wl, mask = make_inputs(case)
-        model, res, dt = run(scalar, case, wl, mask)
+        try:
+            model, res, dt = run(scalar, case, wl, mask)
+        except oracle_lib.CheckerError as e:
+            # the reference rejects the search (e.g. coarse candidate budget):
+            # the fixture records the status the drop-in must return
+            out["cases"][name] = {"digest": wl.digest(), "status": e.status, "message": str(e),
+                                  "truth": [[p.row, p.column, p.angle] for p in wl.poses]}
+            print(name, "status", e.status, flush=True)
+            continue
         info = model.info()
         entry = {"digest": wl.digest(), "matches": res.tolist(), "seconds_scalar": round(dt, 4),
                  "levels": info["levels"], "angle_step": info["angle_step"],
