@@ -54,6 +54,25 @@ MVG_API int32_t mvg_create_ncc_model(const void* pixels, int32_t pixel_type, int
 MVG_API int32_t mvg_get_ncc_model_params(mvg_ncc_model model_id, int32_t* num_levels, double* angle_start,
                                  double* angle_extent, double* angle_step, int32_t* metric);
 
+/* Replaces mv_write_ncc_model (include/mvkit/c/mv_ncc_matching.h:84;
+ * src/ncc_matching/persist.cpp:33-43,78-80).  Writes the reference's
+ * "MVKIT_NCC 1" text file (FNV-1a 64 checksum), byte-identical to what the
+ * reference writes for the same model.  file_name: UTF-8, nonempty. */
+MVG_API int32_t mvg_write_ncc_model(mvg_ncc_model model_id, const char* file_name);
+
+/* Replaces mv_read_ncc_model (include/mvkit/c/mv_ncc_matching.h:94;
+ * src/ncc_matching/persist.cpp:44-83).  Reads a model file written by the
+ * reference or by mvg_write_ncc_model and rebuilds the model; statuses as
+ * the reference: IoError (-100), DecodeError (-101), Unsupported (-6) for
+ * another format version, LimitExceeded (-103). */
+MVG_API int32_t mvg_read_ncc_model(const char* file_name, mvg_ncc_model* model_id);
+
+/* In-memory forms of the two calls above: the file bytes.  serialize
+ * stores the byte count in *size and copies min(size, capacity) bytes to
+ * buffer (buffer may be NULL to query the size). */
+MVG_API int32_t mvg_serialize_ncc_model(mvg_ncc_model model_id, char* buffer, int64_t capacity, int64_t* size);
+MVG_API int32_t mvg_deserialize_ncc_model(const char* bytes, int64_t size, mvg_ncc_model* model_id);
+
 /* Releases a model (the reference frees it with the handle tuple,
  * mv_destroy_tuple; include/mvkit/c/mv_ncc_matching.h:64-67). */
 MVG_API int32_t mvg_clear_ncc_model(mvg_ncc_model model_id);

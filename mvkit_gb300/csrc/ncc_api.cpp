@@ -208,6 +208,8 @@ struct OrigDev {
 
 struct mvg_ncc_model_s {
   mvg::HostModel host;
+  // device tables, uploaded by the first find (under `mutex`) to the device
+  // current then; a model is built and saved on the host alone
   std::vector<std::unique_ptr<mvg::DevLevel>> levels;
   mvg::OrigDev original;
   // unrotated rasters of coarser finest levels (lowest_level > 1), by level
@@ -218,6 +220,23 @@ struct mvg_ncc_model_s {
 
 namespace mvg {
 namespace {
+
+// The model's sample, run and raster tables in HBM (once per model).
+void ensure_device(mvg_ncc_model_s& m) {
+  if (!m.levels.empty()) return;
+  check(cudaGetDevice(&m.device), "cudaGetDevice");
+  std::vector<std::unique_ptr<DevLevel>> levels;
+  for (const ModelLevel& L : m.host.levels) {
+    auto d = std::make_unique<DevLevel>();
+    d->set_geometry(L.width, L.height);
+    for (const Raster& r : L.patches) d->append(r);
+    d->model_patches = d->desc.size();
+    d->upload();
+    levels.push_back(std::move(d));
+  }
+  m.original.set(m.host.original, m.host.levels.front().orow, m.host.levels.front().ocol);
+  m.levels = std::move(levels);
+}
 
 // Index of the raster at `angle` on `level` among the query endpoints,
 // building and uploading it on first use.  -1 when degenerate.
@@ -772,6 +791,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   // Planning reads (and may extend) the model's endpoint rasters: serialise
   // it per model and snapshot the device views used by this find.
   std::unique_lock<std::mutex> lock(m.mutex);
+  ensure_device(m);
   LevelView views[kMaxLevels];
 
   // query patch lists (matcher.cpp:463-482)
@@ -1500,16 +1520,46 @@ int32_t mvg_create_ncc_model(const void* pixels, int32_t pixel_type, int64_t wid
     p.angle_step = angle_step > 0 ? angle_step : 0.;
     auto m = std::make_unique<mvg_ncc_model_s>();
     m->host = create_model(pixels, pixel_type, width, height, row_stride, domain, p);
-    check(cudaGetDevice(&m->device), "cudaGetDevice");
-    for (const ModelLevel& L : m->host.levels) {
-      auto d = std::make_unique<DevLevel>();
-      d->set_geometry(L.width, L.height);
-      for (const Raster& r : L.patches) d->append(r);
-      d->model_patches = d->desc.size();
-      d->upload();
-      m->levels.push_back(std::move(d));
-    }
-    m->original.set(m->host.original, m->host.levels.front().orow, m->host.levels.front().ocol);
+    *model_id = m.release();
+  });
+}
+
+int32_t mvg_write_ncc_model(mvg_ncc_model model_id, const char* file_name) {
+  return guarded([&] {
+    if (!model_id) raise(kInvalidArgument, "control handle is not an NCC model");
+    if (!file_name || !*file_name) raise(kInvalidArgument, "nonempty file name without NUL required");
+    write_model_file(model_id->host, file_name);
+  });
+}
+
+int32_t mvg_read_ncc_model(const char* file_name, mvg_ncc_model* model_id) {
+  return guarded([&] {
+    if (!model_id) raise(kInvalidArgument, "ModelID must not be null");
+    *model_id = nullptr;
+    if (!file_name || !*file_name) raise(kInvalidArgument, "nonempty file name without NUL required");
+    auto m = std::make_unique<mvg_ncc_model_s>();
+    m->host = read_model_file(file_name);
+    *model_id = m.release();
+  });
+}
+
+int32_t mvg_serialize_ncc_model(mvg_ncc_model model_id, char* buffer, int64_t capacity, int64_t* size) {
+  return guarded([&] {
+    if (!model_id) raise(kInvalidArgument, "control handle is not an NCC model");
+    if (!size) raise(kInvalidArgument, "size must not be null");
+    const std::string bytes = serialize_model(model_id->host);
+    *size = int64_t(bytes.size());
+    if (buffer && capacity > 0) std::memcpy(buffer, bytes.data(), size_t(std::min<int64_t>(capacity, *size)));
+  });
+}
+
+int32_t mvg_deserialize_ncc_model(const char* bytes, int64_t size, mvg_ncc_model* model_id) {
+  return guarded([&] {
+    if (!model_id) raise(kInvalidArgument, "ModelID must not be null");
+    *model_id = nullptr;
+    if (size < 0 || (!bytes && size > 0)) raise(kInvalidArgument, "invalid model bytes");
+    auto m = std::make_unique<mvg_ncc_model_s>();
+    m->host = deserialize_model(std::string_view(bytes ? bytes : "", size_t(size)));
     *model_id = m.release();
   });
 }

@@ -137,7 +137,12 @@ bool level_usable(const ModelLevel& L, size_t* count) {
   return energy > 0 && std::isfinite(energy);
 }
 
-HostModel build_levels(ModelLevel first, const CreateParams& params, double origin_row, double origin_col) {
+}  // namespace
+
+// rebuild() of src/ncc_matching/model.cpp:173-242: the original raster, the
+// pyramid, the resolved angle step and every level's rotated rasters from the
+// mean-free level-0 raster.
+HostModel rebuild_model(ModelLevel first, const CreateParams& params, double origin_row, double origin_col) {
   HostModel m;
   m.params = params;
   m.origin_row = origin_row;
@@ -231,6 +236,8 @@ HostModel build_levels(ModelLevel first, const CreateParams& params, double orig
   return m;
 }
 
+namespace {
+
 template <class T>
 HostModel create_typed(const T* px, int64_t width, int64_t height, int64_t stride_elems, const uint8_t* mask,
                        const CreateParams& params) {
@@ -289,7 +296,7 @@ HostModel create_typed(const T* px, int64_t width, int64_t height, int64_t strid
   const double mean = double(isum) / double(a);
   for (size_t i = 0; i < first.gray.size(); ++i)
     if (first.mask[i]) first.gray[i] -= mean;
-  return build_levels(std::move(first), params, origin_row, origin_col);
+  return rebuild_model(std::move(first), params, origin_row, origin_col);
 }
 
 }  // namespace

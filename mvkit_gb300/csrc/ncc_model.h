@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <string_view>
 #include <vector>
 
 #include "ncc_types.h"
@@ -55,6 +56,19 @@ struct HostModel {
 // the whole image.  Throws Error with an MvStatus code.
 HostModel create_model(const void* pixels, int type, int64_t width, int64_t height, int64_t stride_bytes,
                        const uint8_t* mask, const CreateParams& params);
+
+// The model from its mean-free level-0 raster (gray minus the template mean,
+// mask, size and centroid) and the trained options: the path shared by
+// create and by reading a model file.  Throws Error.
+HostModel rebuild_model(ModelLevel first, const CreateParams& params, double origin_row, double origin_col);
+
+// Model files ("MVKIT_NCC 1", src/ncc_matching/persist.cpp:33-83): text body
+// of the trained options, the level-0 raster and its centroid, prefixed by an
+// FNV-1a 64 checksum of the body.  deserialize_model rebuilds the model.
+std::string serialize_model(const HostModel& model);
+HostModel deserialize_model(std::string_view bytes);
+void write_model_file(const HostModel& model, const std::string& path);
+HostModel read_model_file(const std::string& path);
 
 // Raster of `level` rotated by `angle` (used for query-range endpoints that
 // fall between trained angles).  Empty when the rotation is degenerate.

@@ -18,6 +18,8 @@ enum Status : int32_t {
   kOutOfMemory = -5,
   kUnsupported = -6,
   kInvalidState = -7,
+  kIoError = -100,
+  kDecodeError = -101,
   kLimitExceeded = -103,
   kInternal = -1000,
 };

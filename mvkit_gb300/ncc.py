@@ -25,6 +25,8 @@ MV_STATUS_TYPE_MISMATCH = -3
 MV_STATUS_OUT_OF_MEMORY = -5
 MV_STATUS_UNSUPPORTED = -6
 MV_STATUS_INVALID_STATE = -7
+MV_STATUS_IO_ERROR = -100
+MV_STATUS_DECODE_ERROR = -101
 MV_STATUS_LIMIT_EXCEEDED = -103
 MV_STATUS_INTERNAL_ERROR = -1000
 
@@ -70,6 +72,10 @@ def load() -> C.CDLL:
                                              C.c_int32, C.c_int32, C.c_int32, C.c_int32, _dp, C.c_int64, _i64p]
     lib.mvg_ncc_pyramid_level.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_void_p,
                                           C.c_int32, C.c_int32, _fp, C.c_int64, _dp]
+    lib.mvg_write_ncc_model.argtypes = [C.c_void_p, C.c_char_p]
+    lib.mvg_read_ncc_model.argtypes = [C.c_char_p, C.POINTER(C.c_void_p)]
+    lib.mvg_serialize_ncc_model.argtypes = [C.c_void_p, C.c_char_p, C.c_int64, _i64p]
+    lib.mvg_deserialize_ncc_model.argtypes = [C.c_char_p, C.c_int64, C.POINTER(C.c_void_p)]
     lib.mvg_last_error.restype = C.c_char_p
     lib.mvg_host_alloc.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
     lib.mvg_host_free.argtypes = [C.c_void_p]
@@ -83,7 +89,8 @@ def load() -> C.CDLL:
         getattr(lib, name).restype = C.c_int32
     for name in ("mvg_create_ncc_model", "mvg_get_ncc_model_params", "mvg_clear_ncc_model", "mvg_find_ncc_model",
                  "mvg_find_ncc_model_stage", "mvg_ncc_pyramid_level", "mvg_host_alloc", "mvg_host_free",
-                 "mvg_device_alloc", "mvg_device_free", "mvg_copy_to_device"):
+                 "mvg_device_alloc", "mvg_device_free", "mvg_copy_to_device", "mvg_write_ncc_model", "mvg_read_ncc_model",
+                 "mvg_serialize_ncc_model", "mvg_deserialize_ncc_model"):
         getattr(lib, name).restype = C.c_int32
     _LIB = lib
     return lib
@@ -213,6 +220,57 @@ def get_ncc_model_params(model: NccModel):
     _check(load().mvg_get_ncc_model_params(model.handle, C.byref(lv), C.byref(a0), C.byref(a1), C.byref(a2),
                                            C.byref(mt)), "get_ncc_model_params")
     return (lv.value, a0.value, a1.value, a2.value, "ignore_global_polarity" if mt.value else "use_polarity")
+
+
+def _file_name(name, op: str) -> bytes:
+    """FileName control: exactly one nonempty string without NUL
+    (src/c_api/ncc_matching_api.cpp:77-83)."""
+    v = _one(name, op, "FileName")
+    if isinstance(v, Path):
+        v = str(v)
+    if not isinstance(v, str):
+        raise MvError(MV_STATUS_TYPE_MISMATCH, "FileName: string control value required", op)
+    if not v or "\0" in v:
+        raise MvError(MV_STATUS_INVALID_ARGUMENT, "nonempty file name without NUL required", op)
+    return v.encode("utf-8")
+
+
+def write_ncc_model(model: NccModel, file_name) -> None:
+    """WriteNccModel (src/c_api/ncc_matching_api.cpp:97-99): the reference's
+    "MVKIT_NCC 1" model file, byte-identical to the reference's."""
+    op = "write_ncc_model"
+    lib = load()
+    _check(lib.mvg_write_ncc_model(model.handle, _file_name(file_name, op)), op)
+
+
+def read_ncc_model(file_name) -> NccModel:
+    """ReadNccModel (src/c_api/ncc_matching_api.cpp:101-110)."""
+    op = "read_ncc_model"
+    lib = load()
+    h = C.c_void_p()
+    _check(lib.mvg_read_ncc_model(_file_name(file_name, op), C.byref(h)), op)
+    return NccModel(h)
+
+
+def serialize_ncc_model(model: NccModel) -> bytes:
+    """The model file's bytes (what write_ncc_model writes)."""
+    op = "serialize_ncc_model"
+    lib = load()
+    n = C.c_int64()
+    _check(lib.mvg_serialize_ncc_model(model.handle, None, 0, C.byref(n)), op)
+    buf = C.create_string_buffer(max(1, n.value))
+    _check(lib.mvg_serialize_ncc_model(model.handle, buf, n.value, C.byref(n)), op)
+    return buf.raw[:n.value]
+
+
+def deserialize_ncc_model(data: bytes) -> NccModel:
+    """A model from model-file bytes (what read_ncc_model reads)."""
+    op = "deserialize_ncc_model"
+    lib = load()
+    b = bytes(data)
+    h = C.c_void_p()
+    _check(lib.mvg_deserialize_ncc_model(b, len(b), C.byref(h)), op)
+    return NccModel(h)
 
 
 def _find_controls(op, angle_start, angle_extent, min_score, num_matches, max_overlap, subpixel, num_levels):

@@ -12,6 +12,7 @@
 #include <core/image.hpp>
 #include <core/region.hpp>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <exception>
@@ -90,6 +91,27 @@ int ref_ncc_create(const void* tmpl, int type, std::int64_t w, std::int64_t h, s
 }
 
 void ref_ncc_free(void* model) { delete static_cast<ncc::Model*>(model); }
+
+// Model file bytes (mv::ncc_matching::serialize, src/ncc_matching/persist.cpp:33).
+// Returns the size; copies min(size, cap) bytes into buf.  -1 on error.
+std::int64_t ref_ncc_serialize(void* model, char* buf, std::int64_t cap, char* err, int errlen) {
+  std::int64_t size = -1;
+  const int status = guarded(err, errlen, [&] {
+    const std::string bytes = ncc::serialize(*static_cast<ncc::Model*>(model));
+    size = std::int64_t(bytes.size());
+    if (buf && cap > 0) std::memcpy(buf, bytes.data(), std::size_t(std::min<std::int64_t>(cap, size)));
+  });
+  return status ? -1 : size;
+}
+
+// mv::ncc_matching::deserialize (src/ncc_matching/persist.cpp:44); returns
+// the reference status.
+int ref_ncc_deserialize(const char* bytes, std::int64_t size, void** out, char* err, int errlen) {
+  *out = nullptr;
+  return guarded(err, errlen, [&] {
+    *out = new ncc::Model(ncc::deserialize(std::string_view(bytes, std::size_t(size))));
+  });
+}
 
 // info[0]=levels info[1]=angle_step info[2]=origin_row info[3]=origin_column
 // info[4]=patches per level (level 0)  info[5]=original sample count

@@ -69,6 +69,31 @@ class Checker:
                                    C.c_double, C.c_int, C.c_int, C.c_int]
             self._many.restype = C.c_int64
         self._find.restype = C.c_int
+        if prefix == "ref":
+            self._ser = lib.ref_ncc_serialize
+            self._ser.argtypes = [C.c_void_p, C.c_char_p, C.c_int64, C.c_char_p, C.c_int]
+            self._ser.restype = C.c_int64
+            self._deser = lib.ref_ncc_deserialize
+            self._deser.argtypes = [C.c_char_p, C.c_int64, C.POINTER(C.c_void_p), C.c_char_p, C.c_int]
+            self._deser.restype = C.c_int
+
+    # -- model files (reference only: mv::ncc_matching::serialize/deserialize)
+    def serialize(self, model) -> bytes:
+        err = C.create_string_buffer(256)
+        n = self._ser(model.handle, None, 0, err, 256)
+        if n < 0:
+            raise CheckerError(-1000, err.value.decode())
+        buf = C.create_string_buffer(max(1, n))
+        self._ser(model.handle, buf, n, err, 256)
+        return buf.raw[:n]
+
+    def deserialize(self, data: bytes):
+        h = C.c_void_p()
+        err = C.create_string_buffer(256)
+        st = self._deser(bytes(data), len(data), C.byref(h), err, 256)
+        if st != 0:
+            raise CheckerError(st, err.value.decode())
+        return Model(self, h)
 
     # -- model
     def create(self, tmpl: np.ndarray, levels=0, angle_start=0.0, angle_extent=0.0, angle_step=0.0,

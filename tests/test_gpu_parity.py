@@ -79,6 +79,22 @@ def test_find_matches_reference(mg, name):
     assert_same_matches(got, GOLDEN[name]["matches"], name)
 
 
+@pytest.mark.parametrize("name", ["tiny16", "rot3_all", "mask_disc", "u16_rot"])
+def test_find_with_model_from_file(mg, name, tmp_path):
+    """A model read back from its file finds what the reference finds.  For
+    tiny16 the file is the reference's own (tests/golden/models/); the other
+    cases write ours, whose bytes equal the reference's (test_persist.py)."""
+    case = CASES[name]
+    wl, mask = make_inputs(case)
+    if name == "tiny16":
+        path = Path(__file__).parent / "golden" / "models" / "tiny16.ncm"
+    else:
+        path = tmp_path / f"{name}.ncm"
+        mg.write_ncc_model(gpu_model(mg, case, wl, mask), str(path))
+    model = mg.read_ncc_model(str(path))
+    assert_same_matches(gpu_find(mg, model, wl.image, case), GOLDEN[name]["matches"], name)
+
+
 def test_find_matches_reference_2048(mg):
     case = LARGE["cfg2_s1"]
     wl, mask = make_inputs(case)
