@@ -96,6 +96,28 @@ MVG_API int32_t mvg_find_ncc_model(const void* pixels, int32_t pixel_type, int64
                            double* row, double* column, double* angle, double* score, int64_t capacity,
                            int64_t* count, void* stream);
 
+/* Replaces mv_find_ncc_models (include/mvkit/c/mv_ncc_matching.h:119-123;
+ * src/c_api/ncc_matching_api.cpp:191-201 over
+ * mv::ncc_matching::find_models, src/ncc_matching/matcher.cpp:1077-1124).
+ * Searches one image for num_models (1..4096) models.  Each control is an
+ * array with its value count, as the reference's tuples: one value shared by
+ * all models or one per model; num_levels holds 1 (highest), 2 (highest,
+ * lowest), num_models (highest per model) or 2*num_models (pairs) values.
+ * subpixel values are 0/1.  A shared NumMatches / MaxOverlap (one value) is a
+ * limit / suppression over all models; per-model values apply per model,
+ * and with a shared MaxOverlap the per-model quotas are applied before the
+ * cross-model suppression (HALCON's rule, as the reference).  Outputs as
+ * mvg_find_ncc_model plus model[i], the index into model_ids. */
+MVG_API int32_t mvg_find_ncc_models(const void* pixels, int32_t pixel_type, int64_t width, int64_t height,
+                                    int64_t row_stride, int32_t location, const mvg_ncc_model* model_ids,
+                                    int64_t num_models, const double* angle_start, int64_t n_angle_start,
+                                    const double* angle_extent, int64_t n_angle_extent, const double* min_score,
+                                    int64_t n_min_score, const int64_t* num_matches, int64_t n_num_matches,
+                                    const double* max_overlap, int64_t n_max_overlap, const int32_t* subpixel,
+                                    int64_t n_subpixel, const int32_t* num_levels, int64_t n_num_levels,
+                                    double* row, double* column, double* angle, double* score, int64_t* model,
+                                    int64_t capacity, int64_t* count, void* stream);
+
 /* Candidate list of one internal stage of a find, in the matcher's
  * pixel-centre pose convention (mv::ncc_matching::find,
  * src/ncc_matching/matcher.cpp:1063): stage 0 = coarse candidates after

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -588,6 +589,7 @@ struct Workspace {
   DevBuf<Cand> coarse_cand;
   DevBuf<int2> coarse_rc;
   DevBuf<uint32_t> pairs;            // fp16 pairs of the finest level
+  int pairs_level = -1;              // the level `pairs` holds
   DevBuf<uint16_t> tc_planes;
   DevBuf<int32_t> tc_order, tc_counts, tc_offsets, tc_cursor;
   DevBuf<TcTiles> tc_tiles;
@@ -744,10 +746,25 @@ void fetch_stage(Workspace& ws, cudaStream_t s, const Cand* src, int slot, FindO
   for (const Cand& c : h) out.stage.push_back({c.row, c.col, c.angle, c.score});
 }
 
+// One model's query prepared for a multi-model selection
+// (matcher.cpp:1077-1101): its sorted candidates with finite scores and what
+// refining one of them needs.  The refinement reads the workspace's pyramid,
+// which every model of one image shares (same crop, same levels).
+struct Prepared {
+  RefineArgs ra;               // candidate buffers are set per launch
+  RectGeom geom;               // the model's level-0 box (make_rect)
+  int finest = 0;
+  std::vector<Cand> cands;
+  DevBuf<int32_t> plist0;      // own copies of the level-0 query tables
+  DevBuf<PosRange> ranges0;
+};
+
 // One find on the current device.  stage >= 0 stops after that stage and
-// returns its candidate list.
+// returns its candidate list.  With `prep`, the find stops after the sort and
+// fills *prep instead of selecting.
 FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W, int64_t H, int64_t stride,
-                    int location, const FindParams& req, cudaStream_t user_stream, int stage) {
+                    int location, const FindParams& req, cudaStream_t user_stream, int stage,
+                    Prepared* prep = nullptr) {
   FindOutput out;
   const HostModel& hm = m.host;
   // src/ncc_matching/matcher.cpp:349-374 (validation and range clipping)
@@ -1333,6 +1350,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     Span sp(kStScore, s, 1);
     check(launch_pairs(lev[finest].v, lw[finest], lh[finest], ws.pairs.p, s), "pairs");
     fine.pairs = ws.pairs.p;
+    ws.pairs_level = int(finest);
   }
   {
     ScoreArgs sa;
@@ -1404,6 +1422,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   ra.refined_flag = ws.refined_flag.p;
   ra.batch = ws.batch.p;
   ra.state = st;
+  ra.batch_count = -1;
   ra.crop_row = double(crop_row);
   ra.crop_col = double(crop_col);
   ra.scale = fscale;
@@ -1420,6 +1439,35 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   ra.height = Hd;
   ra.width = Wd;
   ra.geom = geom;
+  if (prep) {
+    // multi-model selection: the sorted list to the host, the level-0 query
+    // tables to buffers of the prepared query (the workspace's are reused)
+    check(cudaMemcpyAsync(ws.h_state, st, sizeof(QueryState), cudaMemcpyDeviceToHost, s), "state");
+    check(cudaStreamSynchronize(s), "sync");
+    if (ws.h_state->overflow) raise(kLimitExceeded, "coarse candidate budget exceeded");
+    if (ws.h_state->error) raise(ws.h_state->error, "pyramid sums exceed the exact float range");
+    const int n = std::max(0, std::min(ws.h_state->sorted_count, kMaxCandidates));
+    prep->cands.resize(size_t(n));
+    if (n > 0)
+      check(cudaMemcpyAsync(prep->cands.data(), ws.sorted.p, size_t(n) * sizeof(Cand), cudaMemcpyDeviceToHost, s),
+            "sorted");
+    prep->plist0.reserve(plan[0].plist.size());
+    prep->ranges0.reserve(plan[0].ranges.size());
+    if (!plan[0].plist.empty())
+      check(cudaMemcpyAsync(prep->plist0.p, d_plist[0], plan[0].plist.size() * sizeof(int32_t),
+                            cudaMemcpyDeviceToDevice, s), "plist0");
+    if (!plan[0].ranges.empty())
+      check(cudaMemcpyAsync(prep->ranges0.p, d_ranges[0], plan[0].ranges.size() * sizeof(PosRange),
+                            cudaMemcpyDeviceToDevice, s), "ranges0");
+    check(cudaStreamSynchronize(s), "sync");
+    prep->ra = ra;
+    prep->ra.plist0 = prep->plist0.p;
+    prep->ra.ranges0 = prep->ranges0.p;
+    prep->geom = geom;
+    prep->finest = int(finest);
+    t_prof.collect();
+    return out;
+  }
   {
     Span sp(kStSelect, s, 2);
     check(launch_rects(ws.sorted.p, ws.aux.p, st, geom, kMaxCandidates, s), "rects");
@@ -1454,6 +1502,314 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   }
   for (const Cand& c : acc) out.matches.push_back({c.row, c.col, c.angle, c.score});
   if (stage == -1) out.stage = out.matches;
+  return out;
+}
+
+// ------------------------------------------------------------ FindNccModels
+// Selection shared by all models (matching::Selection, src/matching/multi.hpp:14):
+// -1 means "per model" (the control tuple held one value per model).
+struct Selection {
+  int64_t num_matches = -1;
+  double max_overlap = -1;
+};
+
+struct Pt {
+  double x, y;
+};
+using Quad = std::array<Pt, 4>;
+
+// A pose's rotated template box (matching::box, src/matching/multi.hpp:50-55).
+Quad pose_box(const RectGeom& g, double row, double col, double angle) {
+  const double ca = std::cos(angle), sa = std::sin(angle);
+  const Pt c[4] = {{g.left, g.top}, {g.right, g.top}, {g.right, g.bottom}, {g.left, g.bottom}};
+  Quad q;
+  for (int i = 0; i < 4; ++i) q[size_t(i)] = {col + ca * c[i].x + sa * c[i].y, row - sa * c[i].x + ca * c[i].y};
+  return q;
+}
+
+struct Aabb {
+  double top, bottom, left, right;
+};
+Aabb aabb_of(const Quad& q) {
+  Aabb a{q[0].y, q[0].y, q[0].x, q[0].x};
+  for (const Pt& p : q) {
+    a.top = std::min(a.top, p.y);
+    a.bottom = std::max(a.bottom, p.y);
+    a.left = std::min(a.left, p.x);
+    a.right = std::max(a.right, p.x);
+  }
+  return a;
+}
+bool apart(const Aabb& a, const Aabb& b) {
+  return a.right < b.left || b.right < a.left || a.bottom < b.top || b.bottom < a.top;
+}
+
+double polygon_area(const Pt* p, size_t n) {
+  double a = 0;
+  for (size_t i = 0; i < n; ++i) {
+    const Pt& u = p[i];
+    const Pt& v = p[(i + 1) % n];
+    a += u.x * v.y - v.x * u.y;
+  }
+  return std::abs(a) * .5;
+}
+
+// Intersection area of two boxes over the smaller box's area
+// (matching::overlap, src/matching/multi.hpp:59-75): both boxes are moved to
+// a's first corner, then a is clipped by each edge of b (Sutherland-Hodgman).
+double box_overlap(Quad a, Quad b) {
+  const Pt o = a[0];
+  for (Pt& p : a) p = {p.x - o.x, p.y - o.y};
+  for (Pt& p : b) p = {p.x - o.x, p.y - o.y};
+  const double den = std::min(polygon_area(a.data(), 4), polygon_area(b.data(), 4));
+  if (den <= 1e-12) return 0;
+  std::array<Pt, 16> poly{}, next{};
+  std::copy(a.begin(), a.end(), poly.begin());
+  size_t n = 4;
+  auto side = [](Pt u, Pt v, Pt p) { return (v.x - u.x) * (p.y - u.y) - (v.y - u.y) * (p.x - u.x); };
+  for (int e = 0; e < 4 && n; ++e) {
+    const Pt u = b[size_t(e)], v = b[size_t((e + 1) % 4)];
+    size_t m = 0;
+    for (size_t i = 0; i < n; ++i) {
+      const Pt p = poly[i], q = poly[(i + 1) % n];
+      const double dp = side(u, v, p), dq = side(u, v, q);
+      if (dp >= 0) next[m++] = p;
+      if ((dp >= 0) != (dq >= 0)) {
+        const double t = dp / (dp - dq);
+        next[m++] = {p.x + t * (q.x - p.x), p.y + t * (q.y - p.y)};
+      }
+    }
+    poly = next;
+    n = m;
+  }
+  return std::clamp(polygon_area(poly.data(), n) / den, 0., 1.);
+}
+
+struct MultiCand {
+  Cand c;          // pose (refined once accepted)
+  int model;       // index into the caller's model list
+  int owner;       // model whose prepared query produced it
+  int local;       // index in the owner's candidate list
+};
+
+bool ranks_before(const MultiCand& a, const MultiCand& b) {
+  if (a.c.score != b.c.score) return a.c.score > b.c.score;
+  if (a.model != b.model) return a.model < b.model;
+  if (a.c.row != b.c.row) return a.c.row < b.c.row;
+  if (a.c.col != b.c.col) return a.c.col < b.c.col;
+  return a.c.angle < b.c.angle;
+}
+
+// Device refinement of host-chosen candidates, grouped by owner query, with
+// the results memoised per (owner, candidate).
+struct MultiRefiner {
+  Workspace& ws;
+  cudaStream_t s;
+  std::vector<std::unique_ptr<Prepared>>& preps;
+  std::vector<std::vector<Refined>> result;
+  std::vector<std::vector<uint8_t>> done;
+  DevBuf<Cand> d_cand;
+  DevBuf<Refined> d_ref;
+  DevBuf<int32_t> d_flag, d_iota;
+  static constexpr int kMax = 64;
+
+  MultiRefiner(Workspace& w, cudaStream_t st, std::vector<std::unique_ptr<Prepared>>& p)
+      : ws(w), s(st), preps(p), result(p.size()), done(p.size()) {
+    for (size_t i = 0; i < p.size(); ++i)
+      if (p[i]) {
+        result[i].resize(p[i]->cands.size());
+        done[i].assign(p[i]->cands.size(), 0);
+      }
+    d_cand.reserve(kMax);
+    d_ref.reserve(kMax);
+    d_flag.reserve(kMax);
+    d_iota.reserve(kMax);
+    std::vector<int32_t> iota(kMax);
+    for (int i = 0; i < kMax; ++i) iota[size_t(i)] = i;
+    d_iota.upload(iota, s);
+  }
+  bool has(const MultiCand& m) const { return done[size_t(m.owner)][size_t(m.local)] != 0; }
+  const Refined& get(const MultiCand& m) const { return result[size_t(m.owner)][size_t(m.local)]; }
+
+  // refines `batch` (at most kMax, none refined yet) in one launch per owner
+  void run(const std::vector<MultiCand>& batch) {
+    std::vector<MultiCand> order(batch);
+    std::stable_sort(order.begin(), order.end(), [](const MultiCand& a, const MultiCand& b) { return a.owner < b.owner; });
+    const size_t n = order.size();
+    std::vector<Cand> h(n);
+    for (size_t i = 0; i < n; ++i) h[i] = preps[size_t(order[i].owner)]->cands[size_t(order[i].local)];
+    check(cudaMemcpyAsync(d_cand.p, h.data(), n * sizeof(Cand), cudaMemcpyHostToDevice, s), "refine batch");
+    for (size_t i = 0; i < n;) {
+      size_t j = i;
+      while (j < n && order[j].owner == order[i].owner) ++j;
+      const Prepared& P = *preps[size_t(order[i].owner)];
+      RefineArgs ra = P.ra;
+      if (ra.img.pairs && ws.pairs_level != P.finest) ra.img.pairs = nullptr;  // another model's level
+      ra.sorted = d_cand.p + i;
+      ra.refined = d_ref.p + i;
+      ra.refined_flag = d_flag.p + i;
+      ra.batch = d_iota.p;
+      ra.batch_count = int(j - i);
+      {
+        Span sp(kStRefine, s);
+        check(launch_refine(ra, int(j - i), s), "refine");
+      }
+      i = j;
+    }
+    std::vector<Refined> r(n);
+    check(cudaMemcpyAsync(r.data(), d_ref.p, n * sizeof(Refined), cudaMemcpyDeviceToHost, s), "refined");
+    check(cudaStreamSynchronize(s), "refine");
+    for (size_t i = 0; i < n; ++i) {
+      result[size_t(order[i].owner)][size_t(order[i].local)] = r[i];
+      done[size_t(order[i].owner)][size_t(order[i].local)] = 1;
+    }
+  }
+};
+
+// matching::select_refined (src/matching/multi.hpp:79-119) over the pooled,
+// ranked candidates: per-model or shared quota and overlap threshold, an
+// overlap test before and after refinement (refinement may move the pose),
+// and the final ranking.  Refinement runs in speculative device batches: the
+// next candidates that would be refined next if no earlier one were
+// accepted.
+std::vector<MultiCand> select_models(std::vector<MultiCand> cands, const std::vector<FindParams>& opts,
+                                     const std::vector<RectGeom>& geoms, Selection sel, MultiRefiner* refiner) {
+  std::sort(cands.begin(), cands.end(), ranks_before);
+  std::vector<MultiCand> out;
+  std::vector<Quad> boxes;
+  std::vector<Aabb> bounds;
+  std::vector<size_t> counts(opts.size(), 0);
+  auto quota_full = [&](int m) {
+    const int64_t limit = sel.num_matches >= 0 ? sel.num_matches : opts[size_t(m)].num_matches;
+    return sel.num_matches < 0 && limit && counts[size_t(m)] >= uint64_t(limit);
+  };
+  auto threshold = [&](int m) { return sel.max_overlap >= 0 ? sel.max_overlap : opts[size_t(m)].max_overlap; };
+  auto suppressed = [&](int m, const Quad& q, const Aabb& a) {
+    const double thr = threshold(m) + 1e-12;
+    for (size_t i = 0; i < out.size(); ++i) {
+      if (sel.max_overlap < 0 && out[i].model != m) continue;
+      if (apart(a, bounds[i])) continue;
+      if (box_overlap(q, boxes[i]) > thr) return true;
+    }
+    return false;
+  };
+  for (size_t k = 0; k < cands.size(); ++k) {
+    MultiCand c = cands[k];
+    if (quota_full(c.model)) continue;
+    const RectGeom& g = geoms[size_t(c.model)];
+    Quad q = pose_box(g, c.c.row, c.c.col, c.c.angle);
+    Aabb a = aabb_of(q);
+    if (suppressed(c.model, q, a)) continue;
+    if (refiner) {
+      if (!refiner->has(c)) {
+        // speculative batch: this candidate and the next ones that pass the
+        // same tests now and are not mostly covered by one already queued
+        std::vector<MultiCand> batch{c};
+        std::vector<Aabb> queued{a};
+        const size_t want = sel.num_matches > 0 ? size_t(std::max<int64_t>(1, sel.num_matches - int64_t(out.size())))
+                                                : size_t(32);
+        for (size_t j = k + 1; j < cands.size() && batch.size() < std::min<size_t>(want, MultiRefiner::kMax); ++j) {
+          const MultiCand& o = cands[j];
+          if (refiner->has(o) || quota_full(o.model)) continue;
+          bool dup = false;
+          for (const MultiCand& b : batch) dup = dup || (b.owner == o.owner && b.local == o.local);
+          if (dup) continue;
+          const Quad oq = pose_box(geoms[size_t(o.model)], o.c.row, o.c.col, o.c.angle);
+          const Aabb oa = aabb_of(oq);
+          if (suppressed(o.model, oq, oa)) continue;
+          for (const Aabb& qa : queued) {
+            const double ix = std::min(oa.right, qa.right) - std::max(oa.left, qa.left);
+            const double iy = std::min(oa.bottom, qa.bottom) - std::max(oa.top, qa.top);
+            const double ao = (oa.right - oa.left) * (oa.bottom - oa.top), aq = (qa.right - qa.left) * (qa.bottom - qa.top);
+            if (ix > 0 && iy > 0 && ix * iy > .5 * std::min(ao, aq)) dup = true;
+          }
+          if (dup) continue;
+          batch.push_back(o);
+          queued.push_back(oa);
+        }
+        refiner->run(batch);
+      }
+      const Refined& r = refiner->get(c);
+      if (!r.ok) continue;
+      c.c.row = r.row;
+      c.c.col = r.col;
+      c.c.angle = r.angle;
+      c.c.score = r.score;
+      q = pose_box(g, c.c.row, c.c.col, c.c.angle);
+      a = aabb_of(q);
+      if (suppressed(c.model, q, a)) continue;
+    }
+    out.push_back(c);
+    boxes.push_back(q);
+    bounds.push_back(a);
+    ++counts[size_t(c.model)];
+    if (sel.num_matches > 0 && out.size() >= uint64_t(sel.num_matches)) break;
+  }
+  std::sort(out.begin(), out.end(), ranks_before);
+  return out;
+}
+
+// find_models (src/ncc_matching/matcher.cpp:1077-1124) with HALCON's quota
+// rule (per_model_quota_before_overlap = true, as mv_find_ncc_models calls
+// it): one prepared query per distinct (model, options), the candidates
+// pooled, selected and refined on the device.
+std::vector<MultiCand> run_find_models(const std::vector<mvg_ncc_model_s*>& models, const void* pixels, int type,
+                                       int64_t W, int64_t H, int64_t stride, int location,
+                                       const std::vector<FindParams>& opts, Selection sel, cudaStream_t user_stream) {
+  Workspace& ws = workspace();
+  cudaStream_t s = user_stream ? user_stream : ws.own_stream;
+  if (type != 0 && type != 1) raise(kTypeMismatch, "one byte or uint2 channel required");
+  if (!pixels) raise(kInvalidArgument, "image pixels must not be null");
+  const int64_t bpp = type == 1 ? 2 : 1;
+  if (W <= 0 || H <= 0 || W > std::numeric_limits<int>::max() || H > std::numeric_limits<int>::max() ||
+      H > 32000000 / W)
+    raise(kLimitExceeded, "search image exceeds pixel budget");
+  if (stride < W * bpp || stride % bpp) raise(kInvalidArgument, "invalid row stride");
+  // one upload of a host image for all models
+  const void* dev = pixels;
+  if (location == MVG_MEMORY_HOST) {
+    const size_t bytes = size_t(stride) * size_t(H - 1) + size_t(W * bpp);
+    ws.image.reserve(bytes);
+    Span sp(kStUpload, s, 0);
+    check(cudaMemcpyAsync(ws.image.p, pixels, bytes, cudaMemcpyHostToDevice, s), "image upload");
+    dev = ws.image.p;
+  }
+  const size_t n = models.size();
+  std::vector<int> owner(n);
+  std::vector<std::unique_ptr<Prepared>> preps(n);
+  auto same = [](const FindParams& a, const FindParams& b) {
+    return a.angle_start == b.angle_start && a.angle_extent == b.angle_extent && a.min_score == b.min_score &&
+           a.max_overlap == b.max_overlap && a.num_matches == b.num_matches && a.subpixel == b.subpixel &&
+           a.highest == b.highest && a.lowest == b.lowest;
+  };
+  std::vector<RectGeom> geoms(n);
+  for (size_t i = 0; i < n; ++i) {
+    const ModelLevel& b = models[i]->host.levels.front();
+    geoms[i] = RectGeom{-b.ocol - .5, double(b.width) - b.ocol - .5, -b.orow - .5, double(b.height) - b.orow - .5,
+                        double(b.width) * double(b.height)};
+    owner[i] = int(i);
+    for (size_t j = 0; j < i; ++j)
+      if (models[i] == models[j] && same(opts[i], opts[j])) {
+        owner[i] = owner[j];
+        break;
+      }
+    if (owner[i] != int(i)) continue;
+    preps[i] = std::make_unique<Prepared>();
+    run_find(*models[i], dev, type, W, H, stride, MVG_MEMORY_DEVICE, opts[i], s, -3, preps[i].get());
+  }
+  std::vector<MultiCand> pool;
+  for (size_t i = 0; i < n; ++i) {
+    const Prepared& P = *preps[size_t(owner[i])];
+    for (size_t k = 0; k < P.cands.size(); ++k)
+      if (std::isfinite(P.cands[k].score)) pool.push_back({P.cands[k], int(i), owner[i], int(k)});
+  }
+  MultiRefiner refiner(ws, s, preps);
+  const bool independent = sel.num_matches < 0 && sel.max_overlap >= 0 &&
+                           std::any_of(opts.begin(), opts.end(), [](const FindParams& q) { return q.num_matches > 0; });
+  std::vector<MultiCand> out = select_models(std::move(pool), opts, geoms, independent ? Selection{} : sel, &refiner);
+  if (independent) out = select_models(std::move(out), opts, geoms, sel, nullptr);
+  t_prof.collect();
+  t_prof.finds += 1;
   return out;
 }
 
@@ -1603,6 +1959,96 @@ int32_t mvg_find_ncc_model(const void* pixels, int32_t pixel_type, int64_t width
       if (column) column[i] = mt.col + .5 * (1 - c - s);
       if (angle) angle[i] = mt.angle;
       if (score) score[i] = mt.score;
+    }
+  });
+}
+
+int32_t mvg_find_ncc_models(const void* pixels, int32_t pixel_type, int64_t width, int64_t height, int64_t row_stride,
+                            int32_t location, const mvg_ncc_model* model_ids, int64_t num_models,
+                            const double* angle_start, int64_t n_angle_start, const double* angle_extent,
+                            int64_t n_angle_extent, const double* min_score, int64_t n_min_score,
+                            const int64_t* num_matches, int64_t n_num_matches, const double* max_overlap,
+                            int64_t n_max_overlap, const int32_t* subpixel, int64_t n_subpixel,
+                            const int32_t* num_levels, int64_t n_num_levels, double* row, double* column,
+                            double* angle, double* score, int64_t* model, int64_t capacity, int64_t* count,
+                            void* stream) {
+  return guarded([&] {
+    if (!count) raise(kInvalidArgument, "count must not be null");
+    *count = 0;
+    // ncc_models and NccControls (src/c_api/ncc_matching_api.cpp:112-162)
+    if (!model_ids || num_models <= 0 || num_models > 4096)
+      raise(kInvalidArgument, "one model or a nonempty model array (maximum 4096) required");
+    const size_t n = size_t(num_models);
+    std::vector<mvg_ncc_model_s*> models(n);
+    for (size_t i = 0; i < n; ++i) {
+      if (!model_ids[i]) raise(kTypeMismatch, "control handle is not an NCC model");
+      models[i] = model_ids[i];
+    }
+    auto card = [&](const void* p, int64_t k, const char* name) {
+      if (!p || (k != 1 && k != num_models))
+        raise(kInvalidArgument, std::string(name) + ": one value or one value per model required");
+    };
+    card(angle_start, n_angle_start, "AngleStart");
+    card(angle_extent, n_angle_extent, "AngleExtent");
+    card(min_score, n_min_score, "MinScore");
+    card(num_matches, n_num_matches, "NumMatches");
+    card(max_overlap, n_max_overlap, "MaxOverlap");
+    card(subpixel, n_subpixel, "SubPixel");
+    if (!num_levels ||
+        (n_num_levels != 1 && n_num_levels != 2 && n_num_levels != num_models && n_num_levels != 2 * num_models))
+      raise(kInvalidArgument, "NumLevels: highest level or shared/per-model level pairs required");
+    auto number = [&](const double* v, int64_t k, size_t i, double lo, double hi, const char* name) {
+      const double x = v[k == 1 ? 0 : i];
+      if (!std::isfinite(x) || x < lo || x > hi)
+        raise(kInvalidArgument, std::string(name) + ": numeric control outside allowed range");
+      return x;
+    };
+    std::vector<FindParams> opts(n);
+    for (size_t i = 0; i < n; ++i) {
+      FindParams& q = opts[i];
+      q.angle_start = number(angle_start, n_angle_start, i, -std::numeric_limits<double>::max(),
+                             std::numeric_limits<double>::max(), "AngleStart");
+      q.angle_extent = number(angle_extent, n_angle_extent, i, 0, 6.28318530717958647692, "AngleExtent");
+      q.min_score = number(min_score, n_min_score, i, 0, 1, "MinScore");
+      q.max_overlap = number(max_overlap, n_max_overlap, i, 0, 1, "MaxOverlap");
+      const int64_t quota = num_matches[n_num_matches == 1 ? 0 : i];
+      if (quota < 0) raise(kInvalidArgument, "NumMatches: match count must be nonnegative");
+      q.num_matches = quota;
+      const int32_t sp = subpixel[n_subpixel == 1 ? 0 : i];
+      if (sp != 0 && sp != 1) raise(kInvalidArgument, "SubPixel: expected true or false");
+      q.subpixel = sp != 0;
+      size_t hi_at = 0, lo_at = 0;
+      bool pair = false;
+      if (n_num_levels == num_models && num_models > 1) {
+        hi_at = i;
+      } else if (n_num_levels == 2 * num_models) {
+        hi_at = 2 * i;
+        lo_at = hi_at + 1;
+        pair = true;
+      } else if (n_num_levels == 2) {
+        lo_at = 1;
+        pair = true;
+      }
+      const int64_t highest = num_levels[hi_at], lowest = pair ? num_levels[lo_at] : 1;
+      if (highest < 0 || lowest < 0) raise(kInvalidArgument, "NumLevels: invalid highest/lowest level pair");
+      q.highest = int(highest);
+      q.lowest = int(std::max<int64_t>(1, lowest));
+    }
+    Selection sel;
+    sel.num_matches = n_num_matches == 1 ? opts.front().num_matches : -1;
+    sel.max_overlap = n_max_overlap == 1 ? opts.front().max_overlap : -1;
+    const std::vector<MultiCand> r = run_find_models(models, pixels, pixel_type, width, height, row_stride, location,
+                                                     opts, sel, static_cast<cudaStream_t>(stream));
+    *count = int64_t(r.size());
+    for (size_t i = 0; i < r.size() && int64_t(i) < capacity; ++i) {
+      // edge-centred pose convention (src/c_api/ncc_matching_api.cpp:171-176)
+      const Cand& c = r[i].c;
+      const double cs = std::cos(c.angle), sn = std::sin(c.angle);
+      if (row) row[i] = c.row + .5 * (1 - cs + sn);
+      if (column) column[i] = c.col + .5 * (1 - cs - sn);
+      if (angle) angle[i] = c.angle;
+      if (score) score[i] = c.score;
+      if (model) model[i] = r[i].model;
     }
   });
 }

@@ -1631,7 +1631,7 @@ constexpr int kRefineThreads = 512;
 __global__ void __launch_bounds__(kRefineThreads) refine_kernel(RefineArgs a) {
   __shared__ FitShared f;
   const int b = blockIdx.x;
-  if (b >= a.state->batch_count) return;
+  if (b >= (a.batch_count >= 0 ? a.batch_count : a.state->batch_count)) return;
   const int i = a.batch[b];
   if (threadIdx.x == 0) {
     f.c = a.sorted[i];

@@ -265,7 +265,8 @@ struct RefineArgs {
   Refined* refined;
   int32_t* refined_flag;
   const int32_t* batch;
-  const QueryState* state;
+  const QueryState* state;  // batch size in state->batch_count, unless
+  int batch_count;          // ... this is >= 0 (a host-chosen batch)
   double crop_row, crop_col, scale, phase;
   double angle_start, angle_end, angle_step, min_score;
   int rotate, subpixel, absolute, top, finest;

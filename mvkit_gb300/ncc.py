@@ -76,6 +76,9 @@ def load() -> C.CDLL:
     lib.mvg_read_ncc_model.argtypes = [C.c_char_p, C.POINTER(C.c_void_p)]
     lib.mvg_serialize_ncc_model.argtypes = [C.c_void_p, C.c_char_p, C.c_int64, _i64p]
     lib.mvg_deserialize_ncc_model.argtypes = [C.c_char_p, C.c_int64, C.POINTER(C.c_void_p)]
+    lib.mvg_find_ncc_models.argtypes = ([C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int32,
+                                        C.c_void_p, C.c_int64] + [C.c_void_p, C.c_int64] * 7 +
+                                       [C.c_void_p] * 5 + [C.c_int64, _i64p, C.c_void_p])
     lib.mvg_last_error.restype = C.c_char_p
     lib.mvg_host_alloc.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
     lib.mvg_host_free.argtypes = [C.c_void_p]
@@ -90,7 +93,7 @@ def load() -> C.CDLL:
     for name in ("mvg_create_ncc_model", "mvg_get_ncc_model_params", "mvg_clear_ncc_model", "mvg_find_ncc_model",
                  "mvg_find_ncc_model_stage", "mvg_ncc_pyramid_level", "mvg_host_alloc", "mvg_host_free",
                  "mvg_device_alloc", "mvg_device_free", "mvg_copy_to_device", "mvg_write_ncc_model", "mvg_read_ncc_model",
-                 "mvg_serialize_ncc_model", "mvg_deserialize_ncc_model"):
+                 "mvg_serialize_ncc_model", "mvg_deserialize_ncc_model", "mvg_find_ncc_models"):
         getattr(lib, name).restype = C.c_int32
     _LIB = lib
     return lib
@@ -359,6 +362,79 @@ def find_ncc_model(image, model: NccModel, angle_start, angle_extent, min_score,
         _check(lib.mvg_find_ncc_model(ptr, typ, w, h, stride, loc, model.handle, *ctl,
                                       *[o.ctypes.data_as(_dp) for o in out], cap, C.byref(cnt),
                                       C.c_void_p(stream) if stream else None), op)
+        if cnt.value <= cap:
+            return tuple(o[: cnt.value] for o in out)
+        cap = int(cnt.value)
+
+
+def find_ncc_models(image, models, angle_start, angle_extent, min_score, num_matches, max_overlap, subpixel,
+                    num_levels, stream=None):
+    """FindNccModels (src/c_api/ncc_matching_api.cpp:191-201).
+
+    models: one NccModel or a sequence of 1..4096.  Each control takes one
+    value (shared) or one per model; num_levels takes 1, 2, len(models) or
+    2*len(models) values.  Returns (Row, Column, Angle, Score, Model), Model
+    being the index into `models`."""
+    op = "find_ncc_models"
+    ms = list(models) if isinstance(models, (list, tuple)) else [models]
+    if not ms or len(ms) > 4096:
+        raise MvError(MV_STATUS_INVALID_ARGUMENT, "one model or a nonempty model array (maximum 4096) required", op)
+    for m in ms:
+        if not isinstance(m, NccModel) or not m.handle:
+            raise MvError(MV_STATUS_TYPE_MISMATCH, "control handle is not an NCC model", op)
+    n = len(ms)
+
+    def per(x, name):
+        v = _values(x, op, name)
+        if len(v) not in (1, n):
+            raise MvError(MV_STATUS_INVALID_ARGUMENT, "one value or one value per model required", op)
+        return v
+
+    def numbers(x, name):
+        out = []
+        for v in per(x, name):
+            out.append(_number(v, op, name))
+        return np.array(out, dtype=np.float64)
+
+    starts, extents = numbers(angle_start, "AngleStart"), numbers(angle_extent, "AngleExtent")
+    scores, overlaps = numbers(min_score, "MinScore"), numbers(max_overlap, "MaxOverlap")
+    quotas = np.array([_integer(v, op, "NumMatches") for v in per(num_matches, "NumMatches")], dtype=np.int64)
+    modes = []
+    for v in per(subpixel, "SubPixel"):
+        if not isinstance(v, str):
+            raise MvError(MV_STATUS_TYPE_MISMATCH, "SubPixel: string control value required", op)
+        if v not in ("true", "false"):
+            raise MvError(MV_STATUS_INVALID_ARGUMENT, "expected true or false", op)
+        modes.append(1 if v == "true" else 0)
+    modes = np.array(modes, dtype=np.int32)
+    lv = _values(num_levels, op, "NumLevels")
+    if len(lv) not in (1, 2, n, 2 * n):
+        raise MvError(MV_STATUS_INVALID_ARGUMENT, "highest level or shared/per-model level pairs required", op)
+    levels = np.array([_integer(v, op, "NumLevels") for v in lv], dtype=np.int64)
+    if (levels < 0).any() or (levels > 2**31 - 1).any():
+        raise MvError(MV_STATUS_INVALID_ARGUMENT, "invalid highest/lowest level pair", op)
+    levels = levels.astype(np.int32)
+    if isinstance(image, DeviceImage):
+        ptr, typ, (h, w), stride, loc = image.ptr, image.type, image.shape, image.stride, 1
+    else:
+        a, typ = _image(image, op, "Image")
+        if a.size == 0:
+            e = np.zeros(0)
+            return e, e.copy(), e.copy(), e.copy(), np.zeros(0, dtype=np.int64)
+        ptr, (h, w), stride, loc = a.ctypes.data, a.shape, a.strides[0], 0
+    ids = (C.c_void_p * n)(*[m.handle for m in ms])
+    lib = load()
+    cap = max(64, int(quotas.sum()))
+    arrs = (starts, extents, scores, quotas, overlaps, modes, levels)
+    args = []
+    for arr in arrs:
+        args += [arr.ctypes.data, len(arr)]
+    while True:
+        out = [np.zeros(cap) for _ in range(4)] + [np.zeros(cap, dtype=np.int64)]
+        cnt = C.c_int64()
+        _check(lib.mvg_find_ncc_models(ptr, typ, w, h, stride, loc, ids, n, *args,
+                                       *[o.ctypes.data for o in out], cap, C.byref(cnt),
+                                       C.c_void_p(stream) if stream else None), op)
         if cnt.value <= cap:
             return tuple(o[: cnt.value] for o in out)
         cap = int(cnt.value)

@@ -205,6 +205,64 @@ def make_workload(seed: int, height: int, width: int, tsize: int, n_poses: int,
     return Workload(image=image, template=tmpl_i.astype(dtype), poses=poses, maxval=maxval)
 
 
+@dataclass
+class MultiWorkload:
+    image: np.ndarray
+    templates: list              # one square template per model
+    poses: list                  # per template, its ground-truth Pose list
+    maxval: int = 255
+
+    def digest(self) -> str:
+        h = hashlib.sha256()
+        h.update(np.ascontiguousarray(self.image).tobytes())
+        for t in self.templates:
+            h.update(np.ascontiguousarray(t).tobytes())
+        return h.hexdigest()[:16]
+
+
+def make_multi_workload(seed: int, height: int, width: int, tsizes: tuple, n_poses: tuple,
+                        angle_range: tuple = (0.0, 0.0), noise_sigma: int = 3, shapes: int = 40,
+                        maxval: int = 255) -> MultiWorkload:
+    """One scene holding several different templates (FindNccModels): template
+    k (side tsizes[k], cropped from its own source scene) is pasted n_poses[k]
+    times; no two pastes overlap."""
+    dtype = np.uint8 if maxval <= 255 else np.uint16
+    templates = []
+    for k, ts in enumerate(tsizes):
+        rng_t = np.random.default_rng([seed, 100 + k])
+        src = scene(seed * 7919 + 31 * k + 5, max(2 * ts, 64), max(2 * ts, 64), shapes=max(8, shapes // 4),
+                    maxval=maxval)
+        ty = int(rng_t.integers(0, src.shape[0] - ts + 1))
+        tx = int(rng_t.integers(0, src.shape[1] - ts + 1))
+        t = src[ty:ty + ts, tx:tx + ts]
+        templates.append(np.clip(t + _gauss_int(rng_t, t.shape, noise_sigma), 0, maxval))
+    rng = np.random.default_rng([seed, 3])
+    img = scene(seed, height, width, shapes=shapes, maxval=maxval)
+    placed = []  # (row, col, diag)
+    poses = [[] for _ in tsizes]
+    for k, ts in enumerate(tsizes):
+        diag = math.hypot(ts, ts)
+        margin = diag / 2.0 + 8
+        tries = 0
+        while len(poses[k]) < n_poses[k]:
+            tries += 1
+            if tries > 10000:
+                raise ValueError("cannot place the requested poses without overlap")
+            row = margin + float(rng.integers(0, 1 << 20)) / (1 << 20) * (height - 1 - 2 * margin)
+            col = margin + float(rng.integers(0, 1 << 20)) / (1 << 20) * (width - 1 - 2 * margin)
+            lo, hi = angle_range
+            ang = lo + float(rng.integers(0, 1 << 20)) / (1 << 20) * (hi - lo)
+            if all(math.hypot(row - r, col - c) > (diag + d) / 2 + 4 for r, c, d in placed):
+                poses[k].append(Pose(row, col, ang, 1.0))
+                placed.append((row, col, diag))
+    for k, t in enumerate(templates):
+        tf = t.astype(np.float64)
+        for p in poses[k]:
+            paste(img, tf, p)
+    image = _finish(img, rng, noise_sigma, maxval, dtype)
+    return MultiWorkload(image=image, templates=[t.astype(dtype) for t in templates], poses=poses, maxval=maxval)
+
+
 # Named workloads.  "find_640x480_t64" is the CPU-runnable case; "find_2048_t128_5x"
 # is the single-GPU throughput case.
 CONFIGS = {

@@ -184,6 +184,50 @@ int ref_ncc_find(void* model, const void* img, int type, std::int64_t w, std::in
   });
 }
 
+// Runs the reference multi-model find (mv::ncc_matching::find_models,
+// src/ncc_matching/matcher.cpp:1077) as mv_find_ncc_models calls it
+// (src/c_api/ncc_matching_api.cpp:191-201): per-model options (arrays of
+// `count`), the shared selection (num_matches / max_overlap, -1 = per model)
+// and HALCON's quota-before-overlap rule.  out is capacity x 5 doubles (row,
+// column, angle, score, model index) in the matcher's pixel-centre convention.
+int ref_ncc_find_models(void* const* models, std::int64_t count, const void* img, int type, std::int64_t w,
+                        std::int64_t h, std::int64_t stride, const double* angle_start,
+                        const double* angle_extent, const double* min_score, const std::int64_t* num_matches,
+                        const double* max_overlap, const int* subpixel, const int* highest, const int* lowest,
+                        std::int64_t sel_num_matches, double sel_max_overlap, double* out, std::int64_t capacity,
+                        std::int64_t* found_count, char* err, int errlen) {
+  *found_count = 0;
+  return guarded(err, errlen, [&] {
+    std::vector<const ncc::Model*> ms;
+    std::vector<ncc::FindOptions> opts;
+    for (std::int64_t i = 0; i < count; ++i) {
+      ms.push_back(static_cast<const ncc::Model*>(models[i]));
+      ncc::FindOptions o;
+      o.angle_start = angle_start[i];
+      o.angle_extent = angle_extent[i];
+      o.min_score = min_score[i];
+      o.num_matches = std::size_t(num_matches[i]);
+      o.max_overlap = max_overlap[i];
+      o.subpixel = subpixel[i] != 0;
+      o.highest_level = highest[i];
+      o.lowest_level = lowest[i] < 1 ? 1 : lowest[i];
+      opts.push_back(o);
+    }
+    mv::matching::Selection sel;
+    sel.num_matches = sel_num_matches;
+    sel.max_overlap = sel_max_overlap;
+    const auto found = ncc::find_models(make_image(img, type, w, h, stride, nullptr), ms, opts, sel, true);
+    *found_count = std::int64_t(found.size());
+    for (std::size_t i = 0; i < found.size() && std::int64_t(i) < capacity; ++i) {
+      out[5 * i + 0] = found[i].pose.row;
+      out[5 * i + 1] = found[i].pose.column;
+      out[5 * i + 2] = found[i].pose.angle;
+      out[5 * i + 3] = found[i].pose.score;
+      out[5 * i + 4] = double(found[i].model_index);
+    }
+  });
+}
+
 double ref_normalized_correlation(const double* a, const double* b, std::int64_t n, int absolute) {
   return ncc::normalized_correlation({a, std::size_t(n)}, {b, std::size_t(n)}, absolute != 0);
 }

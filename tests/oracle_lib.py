@@ -77,6 +77,33 @@ class Checker:
             self._deser.argtypes = [C.c_char_p, C.c_int64, C.POINTER(C.c_void_p), C.c_char_p, C.c_int]
             self._deser.restype = C.c_int
 
+    # -- multi-model find (reference only: mv::ncc_matching::find_models)
+    def find_models(self, models, image, opts, sel_num_matches, sel_max_overlap, capacity=4096):
+        img = np.ascontiguousarray(image)
+        typ = 1 if img.dtype == np.uint16 else 0
+        n = len(models)
+        f = self.lib.ref_ncc_find_models
+        f.argtypes = [C.POINTER(C.c_void_p), C.c_int64, C.c_void_p, C.c_int, C.c_int64, C.c_int64, C.c_int64,
+                      _dp, _dp, _dp, _i64p, _dp, _i32p, _i32p, _i32p, C.c_int64, C.c_double, _dp, C.c_int64,
+                      _i64p, C.c_char_p, C.c_int]
+        f.restype = C.c_int
+        hs = (C.c_void_p * n)(*[m.handle for m in models])
+        col = lambda k, dt: np.ascontiguousarray([o[k] for o in opts], dtype=dt)
+        a0, ae, ms, mo = col("angle_start", np.float64), col("angle_extent", np.float64), \
+            col("min_score", np.float64), col("max_overlap", np.float64)
+        nm = col("num_matches", np.int64)
+        sp, hi, lo = col("subpixel", np.int32), col("highest", np.int32), col("lowest", np.int32)
+        out = np.zeros((capacity, 5))
+        cnt = C.c_int64()
+        err = C.create_string_buffer(256)
+        st = f(hs, n, img.ctypes.data, typ, img.shape[1], img.shape[0], img.strides[0],
+               a0.ctypes.data_as(_dp), ae.ctypes.data_as(_dp), ms.ctypes.data_as(_dp), nm.ctypes.data_as(_i64p),
+               mo.ctypes.data_as(_dp), sp.ctypes.data_as(_i32p), hi.ctypes.data_as(_i32p), lo.ctypes.data_as(_i32p),
+               int(sel_num_matches), float(sel_max_overlap), out.ctypes.data_as(_dp), capacity, C.byref(cnt), err, 256)
+        if st != 0:
+            raise CheckerError(st, err.value.decode())
+        return out[: min(cnt.value, capacity)].copy()
+
     # -- model files (reference only: mv::ncc_matching::serialize/deserialize)
     def serialize(self, model) -> bytes:
         err = C.create_string_buffer(256)

@@ -15,6 +15,7 @@ import pytest
 
 import oracle_lib
 from golden.cases import CASES, LARGE, make_inputs
+from golden.multi_cases import MULTI_CASES, make_multi_inputs
 
 pytestmark = pytest.mark.gpu
 
@@ -93,6 +94,52 @@ def test_find_with_model_from_file(mg, name, tmp_path):
         mg.write_ncc_model(gpu_model(mg, case, wl, mask), str(path))
     model = mg.read_ncc_model(str(path))
     assert_same_matches(gpu_find(mg, model, wl.image, case), GOLDEN[name]["matches"], name)
+
+
+MULTI = json.loads((Path(__file__).parent / "golden" / "multi.json").read_text())["cases"]
+
+
+def multi_models(mg, case, wl):
+    models = []
+    for spec in case["models"]:
+        if "same" in spec:
+            models.append(models[spec["same"]])
+            continue
+        c = spec["create"]
+        models.append(mg.create_ncc_model(wl.templates[spec["t"]], c["levels"], c["angle_start"], c["angle_extent"],
+                                          "auto", "use_polarity"))
+    return models
+
+
+@pytest.mark.parametrize("name", sorted(MULTI_CASES))
+def test_find_models_matches_reference(mg, name):
+    """FindNccModels: same matches, order and model indices as the
+    reference's find_models on the same control tuples."""
+    case = MULTI_CASES[name]
+    wl = make_multi_inputs(case)
+    assert wl.digest() == MULTI[name]["digest"]
+    models = multi_models(mg, case, wl)
+    f = case["find"]
+    got = mg.find_ncc_models(wl.image, models, f["angle_start"], f["angle_extent"], f["min_score"],
+                             f["num_matches"], f["max_overlap"], f["subpixel"], f["num_levels"])
+    want = np.array(MULTI[name]["matches"]).reshape(-1, 5)
+    assert list(got[4]) == [int(x) for x in want[:, 4]], f"{name}: model indices {list(got[4])} vs {want[:, 4]}"
+    assert_same_matches(got[:4], want[:, :4], name)
+
+
+def test_find_models_single_equals_find(mg):
+    """One model through FindNccModels gives FindNccModel's matches."""
+    case = CASES["rot3_all"]
+    wl, mask = make_inputs(case)
+    model = gpu_model(mg, case, wl, mask)
+    f = case["find"]
+    one = gpu_find(mg, model, wl.image, case)
+    many = mg.find_ncc_models(wl.image, [model], f["angle_start"], f["angle_extent"], f["min_score"],
+                              f["num_matches"], f["max_overlap"], "true" if f["subpixel"] else "false",
+                              [f["highest"], f["lowest"]])
+    assert list(many[4]) == [0] * len(one[0])
+    for a, b in zip(one, many[:4]):
+        np.testing.assert_array_equal(a, b)
 
 
 def test_find_matches_reference_2048(mg):
