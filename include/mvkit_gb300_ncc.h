@@ -6,7 +6,8 @@
  * double arrays.  Status codes are the reference's MvStatus values
  * (include/mvkit/c/mv_status.h:12-24): 0 ok, -1 invalid argument,
  * -3 type mismatch, -5 out of memory, -6 unsupported, -7 invalid state,
- * -103 limit exceeded, -1000 internal error.  On failure the thread-local
+ * -100 I/O error, -101 decode error, -103 limit exceeded, -1000 internal
+ * error.  On failure the thread-local
  * message of mvg_last_error() says why (reference: mv_get_last_error,
  * include/mvkit/c/mv_api.h:75).  No call throws across the ABI.
  *
@@ -88,9 +89,13 @@ MVG_API int32_t mvg_clear_ncc_model(mvg_ncc_model model_id);
  * entries each) in the operator's convention (edge-centred translation,
  * src/c_api/ncc_matching_api.cpp:171-176); *count receives the number of
  * matches (entries beyond capacity are dropped).  stream: a cudaStream_t or
- * NULL for the library's per-thread stream. */
+ * NULL for the library's per-thread stream.  domain: the search image's
+ * domain (the reference image object's reduced domain, image.domain() in
+ * src/ncc_matching/matcher.cpp:375-393) as width x height bytes in host
+ * memory, nonzero inside, or NULL for the whole image; only poses whose
+ * nearest pixel lies in it are returned. */
 MVG_API int32_t mvg_find_ncc_model(const void* pixels, int32_t pixel_type, int64_t width, int64_t height,
-                           int64_t row_stride, int32_t location, mvg_ncc_model model_id,
+                           int64_t row_stride, int32_t location, const uint8_t* domain, mvg_ncc_model model_id,
                            double angle_start, double angle_extent, double min_score, int64_t num_matches,
                            double max_overlap, int32_t subpixel, int32_t highest_level, int32_t lowest_level,
                            double* row, double* column, double* angle, double* score, int64_t capacity,
@@ -106,10 +111,12 @@ MVG_API int32_t mvg_find_ncc_model(const void* pixels, int32_t pixel_type, int64
  * subpixel values are 0/1.  A shared NumMatches / MaxOverlap (one value) is a
  * limit / suppression over all models; per-model values apply per model,
  * and with a shared MaxOverlap the per-model quotas are applied before the
- * cross-model suppression (HALCON's rule, as the reference).  Outputs as
- * mvg_find_ncc_model plus model[i], the index into model_ids. */
+ * cross-model suppression (HALCON's rule, as the reference).  domain as
+ * for mvg_find_ncc_model.  Outputs as mvg_find_ncc_model plus model[i], the
+ * index into model_ids. */
 MVG_API int32_t mvg_find_ncc_models(const void* pixels, int32_t pixel_type, int64_t width, int64_t height,
-                                    int64_t row_stride, int32_t location, const mvg_ncc_model* model_ids,
+                                    int64_t row_stride, int32_t location, const uint8_t* domain,
+                                    const mvg_ncc_model* model_ids,
                                     int64_t num_models, const double* angle_start, int64_t n_angle_start,
                                     const double* angle_extent, int64_t n_angle_extent, const double* min_score,
                                     int64_t n_min_score, const int64_t* num_matches, int64_t n_num_matches,
@@ -125,7 +132,8 @@ MVG_API int32_t mvg_find_ncc_models(const void* pixels, int32_t pixel_type, int6
  * step; 100 = scored and sorted full-resolution candidates; -1 = final
  * matches.  out holds capacity x 4 doubles (row, column, angle, score). */
 MVG_API int32_t mvg_find_ncc_model_stage(const void* pixels, int32_t pixel_type, int64_t width, int64_t height,
-                                 int64_t row_stride, int32_t location, mvg_ncc_model model_id,
+                                 int64_t row_stride, int32_t location, const uint8_t* domain,
+                                 mvg_ncc_model model_id,
                                  double angle_start, double angle_extent, double min_score,
                                  int64_t num_matches, double max_overlap, int32_t subpixel,
                                  int32_t highest_level, int32_t lowest_level, int32_t stage, double* out,

@@ -336,19 +336,20 @@ template <class Pred> void clip_decreasing(int& lo, int& hi, Pred above_max) {
   hi = a;
 }
 
-// Position interval on a level where the pose lies in the search domain as
-// the reference tests it (may_contain, matcher.cpp:507-534; full image
-// domain) and, optionally, inside [base_lo, base_hi).
-void pose_interval(int& lo, int& hi, double crop, double step, double o, double off, double extent_max) {
+// Position interval on a level where the pose lies in the search domain's
+// bounding box [box_lo, box_hi] as the reference tests it (may_contain,
+// matcher.cpp:507-534).  For the full image that is the whole test; a
+// reduced domain is tested per pose on the device as well.
+void pose_interval(int& lo, int& hi, double crop, double step, double o, double off, double box_lo, double box_hi) {
   auto pose = [&](int r) { return crop + step * (r + o) + off; };
   if (step == 1) {
-    // domain_contains: 0 <= floor(pose + .5) <= extent_max
-    clip_increasing(lo, hi, [&](int r) { return std::floor(pose(r) + .5) < 0; });
-    clip_decreasing(lo, hi, [&](int r) { return std::floor(pose(r) + .5) > extent_max; });
+    // domain_contains: box_lo <= floor(pose + .5) <= box_hi
+    clip_increasing(lo, hi, [&](int r) { return std::floor(pose(r) + .5) < box_lo; });
+    clip_decreasing(lo, hi, [&](int r) { return std::floor(pose(r) + .5) > box_hi; });
   } else {
     const double margin = 2 * step;
-    clip_increasing(lo, hi, [&](int r) { return pose(r) < 0 - margin; });
-    clip_decreasing(lo, hi, [&](int r) { return pose(r) > extent_max + margin; });
+    clip_increasing(lo, hi, [&](int r) { return pose(r) < box_lo - margin; });
+    clip_decreasing(lo, hi, [&](int r) { return pose(r) > box_hi + margin; });
   }
   if (hi < lo) hi = lo;
 }
@@ -590,6 +591,9 @@ struct Workspace {
   DevBuf<int2> coarse_rc;
   DevBuf<uint32_t> pairs;            // fp16 pairs of the finest level
   int pairs_level = -1;              // the level `pairs` holds
+  DevBuf<uint8_t> dom_mask;          // search domain of the current find
+  DevBuf<int32_t> dom_count, dom_row_run;
+  DevBuf<int4> dom_runs;
   DevBuf<uint16_t> tc_planes;
   DevBuf<int32_t> tc_order, tc_counts, tc_offsets, tc_cursor;
   DevBuf<TcTiles> tc_tiles;
@@ -746,6 +750,45 @@ void fetch_stage(Workspace& ws, cudaStream_t s, const Cand* src, int slot, FindO
   for (const Cand& c : h) out.stage.push_back({c.row, c.col, c.angle, c.score});
 }
 
+// The caller's search domain (a W x H mask, nonzero inside) as the
+// reference's region: runs in (row, begin) order, first run per row, area,
+// bounding box and the sparse flag of matcher.cpp:505.
+struct DomainHost {
+  std::vector<int4> runs;
+  std::vector<int32_t> row_run;
+  int64_t area = 0;
+  int64_t rmin = 0, rmax = -1, cmin = 0, cmax = -1;
+  bool sparse = false;
+};
+
+DomainHost scan_domain(const uint8_t* mask, int64_t W, int64_t H) {
+  DomainHost d;
+  d.row_run.resize(size_t(H) + 1);
+  d.rmin = H;
+  d.cmin = W;
+  for (int64_t r = 0; r < H; ++r) {
+    d.row_run[size_t(r)] = int32_t(d.runs.size());
+    const uint8_t* row = mask + r * W;
+    int64_t c = 0;
+    while (c < W) {
+      while (c < W && !row[c]) ++c;
+      if (c >= W) break;
+      const int64_t b = c;
+      while (c < W && row[c]) ++c;
+      d.runs.push_back(make_int4(int(r), int(b), int(c - 1), 0));
+      d.area += c - b;
+      d.rmin = std::min(d.rmin, r);
+      d.rmax = std::max(d.rmax, r);
+      d.cmin = std::min(d.cmin, b);
+      d.cmax = std::max(d.cmax, c - 1);
+    }
+  }
+  d.row_run[size_t(H)] = int32_t(d.runs.size());
+  if (d.area)
+    d.sparse = double(d.area) < .7 * double(d.rmax - d.rmin + 1) * double(d.cmax - d.cmin + 1);
+  return d;
+}
+
 // One model's query prepared for a multi-model selection
 // (matcher.cpp:1077-1101): its sorted candidates with finite scores and what
 // refining one of them needs.  The refinement reads the workspace's pyramid,
@@ -757,13 +800,18 @@ struct Prepared {
   std::vector<Cand> cands;
   DevBuf<int32_t> plist0;      // own copies of the level-0 query tables
   DevBuf<PosRange> ranges0;
+  // with a reduced domain each model crops the image differently: own
+  // copies of the refinement's images
+  bool owned = false;
+  DevBuf<float> lev0, fine;
+  DevBuf<uint32_t> pairs;
 };
 
 // One find on the current device.  stage >= 0 stops after that stage and
 // returns its candidate list.  With `prep`, the find stops after the sort and
 // fills *prep instead of selecting.
 FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W, int64_t H, int64_t stride,
-                    int location, const FindParams& req, cudaStream_t user_stream, int stage,
+                    int location, const uint8_t* domain, const FindParams& req, cudaStream_t user_stream, int stage,
                     Prepared* prep = nullptr) {
   FindOutput out;
   const HostModel& hm = m.host;
@@ -792,16 +840,28 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   const int64_t bpp = type == 1 ? 2 : 1;
   if (stride < W * bpp || stride % bpp) raise(kInvalidArgument, "invalid row stride");
 
-  // crop with halo on the pyramid lattice (matcher.cpp:383-393), full domain
+  // search domain (matcher.cpp:375-382): the whole image, or the caller's
+  // mask; an empty domain finds nothing
+  DomainHost dh;
+  if (domain) {
+    dh = scan_domain(domain, W, H);
+    if (dh.area == 0) return out;
+  } else {
+    dh.rmin = 0;
+    dh.rmax = H - 1;
+    dh.cmin = 0;
+    dh.cmax = W - 1;
+  }
+  // crop of the domain's box with halo on the pyramid lattice (matcher.cpp:383-393)
   const ModelLevel& base = hm.levels.front();
   const double radius = std::hypot(std::max(base.orow, double(base.height - 1) - base.orow),
                                    std::max(base.ocol, double(base.width - 1) - base.ocol));
   const int64_t lattice = int64_t(size_t{1} << (level_count - 1));
   const int64_t halo = int64_t(std::ceil(radius)) + 4 * lattice;
-  const int64_t crop_row = std::max<int64_t>(0, 0 - halo) / lattice * lattice;
-  const int64_t crop_col = std::max<int64_t>(0, 0 - halo) / lattice * lattice;
-  const int64_t crop_bottom = std::min<int64_t>(H, ((H - 1 + halo) / lattice + 1) * lattice);
-  const int64_t crop_right = std::min<int64_t>(W, ((W - 1 + halo) / lattice + 1) * lattice);
+  const int64_t crop_row = std::max<int64_t>(0, dh.rmin - halo) / lattice * lattice;
+  const int64_t crop_col = std::max<int64_t>(0, dh.cmin - halo) / lattice * lattice;
+  const int64_t crop_bottom = std::min<int64_t>(H, ((dh.rmax + halo) / lattice + 1) * lattice);
+  const int64_t crop_right = std::min<int64_t>(W, ((dh.cmax + halo) / lattice + 1) * lattice);
 
   Workspace& ws = workspace();
   cudaStream_t s = user_stream ? user_stream : ws.own_stream;
@@ -863,15 +923,17 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
       if (li == top) {
         // coarse scan bounds (matcher.cpp:549-553)
         const double margin = step == 1 ? .5 : 2 * step;
-        rg.r0 = std::max(rg.r0, int(std::ceil((0 - margin - double(crop_row) - off) / step - d.orow)));
-        rg.r1 = std::min(rg.r1, int(std::floor((Hd - 1 + margin - double(crop_row) - off) / step - d.orow)) + 1);
-        rg.c0 = std::max(rg.c0, int(std::ceil((0 - margin - double(crop_col) - off) / step - d.ocol)));
-        rg.c1 = std::min(rg.c1, int(std::floor((Wd - 1 + margin - double(crop_col) - off) / step - d.ocol)) + 1);
+        rg.r0 = std::max(rg.r0, int(std::ceil((double(dh.rmin) - margin - double(crop_row) - off) / step - d.orow)));
+        rg.r1 = std::min(rg.r1,
+                         int(std::floor((double(dh.rmax) + margin - double(crop_row) - off) / step - d.orow)) + 1);
+        rg.c0 = std::max(rg.c0, int(std::ceil((double(dh.cmin) - margin - double(crop_col) - off) / step - d.ocol)));
+        rg.c1 = std::min(rg.c1,
+                         int(std::floor((double(dh.cmax) + margin - double(crop_col) - off) / step - d.ocol)) + 1);
       }
       if (rg.r1 < rg.r0) rg.r1 = rg.r0;
       if (rg.c1 < rg.c0) rg.c1 = rg.c0;
-      pose_interval(rg.r0, rg.r1, double(crop_row), step, d.orow, off, Hd - 1);
-      pose_interval(rg.c0, rg.c1, double(crop_col), step, d.ocol, off, Wd - 1);
+      pose_interval(rg.r0, rg.r1, double(crop_row), step, d.orow, off, double(dh.rmin), double(dh.rmax));
+      pose_interval(rg.c0, rg.c1, double(crop_col), step, d.ocol, off, double(dh.cmin), double(dh.cmax));
       plan[li].ranges.push_back(rg);
     }
   }
@@ -1071,6 +1133,31 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   }
   check(cudaMemsetAsync(ws.state.p, 0, sizeof(QueryState), s), "memset");
 
+  // search domain on the device (reduced domains only)
+  DomainView dv{};
+  dv.w = int(W);
+  dv.h = int(H);
+  dv.rmin = double(dh.rmin);
+  dv.rmax = double(dh.rmax);
+  dv.cmin = double(dh.cmin);
+  dv.cmax = double(dh.cmax);
+  if (domain) {
+    const size_t px = size_t(W) * size_t(H);
+    ws.dom_mask.reserve(px);
+    check(cudaMemcpyAsync(ws.dom_mask.p, domain, px, cudaMemcpyHostToDevice, s), "domain");
+    ws.dom_runs.upload(dh.runs, s);
+    ws.dom_row_run.upload(dh.row_run, s);
+    dv.mask = ws.dom_mask.p;
+    dv.runs = ws.dom_runs.p;
+    dv.row_run = ws.dom_row_run.p;
+    dv.sparse = dh.sparse;
+    if (dh.sparse) {
+      ws.dom_count.reserve((size_t(W) + 1) * (size_t(H) + 1));
+      check(launch_domain_count(ws.dom_mask.p, int(W), int(H), ws.dom_count.p, s), "domain count");
+      dv.count = ws.dom_count.p;
+    }
+  }
+
   // pyramid (levels finest..top as needed; level 0 always feeds the rest)
   LevelImage lev[kMaxLevels];
   for (size_t l = 0; l < level_count; ++l) {
@@ -1173,6 +1260,11 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     cs.group_of_src = d_co_gsrc;
     cs.planes = ws.planes.p;
     cs.absolute = hm.params.ignore_polarity;
+    cs.dom = dv;
+    cs.crop_row = double(crop_row);
+    cs.crop_col = double(crop_col);
+    cs.scale = scale;
+    cs.phase = phase;
     Span sp(kStCoarse, s);
     check(launch_coarse_tc_score(cs, s), "coarse tc score");
   }
@@ -1186,6 +1278,11 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     ca.planes = ws.planes.p;
     ca.absolute = hm.params.ignore_polarity;
     ca.skip = d_co_skip;
+    ca.dom = dv;
+    ca.crop_row = double(crop_row);
+    ca.crop_col = double(crop_col);
+    ca.scale = scale;
+    ca.phase = phase;
     {
       Span sp(kStCoarse, s);
       const cudaError_t e = launch_coarse(ca, max_bh, max_bw, s, ws.smem_optin);
@@ -1258,6 +1355,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
       ta.tc_dots = nullptr;
       ta.tc_group_of_src = nullptr;
       ta.tc_groups = nullptr;
+      ta.dom = dv;
       if (tc[t]) {
         const TcPlan& P = *tc[t];
         const int ng = int(P.groups.size());
@@ -1326,6 +1424,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     da.snap = snap;
     da.height = Hd;
     da.width = Wd;
+    da.dom = dv;
     {
       Span sp(kStDedup, s, snap ? 2 : 1);
       check(launch_dedup(da, kMaxCandidates, s), "dedup");
@@ -1438,6 +1537,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   ra.finest = int(finest);
   ra.height = Hd;
   ra.width = Wd;
+  ra.dom = dv;
   ra.geom = geom;
   if (prep) {
     // multi-model selection: the sorted list to the host, the level-0 query
@@ -1459,8 +1559,27 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     if (!plan[0].ranges.empty())
       check(cudaMemcpyAsync(prep->ranges0.p, d_ranges[0], plan[0].ranges.size() * sizeof(PosRange),
                             cudaMemcpyDeviceToDevice, s), "ranges0");
-    check(cudaStreamSynchronize(s), "sync");
     prep->ra = ra;
+    if (domain) {
+      const size_t n0 = size_t(lw[0]) * size_t(lh[0]), nf = size_t(lw[finest]) * size_t(lh[finest]);
+      prep->owned = true;
+      prep->lev0.reserve(n0);
+      check(cudaMemcpyAsync(prep->lev0.p, lev[0].v, n0 * sizeof(float), cudaMemcpyDeviceToDevice, s), "lev0");
+      prep->ra.lev0.v = prep->lev0.p;
+      prep->ra.img.v = prep->lev0.p;
+      if (finest) {
+        prep->fine.reserve(nf);
+        check(cudaMemcpyAsync(prep->fine.p, lev[finest].v, nf * sizeof(float), cudaMemcpyDeviceToDevice, s), "fine");
+        prep->ra.img.v = prep->fine.p;
+      }
+      if (fine.pairs) {
+        prep->pairs.reserve(nf);
+        check(cudaMemcpyAsync(prep->pairs.p, fine.pairs, nf * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s),
+              "pairs");
+        prep->ra.img.pairs = prep->pairs.p;
+      }
+    }
+    check(cudaStreamSynchronize(s), "sync");
     prep->ra.plist0 = prep->plist0.p;
     prep->ra.ranges0 = prep->ranges0.p;
     prep->geom = geom;
@@ -1644,7 +1763,7 @@ struct MultiRefiner {
       while (j < n && order[j].owner == order[i].owner) ++j;
       const Prepared& P = *preps[size_t(order[i].owner)];
       RefineArgs ra = P.ra;
-      if (ra.img.pairs && ws.pairs_level != P.finest) ra.img.pairs = nullptr;  // another model's level
+      if (!P.owned && ra.img.pairs && ws.pairs_level != P.finest) ra.img.pairs = nullptr;  // another model's level
       ra.sorted = d_cand.p + i;
       ra.refined = d_ref.p + i;
       ra.refined_flag = d_flag.p + i;
@@ -1754,7 +1873,7 @@ std::vector<MultiCand> select_models(std::vector<MultiCand> cands, const std::ve
 // it): one prepared query per distinct (model, options), the candidates
 // pooled, selected and refined on the device.
 std::vector<MultiCand> run_find_models(const std::vector<mvg_ncc_model_s*>& models, const void* pixels, int type,
-                                       int64_t W, int64_t H, int64_t stride, int location,
+                                       int64_t W, int64_t H, int64_t stride, int location, const uint8_t* domain,
                                        const std::vector<FindParams>& opts, Selection sel, cudaStream_t user_stream) {
   Workspace& ws = workspace();
   cudaStream_t s = user_stream ? user_stream : ws.own_stream;
@@ -1795,7 +1914,7 @@ std::vector<MultiCand> run_find_models(const std::vector<mvg_ncc_model_s*>& mode
       }
     if (owner[i] != int(i)) continue;
     preps[i] = std::make_unique<Prepared>();
-    run_find(*models[i], dev, type, W, H, stride, MVG_MEMORY_DEVICE, opts[i], s, -3, preps[i].get());
+    run_find(*models[i], dev, type, W, H, stride, MVG_MEMORY_DEVICE, domain, opts[i], s, -3, preps[i].get());
   }
   std::vector<MultiCand> pool;
   for (size_t i = 0; i < n; ++i) {
@@ -1938,7 +2057,8 @@ int32_t mvg_clear_ncc_model(mvg_ncc_model model_id) {
 }
 
 int32_t mvg_find_ncc_model(const void* pixels, int32_t pixel_type, int64_t width, int64_t height, int64_t row_stride,
-                           int32_t location, mvg_ncc_model model_id, double angle_start, double angle_extent,
+                           int32_t location, const uint8_t* domain, mvg_ncc_model model_id, double angle_start,
+                           double angle_extent,
                            double min_score, int64_t num_matches, double max_overlap, int32_t subpixel,
                            int32_t highest_level, int32_t lowest_level, double* row, double* column, double* angle,
                            double* score, int64_t capacity, int64_t* count, void* stream) {
@@ -1948,7 +2068,7 @@ int32_t mvg_find_ncc_model(const void* pixels, int32_t pixel_type, int64_t width
     *count = 0;
     const auto p = make_params(angle_start, angle_extent, min_score, num_matches, max_overlap, subpixel,
                                highest_level, lowest_level);
-    const FindOutput r = run_find(*model_id, pixels, pixel_type, width, height, row_stride, location, p,
+    const FindOutput r = run_find(*model_id, pixels, pixel_type, width, height, row_stride, location, domain, p,
                                   static_cast<cudaStream_t>(stream), -2);
     *count = int64_t(r.matches.size());
     for (size_t i = 0; i < r.matches.size() && int64_t(i) < capacity; ++i) {
@@ -1964,7 +2084,8 @@ int32_t mvg_find_ncc_model(const void* pixels, int32_t pixel_type, int64_t width
 }
 
 int32_t mvg_find_ncc_models(const void* pixels, int32_t pixel_type, int64_t width, int64_t height, int64_t row_stride,
-                            int32_t location, const mvg_ncc_model* model_ids, int64_t num_models,
+                            int32_t location, const uint8_t* domain, const mvg_ncc_model* model_ids,
+                            int64_t num_models,
                             const double* angle_start, int64_t n_angle_start, const double* angle_extent,
                             int64_t n_angle_extent, const double* min_score, int64_t n_min_score,
                             const int64_t* num_matches, int64_t n_num_matches, const double* max_overlap,
@@ -2038,7 +2159,7 @@ int32_t mvg_find_ncc_models(const void* pixels, int32_t pixel_type, int64_t widt
     sel.num_matches = n_num_matches == 1 ? opts.front().num_matches : -1;
     sel.max_overlap = n_max_overlap == 1 ? opts.front().max_overlap : -1;
     const std::vector<MultiCand> r = run_find_models(models, pixels, pixel_type, width, height, row_stride, location,
-                                                     opts, sel, static_cast<cudaStream_t>(stream));
+                                                     domain, opts, sel, static_cast<cudaStream_t>(stream));
     *count = int64_t(r.size());
     for (size_t i = 0; i < r.size() && int64_t(i) < capacity; ++i) {
       // edge-centred pose convention (src/c_api/ncc_matching_api.cpp:171-176)
@@ -2054,7 +2175,8 @@ int32_t mvg_find_ncc_models(const void* pixels, int32_t pixel_type, int64_t widt
 }
 
 int32_t mvg_find_ncc_model_stage(const void* pixels, int32_t pixel_type, int64_t width, int64_t height,
-                                 int64_t row_stride, int32_t location, mvg_ncc_model model_id, double angle_start,
+                                 int64_t row_stride, int32_t location, const uint8_t* domain, mvg_ncc_model model_id,
+                                 double angle_start,
                                  double angle_extent, double min_score, int64_t num_matches, double max_overlap,
                                  int32_t subpixel, int32_t highest_level, int32_t lowest_level, int32_t stage,
                                  double* out, int64_t capacity, int64_t* count) {
@@ -2064,7 +2186,8 @@ int32_t mvg_find_ncc_model_stage(const void* pixels, int32_t pixel_type, int64_t
     *count = 0;
     const auto p = make_params(angle_start, angle_extent, min_score, num_matches, max_overlap, subpixel,
                                highest_level, lowest_level);
-    const FindOutput r = run_find(*model_id, pixels, pixel_type, width, height, row_stride, location, p, nullptr,
+    const FindOutput r = run_find(*model_id, pixels, pixel_type, width, height, row_stride, location, domain, p,
+                                  nullptr,
                                   stage);
     *count = int64_t(r.stage.size());
     for (size_t i = 0; i < r.stage.size() && int64_t(i) < capacity; ++i) {

@@ -47,6 +47,38 @@ __device__ __forceinline__ float lattice_pose32(float crop, float step, int r, f
   return __fadd_rn(__fadd_rn(crop, __fmul_rn(step, __fadd_rn(float(r), o))), off);
 }
 
+// ------------------------------------------------------------ search domain
+// domain_contains (src/ncc_matching/matcher.cpp:249-251): the pixel nearest
+// to the pose lies in the domain.
+__device__ __forceinline__ bool domain_contains(const DomainView& d, double row, double col) {
+  const double rr = floor(row + .5), cc = floor(col + .5);
+  if (!(rr >= 0 && cc >= 0 && rr < d.h && cc < d.w)) return false;
+  return !d.mask || d.mask[size_t(rr) * d.w + size_t(cc)] != 0;
+}
+
+// may_contain (matcher.cpp:507-534) for a reduced domain, beyond the bounding
+// box that the position ranges encode: spacing 1 tests the nearest pixel; a
+// coarser spacing s accepts a pose with a domain pixel within 2s rows and
+// columns (a run [b, e] of row y meets |y - row| <= 2s, b <= col + 2s,
+// e >= col - 2s exactly when the mask has a pixel in the integer rectangle
+// [ceil(row - 2s), floor(row + 2s)] x [ceil(col - 2s), floor(col + 2s)]),
+// counted from the mask's 2-D prefix counts.  The full image (mask null)
+// passes.
+__device__ bool may_contain(const DomainView& d, double row, double col, double spacing) {
+  if (!d.mask) return true;
+  if (spacing == 1) return domain_contains(d, row, col);
+  const double m = 2 * spacing;
+  if (row < d.rmin - m || row > d.rmax + m || col < d.cmin - m || col > d.cmax + m) return false;
+  if (!d.sparse) return true;
+  const int r0 = max(0, int(ceil(dsub(row, m)))), r1 = min(d.h - 1, int(floor(dadd(row, m))));
+  const int c0 = max(0, int(ceil(dsub(col, m)))), c1 = min(d.w - 1, int(floor(dadd(col, m))));
+  if (r0 > r1 || c0 > c1) return false;
+  const size_t pitch = size_t(d.w) + 1;
+  const int32_t n = d.count[size_t(r1 + 1) * pitch + c1 + 1] - d.count[size_t(r0) * pitch + c1 + 1] -
+                    d.count[size_t(r1 + 1) * pitch + c0] + d.count[size_t(r0) * pitch + c0];
+  return n > 0;
+}
+
 // ------------------------------------------------------- FP32 pair arithmetic
 struct F2 {
   float hi, lo;
@@ -223,7 +255,9 @@ __global__ void __launch_bounds__(256) coarse_kernel(CoarseArgs a) {
   const int r = R0 + threadIdx.y, c = C0 + threadIdx.x;
   if (r >= h || c >= w) return;
   float score = -INFINITY;
-  if (any && r >= rg.r0 && r < rg.r1 && c >= rg.c0 && c < rg.c1) {
+  if (any && r >= rg.r0 && r < rg.r1 && c >= rg.c0 && c < rg.c1 &&
+      may_contain(a.dom, lattice_pose(a.crop_row, a.scale, r, pd.orow, a.phase),
+                  lattice_pose(a.crop_col, a.scale, c, pd.ocol, a.phase), a.scale)) {
     const int2* sw = a.view.sw + pd.sample_off;
     const float* base = tile + (threadIdx.y - pd.rmin) * TW + (threadIdx.x - pd.cmin);
     const int2 f0 = __ldg(sw);
@@ -286,8 +320,10 @@ __global__ void coarse_tc_score_kernel(CoarseTcArgs a) {
   const int r = rem / w, c = rem % w;
   const PosRange rg = a.ranges[j];
   float score = -INFINITY;
-  if (r >= rg.r0 && r < rg.r1 && c >= rg.c0 && c < rg.c1) {
-    const PatchDesc pd = a.view.patches[a.plist[j]];
+  const PatchDesc pd = a.view.patches[a.plist[j]];
+  if (r >= rg.r0 && r < rg.r1 && c >= rg.c0 && c < rg.c1 &&
+      may_contain(a.dom, lattice_pose(a.crop_row, a.scale, r, pd.orow, a.phase),
+                  lattice_pose(a.crop_col, a.scale, c, pd.ocol, a.phase), a.scale)) {
     const int ci = (src * a.lat_r + r / 5) * a.lat_c + c / 5;
     const int pos = (r % 5) * 5 + c % 5, k = a.k_of[j];
     long long s1, s2;
@@ -484,7 +520,9 @@ __global__ void __launch_bounds__(kTrackThreads, 5) track_kernel(TrackArgs a) {
       const PosRange rg = a.ranges[j];
       r = s_row[k] + pos / 5 - 2;
       c = s_col[k] + pos % 5 - 2;
-      valid = r >= rg.r0 && r < rg.r1 && c >= rg.c0 && c < rg.c1;
+      valid = r >= rg.r0 && r < rg.r1 && c >= rg.c0 && c < rg.c1 &&
+              may_contain(a.dom, lattice_pose(a.crop_row, a.step, r, pd.orow, a.offset),
+                          lattice_pose(a.crop_col, a.step, c, pd.ocol, a.offset), a.step);
       is_tc = s_istc[k] != 0;
     }
     if (is_tc) {
@@ -654,11 +692,43 @@ __device__ void snap_pose(Cand& p, double height, double width) {
   }
 }
 
-__global__ void snap_kernel(Cand* c, const QueryState* state, int slot, double height, double width) {
+// The same for a reduced domain: the nearest pixel of the domain's runs
+// within 4 rows and columns; runs are visited in (row, begin) order and only
+// a strictly nearer one replaces the best (src/ncc_matching/matcher.cpp:633-643).
+__device__ void snap_pose_domain(Cand& p, const DomainView& d) {
+  if (domain_contains(d, p.row, p.col)) return;
+  double best = INFINITY, nr = p.row, nc = p.col;
+  const int first = max(0, int(ceil(p.row - 4)));
+  const double rc = round(p.col);
+  for (int y = first; y < d.h && y <= p.row + 4; ++y)
+    for (int k = d.row_run[y]; k < d.row_run[y + 1]; ++k) {
+      const int4 run = d.runs[k];
+      const double c = fmin(fmax(rc, double(run.y)), double(run.z));
+      if (fabs(c - p.col) > 4) continue;
+      const double dist = hypot(double(run.x) - p.row, c - p.col);
+      if (dist < best) {
+        best = dist;
+        nr = double(run.x);
+        nc = c;
+      }
+    }
+  if (isfinite(best)) {
+    p.row = nr;
+    p.col = nc;
+    p.patch = -1;
+  } else {
+    p.score = -INFINITY;
+  }
+}
+
+__global__ void snap_kernel(Cand* c, const QueryState* state, int slot, double height, double width, DomainView dom) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= live_count(state, slot)) return;
   Cand p = c[i];
-  snap_pose(p, height, width);
+  if (dom.mask)
+    snap_pose_domain(p, dom);
+  else
+    snap_pose(p, height, width);
   c[i] = p;
 }
 
@@ -1402,10 +1472,6 @@ __device__ void gn_pass(const ImageView& img, const OriginalView& orig, double r
   __syncthreads();
 }
 
-__device__ __forceinline__ bool inside_image(double row, double col, double height, double width) {
-  const double r = floor(row + .5), c = floor(col + .5);
-  return r >= 0 && c >= 0 && r < height && c < width;
-}
 
 // Per-block fit state; scalar decisions are made by thread 0 and read by all
 // threads after a barrier.
@@ -1461,7 +1527,7 @@ __device__ void fit_full(const RefineArgs& a, FitShared& f) {
         imp.col = dadd(imp.col, dmul(st, f.delta[1]));
         imp.angle = fmin(fmax(dadd(imp.angle, dmul(st, f.delta[2])), a.angle_start), a.angle_end);
         f.imp = imp;
-        f.flag = inside_image(imp.row, imp.col, a.height, a.width);
+        f.flag = domain_contains(a.dom, imp.row, imp.col);
         f.next_valid = 0;
       }
       __syncthreads();
@@ -1521,7 +1587,7 @@ __device__ void fit_coarse(const RefineArgs& a, FitShared& f) {
         nx.col = dadd(nx.col, dmul(dmul(a.scale, st), f.delta[1]));
         nx.angle = fmin(fmax(dadd(nx.angle, dmul(st, f.delta[2])), a.angle_start), a.angle_end);
         f.imp = nx;
-        f.flag = inside_image(nx.row, nx.col, a.height, a.width);
+        f.flag = domain_contains(a.dom, nx.row, nx.col);
       }
       __syncthreads();
       if (!f.flag) continue;
@@ -1558,6 +1624,9 @@ __device__ void recovery_search(const RefineArgs& a, FitShared& f) {
     for (int pos = warp; pos < 25; pos += nw) {
       const int r = r0 + pos / 5 - 2, c = c0 + pos % 5 - 2;
       if (r < rg.r0 || r >= rg.r1 || c < rg.c0 || c >= rg.c1) continue;
+      if (a.dom.mask && !domain_contains(a.dom, double((long long)a.crop_row + r) + pd.orow,
+                                         double((long long)a.crop_col + c) + pd.ocol))
+        continue;
       const int2* sw = a.view0.sw + pd.sample_off;
       const float* base = a.lev0.v + size_t(r) * a.lev0.w + c;
       const int2 f0 = __ldg(sw);
@@ -1671,7 +1740,7 @@ __global__ void __launch_bounds__(kRefineThreads) refine_kernel(RefineArgs a) {
     r.col = f.c.col;
     r.angle = f.c.angle;
     r.score = f.c.score;
-    r.ok = (f.c.score >= a.min_score) && inside_image(f.c.row, f.c.col, a.height, a.width);
+    r.ok = (f.c.score >= a.min_score) && domain_contains(a.dom, f.c.row, f.c.col);
     r.pad = 0;
     r.rect = make_rect(f.c, a.geom);
     a.refined[i] = r;
@@ -1682,7 +1751,42 @@ __global__ void __launch_bounds__(kRefineThreads) refine_kernel(RefineArgs a) {
 
 }  // namespace
 
+// 2-D prefix counts of a domain mask, (h + 1) x (w + 1): row prefixes (one
+// thread per row), then column sums (one thread per column, coalesced).
+__global__ void domain_rows_kernel(const uint8_t* mask, int w, int h, int32_t* count) {
+  const int y = blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t pitch = size_t(w) + 1;
+  if (y == 0)
+    for (int x = 0; x <= w; ++x) count[x] = 0;
+  if (y >= h) return;
+  int32_t sum = 0;
+  int32_t* out = count + size_t(y + 1) * pitch;
+  out[0] = 0;
+  const uint8_t* row = mask + size_t(y) * w;
+  for (int x = 0; x < w; ++x) {
+    sum += row[x] != 0;
+    out[x + 1] = sum;
+  }
+}
+
+__global__ void domain_cols_kernel(int w, int h, int32_t* count) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x > w) return;
+  const size_t pitch = size_t(w) + 1;
+  int32_t sum = 0;
+  for (int y = 1; y <= h; ++y) {
+    sum += count[size_t(y) * pitch + x];
+    count[size_t(y) * pitch + x] = sum;
+  }
+}
+
 // --------------------------------------------------------------- launchers
+cudaError_t launch_domain_count(const uint8_t* mask, int w, int h, int32_t* count, cudaStream_t s) {
+  domain_rows_kernel<<<(h + 127) / 128, 128, 0, s>>>(mask, w, h, count);
+  domain_cols_kernel<<<(w + 1 + 255) / 256, 256, 0, s>>>(w, h, count);
+  return cudaGetLastError();
+}
+
 cudaError_t reserve_dynamic_smem(const void* kernel, size_t bytes) {
   static std::mutex mu;
   static std::map<std::pair<const void*, int>, size_t> granted;
@@ -1762,7 +1866,8 @@ cudaError_t launch_track(const TrackArgs& a, int max_candidates, cudaStream_t s,
 
 cudaError_t launch_dedup(const DedupArgs& a, int max_candidates, cudaStream_t s) {
   const unsigned blocks = unsigned((max_candidates + 255) / 256);
-  if (a.snap) snap_kernel<<<blocks, 256, 0, s>>>(const_cast<Cand*>(a.in), a.state, a.in_slot, a.height, a.width);
+  if (a.snap)
+    snap_kernel<<<blocks, 256, 0, s>>>(const_cast<Cand*>(a.in), a.state, a.in_slot, a.height, a.width, a.dom);
   dedup_kernel<<<blocks, 256, 0, s>>>(a);
   return cudaGetLastError();
 }

@@ -37,6 +37,21 @@ struct PosRange {
   int r0, r1, c0, c1;  // half-open [r0, r1) x [c0, c1)
 };
 
+// Reduced search domain (the search image's ROI, image.domain() in the
+// reference).  mask == nullptr: the full image, whose bounds the position
+// ranges already encode.  Otherwise the position ranges encode the domain's
+// bounding box and the kernels test each pose against the mask (one-pixel
+// spacing) or, for a sparse domain, the mask's pixel count near the pose.
+struct DomainView {
+  const uint8_t* mask;      // h x w, nonzero inside (image coordinates)
+  const int32_t* count;     // (h + 1) x (w + 1) 2-D prefix counts of mask (sparse domains)
+  const int4* runs;         // (row, begin, end, 0) sorted by row and begin
+  const int32_t* row_run;   // h + 1: first run of each row
+  int w, h;
+  int sparse;               // area < 0.7 x bounding-box area (matcher.cpp:505)
+  double rmin, rmax, cmin, cmax;  // bounding box
+};
+
 struct CoarseArgs {
   LevelImage lev;
   LevelView view;
@@ -46,6 +61,8 @@ struct CoarseArgs {
   float* planes;            // nplist x h x w scores
   int absolute;
   const uint8_t* skip;      // per kept patch: 1 = plane written by the tensor-core scan (nullable)
+  DomainView dom;
+  double crop_row, crop_col, scale, phase;
 };
 
 // Tensor-core coarse scan: a lattice of pseudo-candidates at stride 5 (each
@@ -66,6 +83,8 @@ struct CoarseTcArgs {
   const int32_t* group_of_src;
   float* planes;
   int absolute;
+  DomainView dom;
+  double crop_row, crop_col, scale, phase;
 };
 
 struct NmsArgs {
@@ -105,6 +124,7 @@ struct TrackArgs {
   const float* tc_dots;
   const int32_t* tc_group_of_src;
   const TcGroup* tc_groups;
+  DomainView dom;
 };
 
 // Raises a kernel's dynamic shared-memory limit on the current device to at
@@ -188,6 +208,8 @@ cudaError_t launch_tc_track(const TcArgs& a, size_t smem, int grid, cudaStream_t
 cudaError_t launch_coarse_lattice(Cand* cand, int2* rc, int nsrc, int nbr, int nbc, const int32_t* group_of_src,
                                   int32_t* order, TcTiles* tiles, QueryState* state, int slot, cudaStream_t s);
 cudaError_t launch_coarse_tc_score(const CoarseTcArgs& a, cudaStream_t s);
+// (h + 1) x (w + 1) prefix counts of a domain mask (DomainView::count)
+cudaError_t launch_domain_count(const uint8_t* mask, int w, int h, int32_t* count, cudaStream_t s);
 
 // half2 pairs (v[x], v[min(x + 1, w - 1)]) of a level whose values are exact
 // in fp16, w x h entries.
@@ -200,8 +222,9 @@ struct DedupArgs {
   QueryState* state;
   int in_slot, out_slot;
   double threshold;         // drop score < threshold; -inf keeps all finite
-  int snap;                 // 1: snap poses outside the image into it first
+  int snap;                 // 1: snap poses outside the domain into it first
   double height, width;     // image size for the snap (full domain)
+  DomainView dom;
 };
 
 struct ImageView {
@@ -272,6 +295,7 @@ struct RefineArgs {
   int rotate, subpixel, absolute, top, finest;
   double height, width;     // full image (domain test)
   RectGeom geom;
+  DomainView dom;
 };
 
 cudaError_t launch_pyramid0(const void* src, int type, int64_t pitch_elems, int crop_row, int crop_col, LevelImage dst,

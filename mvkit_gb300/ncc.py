@@ -65,10 +65,10 @@ def load() -> C.CDLL:
     lib.mvg_get_ncc_model_params.argtypes = [C.c_void_p, _i32p, _dp, _dp, _dp, _i32p]
     lib.mvg_clear_ncc_model.argtypes = [C.c_void_p]
     lib.mvg_find_ncc_model.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int32, C.c_void_p,
-                                       C.c_double, C.c_double, C.c_double, C.c_int64, C.c_double, C.c_int32,
+                                       C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int64, C.c_double, C.c_int32,
                                        C.c_int32, C.c_int32, _dp, _dp, _dp, _dp, C.c_int64, _i64p, C.c_void_p]
     lib.mvg_find_ncc_model_stage.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int32,
-                                             C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int64, C.c_double,
+                                             C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int64, C.c_double,
                                              C.c_int32, C.c_int32, C.c_int32, C.c_int32, _dp, C.c_int64, _i64p]
     lib.mvg_ncc_pyramid_level.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_void_p,
                                           C.c_int32, C.c_int32, _fp, C.c_int64, _dp]
@@ -77,7 +77,7 @@ def load() -> C.CDLL:
     lib.mvg_serialize_ncc_model.argtypes = [C.c_void_p, C.c_char_p, C.c_int64, _i64p]
     lib.mvg_deserialize_ncc_model.argtypes = [C.c_char_p, C.c_int64, C.POINTER(C.c_void_p)]
     lib.mvg_find_ncc_models.argtypes = ([C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int32,
-                                        C.c_void_p, C.c_int64] + [C.c_void_p, C.c_int64] * 7 +
+                                        C.c_void_p, C.c_void_p, C.c_int64] + [C.c_void_p, C.c_int64] * 7 +
                                        [C.c_void_p] * 5 + [C.c_int64, _i64p, C.c_void_p])
     lib.mvg_last_error.restype = C.c_char_p
     lib.mvg_host_alloc.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
@@ -335,11 +335,24 @@ class DeviceImage:
             pass
 
 
+def _domain(domain, shape, op: str):
+    """The search image's domain (the reference image object's reduced
+    domain) as a contiguous byte mask of the image's shape, or None."""
+    if domain is None:
+        return None
+    d = np.ascontiguousarray(np.asarray(domain) != 0, dtype=np.uint8)
+    if d.shape != tuple(shape):
+        raise MvError(MV_STATUS_INVALID_ARGUMENT, "domain must match the image size", op)
+    return d
+
+
 def find_ncc_model(image, model: NccModel, angle_start, angle_extent, min_score, num_matches, max_overlap,
-                   subpixel, num_levels, stream=None):
+                   subpixel, num_levels, stream=None, domain=None):
     """FindNccModel (src/c_api/ncc_matching_api.cpp:178-190).
 
     image: 2-D uint8/uint16 array in host memory, or a DeviceImage.
+    domain: the image's reduced domain (ROI) as a mask of the image's shape,
+    nonzero inside; None = the whole image.
     Returns (Row, Column, Angle, Score) as float64 arrays in the operator's
     edge-centred convention.  An empty image returns empty outputs."""
     op = "find_ncc_model"
@@ -354,12 +367,14 @@ def find_ncc_model(image, model: NccModel, angle_start, angle_extent, min_score,
             e = np.zeros(0)
             return e, e.copy(), e.copy(), e.copy()
         ptr, (h, w), stride, loc = a.ctypes.data, a.shape, a.strides[0], 0
+    dom = _domain(domain, (h, w), op)
     cap = 64 if ctl[3] == 0 else int(ctl[3])
     lib = load()
     while True:
         out = [np.zeros(cap) for _ in range(4)]
         cnt = C.c_int64()
-        _check(lib.mvg_find_ncc_model(ptr, typ, w, h, stride, loc, model.handle, *ctl,
+        _check(lib.mvg_find_ncc_model(ptr, typ, w, h, stride, loc, None if dom is None else dom.ctypes.data,
+                                      model.handle, *ctl,
                                       *[o.ctypes.data_as(_dp) for o in out], cap, C.byref(cnt),
                                       C.c_void_p(stream) if stream else None), op)
         if cnt.value <= cap:
@@ -368,7 +383,7 @@ def find_ncc_model(image, model: NccModel, angle_start, angle_extent, min_score,
 
 
 def find_ncc_models(image, models, angle_start, angle_extent, min_score, num_matches, max_overlap, subpixel,
-                    num_levels, stream=None):
+                    num_levels, stream=None, domain=None):
     """FindNccModels (src/c_api/ncc_matching_api.cpp:191-201).
 
     models: one NccModel or a sequence of 1..4096.  Each control takes one
@@ -422,6 +437,7 @@ def find_ncc_models(image, models, angle_start, angle_extent, min_score, num_mat
             e = np.zeros(0)
             return e, e.copy(), e.copy(), e.copy(), np.zeros(0, dtype=np.int64)
         ptr, (h, w), stride, loc = a.ctypes.data, a.shape, a.strides[0], 0
+    dom = _domain(domain, (h, w), op)
     ids = (C.c_void_p * n)(*[m.handle for m in ms])
     lib = load()
     cap = max(64, int(quotas.sum()))
@@ -432,7 +448,8 @@ def find_ncc_models(image, models, angle_start, angle_extent, min_score, num_mat
     while True:
         out = [np.zeros(cap) for _ in range(4)] + [np.zeros(cap, dtype=np.int64)]
         cnt = C.c_int64()
-        _check(lib.mvg_find_ncc_models(ptr, typ, w, h, stride, loc, ids, n, *args,
+        _check(lib.mvg_find_ncc_models(ptr, typ, w, h, stride, loc, None if dom is None else dom.ctypes.data, ids,
+                                       n, *args,
                                        *[o.ctypes.data for o in out], cap, C.byref(cnt),
                                        C.c_void_p(stream) if stream else None), op)
         if cnt.value <= cap:
@@ -441,7 +458,7 @@ def find_ncc_models(image, models, angle_start, angle_extent, min_score, num_mat
 
 
 def find_ncc_model_stage(image, model: NccModel, angle_start, angle_extent, min_score, num_matches, max_overlap,
-                         subpixel, num_levels, stage: int) -> np.ndarray:
+                         subpixel, num_levels, stage: int, domain=None) -> np.ndarray:
     """Candidate list of an internal stage (n x 4: row, column, angle, score;
     pixel-centre convention of mv::ncc_matching::find)."""
     op = "find_ncc_model"
@@ -450,8 +467,10 @@ def find_ncc_model_stage(image, model: NccModel, angle_start, angle_extent, min_
     cap = 20000
     out = np.zeros((cap, 4))
     cnt = C.c_int64()
-    _check(load().mvg_find_ncc_model_stage(a.ctypes.data, typ, a.shape[1], a.shape[0], a.strides[0], 0, model.handle,
-                                           *ctl, int(stage), out.ctypes.data_as(_dp), cap, C.byref(cnt)), op)
+    dom = _domain(domain, a.shape, op)
+    _check(load().mvg_find_ncc_model_stage(a.ctypes.data, typ, a.shape[1], a.shape[0], a.strides[0], 0,
+                                           None if dom is None else dom.ctypes.data, model.handle, *ctl, int(stage),
+                                           out.ctypes.data_as(_dp), cap, C.byref(cnt)), op)
     return out[: min(cnt.value, cap)].copy()
 
 

@@ -111,6 +111,56 @@ CASES = {
                              subpixel=True, highest=4, lowest=1)),
 }
 
+# Reduced search domains (ROI, image.domain() in src/ncc_matching/matcher.cpp:
+# 249-251, 375-393, 505-534, 633-643, 870-876, 954, 1034-1060) on one
+# three-pose rotated scene.  "domain" lists shapes relative to the true poses
+# (see search_domain); an empty list is an empty domain.
+_ROI_GEN = dict(seed=11, height=600, width=800, tsize=64, n_poses=3, angle_range=(-D(30), D(30)))
+_ROI_CREATE = dict(levels=3, angle_start=-D(30), angle_extent=D(60))
+_ROI_FIND = dict(angle_start=-D(30), angle_extent=D(60), min_score=0.7, num_matches=0, max_overlap=0.5,
+                 subpixel=True, highest=3, lowest=1)
+for _name, _dom in {
+        "roi_rect": [("around", 0, 40)],                      # one pose inside, dense domain
+        "roi_two": [("around", 0, 20), ("around", 2, 20)],    # two far rectangles: sparse domain
+        "roi_ring": [("ring", 1, 3, 30), ("around", 0, 2)],   # a hole at a pose centre, sparse
+        "roi_strips": [("hline", 0, 0, 60), ("hline", 0, 6, 60)],  # two one-pixel rows
+        "roi_point": [("around", 2, 0)],                      # one pixel at a pose
+        "roi_border": [("left_of", 0, 5)],                    # full-height band cut through a pose
+        "roi_empty": [],
+}.items():
+    CASES[_name] = dict(gen=_ROI_GEN, create=_ROI_CREATE, find=_ROI_FIND, domain=_dom)
+CASES["roi_lowest2"] = dict(gen=_ROI_GEN, create=_ROI_CREATE, find=dict(_ROI_FIND, lowest=2),
+                            domain=[("around", 0, 40), ("around", 1, 6)])
+CASES["roi_no_subpixel"] = dict(gen=_ROI_GEN, create=_ROI_CREATE, find=dict(_ROI_FIND, subpixel=False),
+                                domain=[("ring", 1, 2, 25), ("around", 2, 30)])
+
+
+def search_domain(case: dict, wl):
+    """The search-image domain mask of a case (None = the full image)."""
+    import numpy as np
+    if "domain" not in case:
+        return None
+    h, w = wl.image.shape
+    m = np.zeros((h, w), np.uint8)
+    yy, xx = np.mgrid[0:h, 0:w]
+    for shape in case["domain"]:
+        p = wl.poses[shape[1]]
+        r, c = int(math.floor(p.row + .5)), int(math.floor(p.column + .5))
+        if shape[0] == "around":
+            k = shape[2]
+            m[max(0, r - k):r + k + 1, max(0, c - k):c + k + 1] = 1
+        elif shape[0] == "ring":
+            d2 = (yy - r) ** 2 + (xx - c) ** 2
+            m[(d2 > shape[2] ** 2) & (d2 <= shape[3] ** 2)] = 1
+        elif shape[0] == "hline":
+            m[r + shape[2], max(0, c - shape[3]):c + shape[3] + 1] = 1
+        elif shape[0] == "left_of":
+            m[:, :c + shape[2] + 1] = 1
+        else:
+            raise ValueError(shape[0])
+    return m
+
+
 # Large single-GPU throughput case, checked against the oracle at full size.
 LARGE = {
     "cfg2_s1": dict(gen=dict(seed=1, height=2048, width=2048, tsize=128, n_poses=5, angle_range=(-D(30), D(30))),

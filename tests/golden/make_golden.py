@@ -18,7 +18,7 @@ sys.path.insert(0, str(HERE.parent))
 sys.path.insert(0, str(HERE.parents[1]))
 
 import oracle_lib  # noqa: E402
-from golden.cases import CASES, LARGE, make_inputs  # noqa: E402
+from golden.cases import CASES, LARGE, make_inputs, search_domain  # noqa: E402
 
 
 def run(checker, case, wl, mask):
@@ -29,7 +29,7 @@ def run(checker, case, wl, mask):
     f = case["find"]
     t0 = time.perf_counter()
     res = checker.find(model, wl.image, f["angle_start"], f["angle_extent"], f["min_score"], f["num_matches"],
-                       f["max_overlap"], f["subpixel"], f["highest"], f["lowest"])
+                       f["max_overlap"], f["subpixel"], f["highest"], f["lowest"], domain=search_domain(case, wl))
     dt = time.perf_counter() - t0
     return model, res, dt
 

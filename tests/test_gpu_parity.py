@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 import oracle_lib
-from golden.cases import CASES, LARGE, make_inputs
+from golden.cases import CASES, LARGE, make_inputs, search_domain
 from golden.multi_cases import MULTI_CASES, make_multi_inputs
 
 pytestmark = pytest.mark.gpu
@@ -46,11 +46,12 @@ def gpu_model(mg, case, wl, mask):
                                "ignore_global_polarity" if c.get("ignore_polarity") else "use_polarity", domain=mask)
 
 
-def gpu_find(mg, model, image, case, **over):
+def gpu_find(mg, model, image, case, domain=None, **over):
     f = dict(case["find"])
     f.update(over)
     return mg.find_ncc_model(image, model, f["angle_start"], f["angle_extent"], f["min_score"], f["num_matches"],
-                             f["max_overlap"], "true" if f["subpixel"] else "false", [f["highest"], f["lowest"]])
+                             f["max_overlap"], "true" if f["subpixel"] else "false", [f["highest"], f["lowest"]],
+                             domain=domain)
 
 
 def assert_same_matches(got, want_internal, label=""):
@@ -76,7 +77,7 @@ def test_find_matches_reference(mg, name):
             gpu_find(mg, model, wl.image, case)
         assert err.value.status == GOLDEN[name]["status"]
         return
-    got = gpu_find(mg, model, wl.image, case)
+    got = gpu_find(mg, model, wl.image, case, domain=search_domain(case, wl))
     assert_same_matches(got, GOLDEN[name]["matches"], name)
 
 
@@ -125,6 +126,27 @@ def test_find_models_matches_reference(mg, name):
     want = np.array(MULTI[name]["matches"]).reshape(-1, 5)
     assert list(got[4]) == [int(x) for x in want[:, 4]], f"{name}: model indices {list(got[4])} vs {want[:, 4]}"
     assert_same_matches(got[:4], want[:, :4], name)
+
+
+def test_find_models_with_domain(mg):
+    """FindNccModels on a reduced domain: each model's find restricted to
+    it, the selection over all (each model crops the image differently)."""
+    case = CASES["roi_two"]
+    wl, mask = make_inputs(case)
+    dom = search_domain(case, wl)
+    a = gpu_model(mg, case, wl, mask)
+    b = mg.create_ncc_model(wl.template, 2, case["create"]["angle_start"], case["create"]["angle_extent"], "auto",
+                            "use_polarity")
+    f = case["find"]
+    many = mg.find_ncc_models(wl.image, [a, b], f["angle_start"], f["angle_extent"], f["min_score"], [0],
+                              [0.5, 0.5], "true", [3, 1, 2, 1], domain=dom)
+    for k, m in enumerate((a, b)):
+        one = mg.find_ncc_model(wl.image, m, f["angle_start"], f["angle_extent"], f["min_score"], 0, 0.5, "true",
+                                [3 if k == 0 else 2, 1], domain=dom)
+        sel = many[4] == k
+        assert sel.sum() == len(one[0]) and len(one[0]) == 2
+        for x, y in zip(one, many[:4]):
+            np.testing.assert_allclose(np.sort(x), np.sort(y[sel]), atol=1e-9)
 
 
 def test_find_models_single_equals_find(mg):
@@ -194,7 +216,7 @@ def path(mg, request):
 
 @pytest.mark.parametrize("path", ["tensor", "plain"], indirect=True)
 @pytest.mark.parametrize("name", ["cfg1_s1", "rot3_all", "rot_l4_2", "u16_rot", "polarity", "full_circle",
-                                  "u16_12bit", "tiny16"])
+                                  "u16_12bit", "tiny16", "roi_two", "roi_ring", "roi_strips", "roi_no_subpixel"])
 def test_candidate_stages_match_oracle(mg, orc, name, path):
     case = CASES[name]
     wl, mask = make_inputs(case)
@@ -205,10 +227,11 @@ def test_candidate_stages_match_oracle(mg, orc, name, path):
     ctl = (f["angle_start"], f["angle_extent"], f["min_score"], f["num_matches"], f["max_overlap"],
            "true" if f["subpixel"] else "false", [f["highest"], f["lowest"]])
     steps = [0] + list(range(1, f["highest"]))
+    dom = search_domain(case, wl)
     for stage in steps:
         want = orc.find(om, wl.image, f["angle_start"], f["angle_extent"], f["min_score"], f["num_matches"],
-                        f["max_overlap"], f["subpixel"], f["highest"], f["lowest"], stage=stage)
-        got = mg.find_ncc_model_stage(wl.image, model, *ctl, stage=stage)
+                        f["max_overlap"], f["subpixel"], f["highest"], f["lowest"], stage=stage, domain=dom)
+        got = mg.find_ncc_model_stage(wl.image, model, *ctl, stage=stage, domain=dom)
         a, b = pose_set(got), pose_set(want)
         sym = len(a ^ b)
         assert sym <= max(2, len(b) // 100), f"{name} stage {stage}: {len(a)} vs {len(b)} candidates, {sym} differ"
@@ -220,8 +243,8 @@ def test_candidate_stages_match_oracle(mg, orc, name, path):
                 assert abs(r[3] - ws[k]) < 2e-5, f"{name} stage {stage} score {r[3]} vs {ws[k]}"
     # full-resolution scores of the sorted candidate list
     want = orc.find(om, wl.image, f["angle_start"], f["angle_extent"], f["min_score"], f["num_matches"],
-                    f["max_overlap"], f["subpixel"], f["highest"], f["lowest"], stage=100)
-    got = mg.find_ncc_model_stage(wl.image, model, *ctl, stage=100)
+                    f["max_overlap"], f["subpixel"], f["highest"], f["lowest"], stage=100, domain=dom)
+    got = mg.find_ncc_model_stage(wl.image, model, *ctl, stage=100, domain=dom)
     want = want[np.isfinite(want[:, 3])]   # the find loop skips unscorable candidates
     ws = {(r[0], r[1], r[2]): r[3] for r in want}
     common = [r for r in got if (r[0], r[1], r[2]) in ws]
@@ -233,11 +256,11 @@ def test_candidate_stages_match_oracle(mg, orc, name, path):
 
 @pytest.mark.parametrize("path", ["plain"], indirect=True)
 @pytest.mark.parametrize("name", ["cfg1_s1", "rot_l4_2", "u16_rot", "polarity", "mask_disc", "full_circle",
-                                  "u16_12bit", "big160"])
+                                  "u16_12bit", "big160", "roi_two", "roi_ring", "roi_lowest2"])
 def test_find_matches_reference_plain_path(mg, name, path):
     case = CASES[name]
     wl, mask = make_inputs(case)
-    got = gpu_find(mg, gpu_model(mg, case, wl, mask), wl.image, case)
+    got = gpu_find(mg, gpu_model(mg, case, wl, mask), wl.image, case, domain=search_domain(case, wl))
     assert_same_matches(got, GOLDEN[name]["matches"], f"{name} plain")
 
 

@@ -73,11 +73,11 @@ def test_c_abi_cardinality(models):
     sp = np.array([1], dtype=np.int32)
     lv = np.array([2], dtype=np.int32)
     cnt = C.c_int64()
-    st = lib.mvg_find_ncc_models(IMG.ctypes.data, 0, 64, 64, 64, 0, ids, 3, one.ctypes.data, 1, one.ctypes.data, 1,
+    st = lib.mvg_find_ncc_models(IMG.ctypes.data, 0, 64, 64, 64, 0, None, ids, 3, one.ctypes.data, 1, one.ctypes.data, 1,
                                  one.ctypes.data, 1, q.ctypes.data, 1, d.ctypes.data, 2, sp.ctypes.data, 1,
                                  lv.ctypes.data, 1, None, None, None, None, None, 0, C.byref(cnt), None)
     assert st == ncc.MV_STATUS_INVALID_ARGUMENT
-    st = lib.mvg_find_ncc_models(IMG.ctypes.data, 0, 64, 64, 64, 0, ids, 4097, one.ctypes.data, 1, one.ctypes.data,
+    st = lib.mvg_find_ncc_models(IMG.ctypes.data, 0, 64, 64, 64, 0, None, ids, 4097, one.ctypes.data, 1, one.ctypes.data,
                                  1, one.ctypes.data, 1, q.ctypes.data, 1, one.ctypes.data, 1, sp.ctypes.data, 1,
                                  lv.ctypes.data, 1, None, None, None, None, None, 0, C.byref(cnt), None)
     assert st == ncc.MV_STATUS_INVALID_ARGUMENT

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import oracle_lib
-from golden.cases import CASES, LARGE, make_inputs
+from golden.cases import CASES, LARGE, make_inputs, search_domain
 
 GOLDEN = json.loads((Path(__file__).parent / "golden" / "golden.json").read_text())["cases"]
 
@@ -27,7 +27,8 @@ def run(checker, case, wl, mask, **over):
     f = dict(case["find"])
     f.update(over)
     return model, checker.find(model, wl.image, f["angle_start"], f["angle_extent"], f["min_score"],
-                               f["num_matches"], f["max_overlap"], f["subpixel"], f["highest"], f["lowest"])
+                               f["num_matches"], f["max_overlap"], f["subpixel"], f["highest"], f["lowest"],
+                               domain=search_domain(case, wl))
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
