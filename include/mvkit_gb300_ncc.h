@@ -74,6 +74,18 @@ MVG_API int32_t mvg_read_ncc_model(const char* file_name, mvg_ncc_model* model_i
 MVG_API int32_t mvg_serialize_ncc_model(mvg_ncc_model model_id, char* buffer, int64_t capacity, int64_t* size);
 MVG_API int32_t mvg_deserialize_ncc_model(const char* bytes, int64_t size, mvg_ncc_model* model_id);
 
+/* Where models are built (create and read): 0 (default) = the rotated
+ * rasters on the current CUDA device when one is present, straight into the
+ * find tables; 1 = on the host in FP64 (the reference's CPU order).  Both
+ * give the same weights bit for bit; a process without a CUDA device builds
+ * on the host. */
+MVG_API int32_t mvg_set_model_build(int32_t where);
+
+/* FNV-1a 64 digest of a model's find tables (patch descriptors, angles,
+ * sample, weight and run tables of every level, trained patches only):
+ * equal digests mean bit-identical tables.  Uploads the tables first. */
+MVG_API int32_t mvg_ncc_model_tables_digest(mvg_ncc_model model_id, uint64_t* digest);
+
 /* Releases a model (the reference frees it with the handle tuple,
  * mv_destroy_tuple; include/mvkit/c/mv_ncc_matching.h:64-67). */
 MVG_API int32_t mvg_clear_ncc_model(mvg_ncc_model model_id);

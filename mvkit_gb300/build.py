@@ -17,7 +17,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_lib"
 LIB = OUT / "libmvkit_gb300.so"
-SOURCES = ["ncc_kernels.cu", "ncc_tc.cu", "ncc_api.cpp", "ncc_model.cpp", "ncc_persist.cpp", "ncc_noalloc.cu"]
+SOURCES = ["ncc_kernels.cu", "ncc_tc.cu", "ncc_api.cpp", "ncc_model.cpp", "ncc_persist.cpp", "ncc_build.cu", "ncc_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -19,6 +20,7 @@
 #include <vector>
 
 #include "../../include/mvkit_gb300_ncc.h"
+#include "ncc_build.h"
 #include "ncc_kernels.h"
 #include "ncc_model.h"
 
@@ -221,6 +223,48 @@ struct mvg_ncc_model_s {
 
 namespace mvg {
 namespace {
+
+// Where models are built: 0 = the rotated rasters on the device when one is
+// present, 1 = on the host (the reference's order in FP64 on the CPU).
+std::atomic<int> g_model_build{0};
+
+// Rotated rasters of a model whose pyramid and angles are built: on the
+// device (straight into the find tables, uploaded now) or on the host (tables
+// packed and uploaded by the first find).
+void finish_model(mvg_ncc_model_s& m) {
+  int ndev = 0;
+  if (g_model_build.load() != 0 || cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    build_rasters(m.host);
+    return;
+  }
+  check(cudaGetDevice(&m.device), "cudaGetDevice");
+  std::vector<std::unique_ptr<DevLevel>> levels;
+  std::vector<int32_t> pitch;
+  for (const ModelLevel& L : m.host.levels) {
+    auto d = std::make_unique<DevLevel>();
+    d->set_geometry(L.width, L.height);
+    pitch.push_back(d->lin_pitch);
+    levels.push_back(std::move(d));
+  }
+  std::vector<LevelTables> t;
+  build_tables_device(m.host, pitch, t, nullptr);
+  for (size_t l = 0; l < levels.size(); ++l) {
+    DevLevel& d = *levels[l];
+    d.desc = std::move(t[l].desc);
+    d.angles = std::move(t[l].angles);
+    d.offs = std::move(t[l].offs);
+    d.w = std::move(t[l].w);
+    d.sw = std::move(t[l].sw);
+    d.lw = std::move(t[l].lw);
+    d.runs = std::move(t[l].runs);
+    d.runs_end = std::move(t[l].runs_end);
+    d.model_patches = d.desc.size();
+    d.upload();
+  }
+  m.original.set(m.host.original, m.host.levels.front().orow, m.host.levels.front().ocol);
+  m.levels = std::move(levels);
+}
 
 // The model's sample, run and raster tables in HBM (once per model).
 void ensure_device(mvg_ncc_model_s& m) {
@@ -1994,8 +2038,46 @@ int32_t mvg_create_ncc_model(const void* pixels, int32_t pixel_type, int64_t wid
     p.angle_extent = angle_extent;
     p.angle_step = angle_step > 0 ? angle_step : 0.;
     auto m = std::make_unique<mvg_ncc_model_s>();
-    m->host = create_model(pixels, pixel_type, width, height, row_stride, domain, p);
+    m->host = create_model(pixels, pixel_type, width, height, row_stride, domain, p, false);
+    finish_model(*m);
     *model_id = m.release();
+  });
+}
+
+int32_t mvg_set_model_build(int32_t where) {
+  return guarded([&] {
+    if (where != 0 && where != 1) raise(kInvalidArgument, "model build must be 0 (device) or 1 (host)");
+    g_model_build.store(where);
+  });
+}
+
+int32_t mvg_ncc_model_tables_digest(mvg_ncc_model model_id, uint64_t* digest) {
+  return guarded([&] {
+    if (!model_id || !digest) raise(kInvalidArgument, "model and digest must not be null");
+    std::unique_lock<std::mutex> lock(model_id->mutex);
+    ensure_device(*model_id);
+    uint64_t h = 14695981039346656037ULL;
+    auto mix = [&](const void* p, size_t n) {
+      const unsigned char* b = static_cast<const unsigned char*>(p);
+      for (size_t i = 0; i < n; ++i) {
+        h ^= b[i];
+        h *= 1099511628211ULL;
+      }
+    };
+    for (const auto& L : model_id->levels) {
+      const size_t np = L->model_patches;
+      mix(L->desc.data(), np * sizeof(PatchDesc));
+      mix(L->angles.data(), np * sizeof(double));
+      const size_t ns = np ? size_t(L->desc[np - 1].sample_off + L->desc[np - 1].n) : 0;
+      const size_t nr = np ? size_t(L->desc[np - 1].run_off + L->desc[np - 1].nruns) : 0;
+      mix(L->offs.data(), ns * sizeof(int32_t));
+      mix(L->w.data(), ns * sizeof(float));
+      mix(L->sw.data(), ns * sizeof(int2));
+      mix(L->lw.data(), ns * sizeof(int2));
+      mix(L->runs.data(), nr * sizeof(int32_t));
+      mix(L->runs_end.data(), nr * sizeof(int32_t));
+    }
+    *digest = h;
   });
 }
 
@@ -2013,7 +2095,13 @@ int32_t mvg_read_ncc_model(const char* file_name, mvg_ncc_model* model_id) {
     *model_id = nullptr;
     if (!file_name || !*file_name) raise(kInvalidArgument, "nonempty file name without NUL required");
     auto m = std::make_unique<mvg_ncc_model_s>();
-    m->host = read_model_file(file_name);
+    m->host = read_model_file(file_name, false);
+    try {
+      finish_model(*m);
+    } catch (const Error& e) {
+      // persist.cpp:73-76: a model whose rasters cannot be built
+      raise(e.status == kLimitExceeded ? kLimitExceeded : kDecodeError, "invalid prepared NCC model");
+    }
     *model_id = m.release();
   });
 }
@@ -2034,7 +2122,13 @@ int32_t mvg_deserialize_ncc_model(const char* bytes, int64_t size, mvg_ncc_model
     *model_id = nullptr;
     if (size < 0 || (!bytes && size > 0)) raise(kInvalidArgument, "invalid model bytes");
     auto m = std::make_unique<mvg_ncc_model_s>();
-    m->host = deserialize_model(std::string_view(bytes ? bytes : "", size_t(size)));
+    m->host = deserialize_model(std::string_view(bytes ? bytes : "", size_t(size)), false);
+    try {
+      finish_model(*m);
+    } catch (const Error& e) {
+      // persist.cpp:73-76: a model whose rasters cannot be built
+      raise(e.status == kLimitExceeded ? kLimitExceeded : kDecodeError, "invalid prepared NCC model");
+    }
     *model_id = m.release();
   });
 }

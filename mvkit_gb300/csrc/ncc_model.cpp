@@ -15,7 +15,7 @@ namespace mvg {
 namespace {
 
 constexpr double kTwoPi = 6.283185307179586476925286766559;
-constexpr size_t kTemplatePixels = 1048576, kAngles = 4096, kSampleBudget = 16000000;
+constexpr size_t kTemplatePixels = kModelTemplatePixels, kAngles = kModelAngles, kSampleBudget = kModelSampleBudget;
 
 // Pending raster before normalisation: FP64 gray values at integer offsets.
 struct RawSample { int32_t row, col; double value; };
@@ -68,22 +68,22 @@ bool finish_raster(std::vector<RawSample>& s, Raster& out, const Moments* known)
   return true;
 }
 
-Raster rotate_impl(const ModelLevel& L, double angle, const Moments* known) {
-  Raster out;
-  out.angle = angle;
-  std::vector<RawSample> s;
-  s.reserve(size_t(std::count(L.mask.begin(), L.mask.end(), uint8_t{1})));
-  if (std::abs(std::remainder(angle, kTwoPi)) < 1e-12) {
-    // Unrotated raster keeps absolute level coordinates.
-    out.orow = L.orow;
-    out.ocol = L.ocol;
-    for (size_t r = 0; r < L.height; ++r)
-      for (size_t c = 0; c < L.width; ++c)
-        if (L.mask[r * L.width + c]) s.push_back({int32_t(r), int32_t(c), L.gray[r * L.width + c]});
-    if (!finish_raster(s, out, known)) return Raster{};
-    return out;
+}  // namespace
+
+RasterBox raster_box(const ModelLevel& L, double angle) {
+  RasterBox b;
+  b.angle = angle;
+  b.unrotated = std::abs(std::remainder(angle, kTwoPi)) < 1e-12;
+  if (b.unrotated) {
+    b.r0 = 0;
+    b.r1 = int(L.height) - 1;
+    b.c0 = 0;
+    b.c1 = int(L.width) - 1;
+    return b;
   }
   const double ca = std::cos(angle), sa = std::sin(angle);
+  b.ca = ca;
+  b.sa = sa;
   // Bounding box of the rotated level corners about the origin (origin
   // included, so the box always contains 0).
   double lo_r = 0, hi_r = 0, lo_c = 0, hi_c = 0;
@@ -98,11 +98,36 @@ Raster rotate_impl(const ModelLevel& L, double angle, const Moments* known) {
       hi_c = std::max(hi_c, cc);
     }
   const double span_r = std::ceil(hi_r) - std::floor(lo_r) + 1, span_c = std::ceil(hi_c) - std::floor(lo_c) + 1;
-  if (span_r > 4 * kTemplatePixels / span_c) raise(kLimitExceeded, "rotated bounding box exceeds budget");
-  const int r_first = int(std::floor(lo_r)), r_last = int(std::ceil(hi_r));
-  const int c_first = int(std::floor(lo_c)), c_last = int(std::ceil(hi_c));
-  for (int r = r_first; r <= r_last; ++r)
-    for (int c = c_first; c <= c_last; ++c) {
+  b.too_large = span_r > 4 * kTemplatePixels / span_c;
+  b.r0 = int(std::floor(lo_r));
+  b.r1 = int(std::ceil(hi_r));
+  b.c0 = int(std::floor(lo_c));
+  b.c1 = int(std::ceil(hi_c));
+  return b;
+}
+
+namespace {
+
+Raster rotate_impl(const ModelLevel& L, double angle, const Moments* known) {
+  Raster out;
+  out.angle = angle;
+  std::vector<RawSample> s;
+  s.reserve(size_t(std::count(L.mask.begin(), L.mask.end(), uint8_t{1})));
+  const RasterBox box = raster_box(L, angle);
+  if (box.unrotated) {
+    // Unrotated raster keeps absolute level coordinates.
+    out.orow = L.orow;
+    out.ocol = L.ocol;
+    for (size_t r = 0; r < L.height; ++r)
+      for (size_t c = 0; c < L.width; ++c)
+        if (L.mask[r * L.width + c]) s.push_back({int32_t(r), int32_t(c), L.gray[r * L.width + c]});
+    if (!finish_raster(s, out, known)) return Raster{};
+    return out;
+  }
+  const double ca = box.ca, sa = box.sa;
+  if (box.too_large) raise(kLimitExceeded, "rotated bounding box exceeds budget");
+  for (int r = box.r0; r <= box.r1; ++r)
+    for (int c = box.c0; c <= box.c1; ++c) {
       // source position of the rotated offset (r, c) in the level raster
       const double y = ca * r + sa * c + L.orow, x = -sa * r + ca * c + L.ocol;
       if (y < 0 || x < 0 || y > L.height - 1 || x > L.width - 1) continue;
@@ -142,7 +167,8 @@ bool level_usable(const ModelLevel& L, size_t* count) {
 // rebuild() of src/ncc_matching/model.cpp:173-242: the original raster, the
 // pyramid, the resolved angle step and every level's rotated rasters from the
 // mean-free level-0 raster.
-HostModel rebuild_model(ModelLevel first, const CreateParams& params, double origin_row, double origin_col) {
+HostModel rebuild_model(ModelLevel first, const CreateParams& params, double origin_row, double origin_col,
+                        bool rasters) {
   HostModel m;
   m.params = params;
   m.origin_row = origin_row;
@@ -220,12 +246,23 @@ HostModel rebuild_model(ModelLevel first, const CreateParams& params, double ori
   const double intervals = std::ceil(params.angle_extent / m.params.angle_step);
   if (!std::isfinite(intervals) || intervals >= kAngles) raise(kLimitExceeded, "angle grid exceeds limit");
   const size_t angles = size_t(intervals) + 1;
+  for (size_t i = 0; i < angles; ++i)
+    m.angles.push_back(params.angle_start + std::min(params.angle_extent, i * m.params.angle_step));
+  m.level0_mean = level0.mean;
+  m.level0_energy = level0.energy;
+  m.rasters = false;
+  if (rasters) build_rasters(m);
+  return m;
+}
+
+void build_rasters(HostModel& m) {
+  const Moments level0{m.level0_mean, m.level0_energy};
   size_t total = 0;
   for (size_t li = 0; li < m.levels.size(); ++li) {
     ModelLevel& L = m.levels[li];
-    L.patches.reserve(angles);
-    for (size_t i = 0; i < angles; ++i) {
-      const double angle = params.angle_start + std::min(params.angle_extent, i * m.params.angle_step);
+    L.patches.clear();
+    L.patches.reserve(m.angles.size());
+    for (const double angle : m.angles) {
       Raster p = rotate_impl(L, angle, li == 0 ? &level0 : nullptr);
       if (p.w.empty()) raise(kInvalidArgument, "rotation produces a degenerate template");
       if (p.size() > kSampleBudget - total) raise(kLimitExceeded, "model raster budget exceeded");
@@ -233,14 +270,14 @@ HostModel rebuild_model(ModelLevel first, const CreateParams& params, double ori
       L.patches.push_back(std::move(p));
     }
   }
-  return m;
+  m.rasters = true;
 }
 
 namespace {
 
 template <class T>
 HostModel create_typed(const T* px, int64_t width, int64_t height, int64_t stride_elems, const uint8_t* mask,
-                       const CreateParams& params) {
+                       const CreateParams& params, bool rasters) {
   // Template domain as runs: mask or the full rectangle.
   int64_t rmin = height, rmax = -1, cmin = width, cmax = -1, area = 0;
   struct Span { int64_t row, begin, end; };
@@ -296,13 +333,13 @@ HostModel create_typed(const T* px, int64_t width, int64_t height, int64_t strid
   const double mean = double(isum) / double(a);
   for (size_t i = 0; i < first.gray.size(); ++i)
     if (first.mask[i]) first.gray[i] -= mean;
-  return rebuild_model(std::move(first), params, origin_row, origin_col);
+  return rebuild_model(std::move(first), params, origin_row, origin_col, rasters);
 }
 
 }  // namespace
 
 HostModel create_model(const void* pixels, int type, int64_t width, int64_t height, int64_t stride_bytes,
-                       const uint8_t* mask, const CreateParams& p) {
+                       const uint8_t* mask, const CreateParams& p, bool rasters) {
   if (!pixels) raise(kInvalidArgument, "template pixels must not be null");
   if (type != 0 && type != 1) raise(kTypeMismatch, "one byte or uint2 channel required");
   if (width <= 0 || height <= 0) raise(kInvalidArgument, "one nonempty single-channel image required");
@@ -313,8 +350,8 @@ HostModel create_model(const void* pixels, int type, int64_t width, int64_t heig
       p.angle_step < 0 || p.levels < 0 || p.levels > 16)
     raise(kInvalidArgument, "invalid levels or angle range");
   if (type == 1)
-    return create_typed(static_cast<const uint16_t*>(pixels), width, height, stride_bytes / 2, mask, p);
-  return create_typed(static_cast<const uint8_t*>(pixels), width, height, stride_bytes, mask, p);
+    return create_typed(static_cast<const uint16_t*>(pixels), width, height, stride_bytes / 2, mask, p, rasters);
+  return create_typed(static_cast<const uint8_t*>(pixels), width, height, stride_bytes, mask, p, rasters);
 }
 
 Raster rotate_level(const ModelLevel& level, double angle) { return rotate_impl(level, angle, nullptr); }

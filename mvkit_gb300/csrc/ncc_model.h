@@ -49,26 +49,51 @@ struct HostModel {
   double origin_row = 0, origin_col = 0;
   Raster original;              // unrotated level-0 raster (row/col absolute)
   std::vector<ModelLevel> levels;
+  // trained angles (the same list on every level) and the level-0 moments
+  // that the unrotated level-0 raster reuses
+  std::vector<double> angles;
+  double level0_mean = 0, level0_energy = 0;
+  bool rasters = true;          // levels[l].patches built (false: built on the device)
 };
+
+// Limits of the model build (src/ncc_matching/model.cpp:14-18).
+constexpr size_t kModelTemplatePixels = 1048576, kModelAngles = 4096, kModelSampleBudget = 16000000;
 
 // CreateNccModel on a byte (type 0) or uint16 (type 1) template.  `mask`
 // (width*height bytes, nonzero = inside) is the template domain; NULL means
 // the whole image.  Throws Error with an MvStatus code.
 HostModel create_model(const void* pixels, int type, int64_t width, int64_t height, int64_t stride_bytes,
-                       const uint8_t* mask, const CreateParams& params);
+                       const uint8_t* mask, const CreateParams& params, bool rasters = true);
 
 // The model from its mean-free level-0 raster (gray minus the template mean,
 // mask, size and centroid) and the trained options: the path shared by
 // create and by reading a model file.  Throws Error.
-HostModel rebuild_model(ModelLevel first, const CreateParams& params, double origin_row, double origin_col);
+HostModel rebuild_model(ModelLevel first, const CreateParams& params, double origin_row, double origin_col,
+                        bool rasters = true);
+
+// The rotated rasters of every level and trained angle, in the reference's
+// order (levels, then angles), with its errors.  Fills levels[l].patches.
+void build_rasters(HostModel& m);
 
 // Model files ("MVKIT_NCC 1", src/ncc_matching/persist.cpp:33-83): text body
 // of the trained options, the level-0 raster and its centroid, prefixed by an
 // FNV-1a 64 checksum of the body.  deserialize_model rebuilds the model.
 std::string serialize_model(const HostModel& model);
-HostModel deserialize_model(std::string_view bytes);
+HostModel deserialize_model(std::string_view bytes, bool rasters = true);
 void write_model_file(const HostModel& model, const std::string& path);
-HostModel read_model_file(const std::string& path);
+HostModel read_model_file(const std::string& path, bool rasters = true);
+
+// Geometry of one rotated raster (src/ncc_matching/model.cpp:66-80): the
+// unrotated raster keeps the level's own pixels; a rotated one scans the
+// integer offsets [r0, r1] x [c0, c1] about the level origin, sampling the
+// level at (ca r + sa c + orow, -sa r + ca c + ocol).  too_large: the box
+// exceeds the reference's budget (LimitExceeded).
+struct RasterBox {
+  double angle = 0, ca = 1, sa = 0;
+  bool unrotated = false, too_large = false;
+  int r0 = 0, r1 = -1, c0 = 0, c1 = -1;
+};
+RasterBox raster_box(const ModelLevel& level, double angle);
 
 // Raster of `level` rotated by `angle` (used for query-range endpoints that
 // fall between trained angles).  Empty when the rotation is degenerate.

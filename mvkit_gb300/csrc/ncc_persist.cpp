@@ -182,7 +182,7 @@ std::string serialize_model(const HostModel& m) {
 }
 
 // deserialize(), src/ncc_matching/persist.cpp:44-77
-HostModel deserialize_model(std::string_view bytes) {
+HostModel deserialize_model(std::string_view bytes, bool rasters) {
   if (bytes.size() > kMaxModelFile + 128) raise(kLimitExceeded, "model file exceeds budget");
   // signature line (std::getline: up to the first '\n', which is consumed)
   const size_t nl = bytes.find('\n');
@@ -249,7 +249,7 @@ HostModel deserialize_model(std::string_view bytes) {
     decode_error("invalid template domain centroid");
   if (!f.at_end()) decode_error("trailing model data");
   try {
-    return rebuild_model(std::move(first), o, origin_row, origin_col);
+    return rebuild_model(std::move(first), o, origin_row, origin_col, rasters);
   } catch (const Error& e) {
     raise(e.status == kLimitExceeded ? kLimitExceeded : kDecodeError, "invalid prepared NCC model");
   }
@@ -266,7 +266,7 @@ void write_model_file(const HostModel& m, const std::string& path) {
   if (!out) raise(kIoError, "cannot write model file");
 }
 
-HostModel read_model_file(const std::string& path) {
+HostModel read_model_file(const std::string& path, bool rasters) {
   std::ifstream in(path, std::ios::binary | std::ios::ate);
   if (!in) raise(kIoError, "cannot open model for reading");
   const auto size = in.tellg();
@@ -275,7 +275,7 @@ HostModel read_model_file(const std::string& path) {
   in.seekg(0);
   if (!bytes.empty()) in.read(bytes.data(), std::streamsize(bytes.size()));
   if (!in) raise(kIoError, "cannot read model file");
-  return deserialize_model(bytes);
+  return deserialize_model(bytes, rasters);
 }
 
 }  // namespace mvg

@@ -508,6 +508,27 @@ class PinnedBuffer:
 PROFILE_STAGES = 13
 
 
+def set_model_build(where: str) -> None:
+    """'device' (default): models' rotated rasters are built on the GPU when
+    one is present; 'host': in FP64 on the CPU.  Same weights bit for bit."""
+    if where not in ("device", "host"):
+        raise MvError(MV_STATUS_INVALID_ARGUMENT, "model build must be 'device' or 'host'", "set_model_build")
+    lib = load()
+    lib.mvg_set_model_build.argtypes = [C.c_int32]
+    lib.mvg_set_model_build.restype = C.c_int32
+    _check(lib.mvg_set_model_build(0 if where == "device" else 1), "set_model_build")
+
+
+def model_tables_digest(model: NccModel) -> int:
+    """FNV-1a 64 digest of the model's find tables (equal = bit-identical)."""
+    lib = load()
+    lib.mvg_ncc_model_tables_digest.argtypes = [C.c_void_p, C.POINTER(C.c_uint64)]
+    lib.mvg_ncc_model_tables_digest.restype = C.c_int32
+    d = C.c_uint64()
+    _check(lib.mvg_ncc_model_tables_digest(model.handle, C.byref(d)), "model_tables_digest")
+    return d.value
+
+
 def set_correlation_path(path: str) -> None:
     """'tensor' (default) or 'plain' for this thread's finds."""
     lib = load()

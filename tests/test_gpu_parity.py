@@ -149,6 +149,49 @@ def test_find_models_with_domain(mg):
             np.testing.assert_allclose(np.sort(x), np.sort(y[sel]), atol=1e-9)
 
 
+@pytest.fixture
+def host_build(mg):
+    yield
+    mg.ncc.set_model_build("device")
+
+
+@pytest.mark.parametrize("spec", [
+    dict(case="rot3_all"), dict(case="u16_rot"), dict(case="mask_disc"), dict(case="full_circle"),
+    dict(case="polarity"), dict(case="tiny16"), dict(case="big160"), dict(case="cfg1_s1"),
+    dict(case="rot3_all", levels=0, angle_start=-math.pi, angle_extent=2 * math.pi),
+    dict(case="cfg1_s1", levels=0, angle_start=-1.0, angle_extent=2.0, angle_step=0.03)])
+def test_device_model_build_bit_identical(mg, spec, host_build):
+    """The model built on the GPU has the host FP64 build's tables bit for
+    bit (weights, sample and run tables, descriptors)."""
+    case = CASES[spec["case"]]
+    wl, mask = make_inputs(case)
+    c = dict(case["create"])
+    c.update({k: v for k, v in spec.items() if k != "case"})
+    args = (wl.template, c["levels"] or "auto", c["angle_start"], c["angle_extent"], c.get("angle_step", 0) or "auto",
+            "ignore_global_polarity" if c.get("ignore_polarity") else "use_polarity")
+    mg.ncc.set_model_build("device")
+    dev = mg.create_ncc_model(*args, domain=mask)
+    mg.ncc.set_model_build("host")
+    host = mg.create_ncc_model(*args, domain=mask)
+    assert mg.ncc.model_tables_digest(dev) == mg.ncc.model_tables_digest(host)
+    assert mg.get_ncc_model_params(dev) == mg.get_ncc_model_params(host)
+
+
+def test_device_model_build_errors(mg, host_build):
+    """Both builds raise the reference's errors: a raster with fewer than
+    four samples, and the 16 M sample budget."""
+    tiny = np.array([[10, 200], [30, 90]], np.uint8)
+    big = (np.arange(700 * 700) % 251).astype(np.uint8).reshape(700, 700)
+    for where in ("device", "host"):
+        mg.ncc.set_model_build(where)
+        with pytest.raises(mg.MvError) as e:
+            mg.create_ncc_model(tiny, 1, 0.0, 1.0, "auto", "use_polarity")
+        assert e.value.status == -1 and "degenerate" in e.value.message
+        with pytest.raises(mg.MvError) as e:
+            mg.create_ncc_model(big, 1, -math.pi, 2 * math.pi, 0.01, "use_polarity")
+        assert e.value.status == -103 and "budget" in e.value.message
+
+
 def test_find_models_single_equals_find(mg):
     """One model through FindNccModels gives FindNccModel's matches."""
     case = CASES["rot3_all"]
