@@ -137,6 +137,33 @@ MVG_API int32_t mvg_find_ncc_models(const void* pixels, int32_t pixel_type, int6
                                     double* row, double* column, double* angle, double* score, int64_t* model,
                                     int64_t capacity, int64_t* count, void* stream);
 
+/* NCC adjoint with a scale degree of freedom (no counterpart in the rigid
+ * reference).  For each of `count` poses (row, column, angle, scale; 4
+ * doubles each, the matcher's pixel-centre image coordinates of the model
+ * origin, as mvg_find_ncc_model_stage reports them, scale 1 = trained size)
+ * it warps the model's unrotated level-0 raster by the similarity
+ * transform, samples the image bilinearly and returns the NCC in score[i]
+ * and its gradient d score / d (row, column, angle, scale) in
+ * gradient[4 i .. 4 i + 3].  A pose with a sample outside the image or a flat
+ * window gets score -inf and a zero gradient.  pixels/location as for
+ * mvg_find_ncc_model. */
+MVG_API int32_t mvg_ncc_score_gradient(const void* pixels, int32_t pixel_type, int64_t width, int64_t height,
+                                       int64_t row_stride, int32_t location, mvg_ncc_model model_id,
+                                       const double* poses, int64_t count, double* score, double* gradient,
+                                       void* stream);
+
+/* Gauss-Newton refinement of `count` similarity poses (row, column, angle,
+ * scale; as for mvg_ncc_score_gradient, refined in place) on the NCC above:
+ * the reference's refinement step (normal equations of the centred,
+ * normalised samples, FP64 solve with partial pivoting, steps clipped to
+ * 0.75 px, one trained angle step and 0.01 in scale, up to four halvings, a
+ * step only on a strictly higher score) with scale as a fourth parameter;
+ * at most `iterations` steps.  score[i]: NCC at the final pose. */
+MVG_API int32_t mvg_ncc_refine_similarity(const void* pixels, int32_t pixel_type, int64_t width, int64_t height,
+                                          int64_t row_stride, int32_t location, mvg_ncc_model model_id,
+                                          double* poses, int64_t count, int32_t iterations, double* score,
+                                          void* stream);
+
 /* Candidate list of one internal stage of a find, in the matcher's
  * pixel-centre pose convention (mv::ncc_matching::find,
  * src/ncc_matching/matcher.cpp:1063): stage 0 = coarse candidates after

@@ -87,7 +87,7 @@ struct DevLevel {
   DevBuf<PatchDesc> d_desc;
   DevBuf<int32_t> d_offs, d_runs, d_runs_end;
   DevBuf<float> d_w;
-  DevBuf<int2> d_sw, d_lw;
+  DevBuf<int2> d_sw, d_lw, d_run2;
   // Window geometry for a level of width x height: any rotation's raster
   // fits the diagonal; 5x5 placements and centre rounding add 8 cells.
   void set_geometry(size_t width, size_t height) {
@@ -149,6 +149,10 @@ struct DevLevel {
     retire(d_w);
     retire(d_sw);
     retire(d_lw);
+    retire(d_run2);
+    std::vector<int2> run2(runs.size());
+    for (size_t i = 0; i < runs.size(); ++i) run2[i] = make_int2(runs[i], runs_end[i]);
+    d_run2.upload(run2, nullptr);
     d_desc.upload(desc, nullptr);
     d_sw.upload(sw, nullptr);
     d_lw.upload(lw, nullptr);
@@ -169,6 +173,7 @@ struct DevLevel {
     v.lin_rows = lin_rows;
     v.runs = d_runs.p;
     v.runs_end = d_runs_end.p;
+    v.run2 = d_run2.p;
     v.npatches = int32_t(desc.size());
     return v;
   }
@@ -638,6 +643,7 @@ struct Workspace {
   DevBuf<uint8_t> dom_mask;          // search domain of the current find
   DevBuf<int32_t> dom_count, dom_row_run;
   DevBuf<int4> dom_runs;
+  DevBuf<double> adj_poses, adj_score, adj_grad;  // NCC adjoint calls
   DevBuf<uint16_t> tc_planes;
   DevBuf<int32_t> tc_order, tc_counts, tc_offsets, tc_cursor;
   DevBuf<TcTiles> tc_tiles;
@@ -2265,6 +2271,127 @@ int32_t mvg_find_ncc_models(const void* pixels, int32_t pixel_type, int64_t widt
       if (score) score[i] = c.score;
       if (model) model[i] = r[i].model;
     }
+  });
+}
+
+int32_t mvg_ncc_score_gradient(const void* pixels, int32_t pixel_type, int64_t width, int64_t height,
+                               int64_t row_stride, int32_t location, mvg_ncc_model model_id, const double* poses,
+                               int64_t count, double* score, double* gradient, void* stream) {
+  return guarded([&] {
+    if (!model_id) raise(kInvalidArgument, "control handle is not an NCC model");
+    if (pixel_type != 0 && pixel_type != 1) raise(kTypeMismatch, "one byte or uint2 channel required");
+    if (!pixels) raise(kInvalidArgument, "image pixels must not be null");
+    if (count < 0 || (count > 0 && (!poses || !score || !gradient)))
+      raise(kInvalidArgument, "poses, score and gradient arrays required");
+    if (width <= 0 || height <= 0 || width > std::numeric_limits<int>::max() ||
+        height > std::numeric_limits<int>::max() || height > 32000000 / width)
+      raise(kLimitExceeded, "search image exceeds pixel budget");
+    const int64_t bpp = pixel_type == 1 ? 2 : 1;
+    if (row_stride < width * bpp || row_stride % bpp) raise(kInvalidArgument, "invalid row stride");
+    for (int64_t i = 0; i < 4 * count; ++i)
+      if (!std::isfinite(poses[i])) raise(kInvalidArgument, "poses must be finite");
+    if (count == 0) return;
+    Workspace& ws = workspace();
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ws.own_stream;
+    OriginalView orig;
+    {
+      std::unique_lock<std::mutex> lock(model_id->mutex);
+      ensure_device(*model_id);
+      orig = model_id->original.view();
+    }
+    const void* dev = pixels;
+    if (location == MVG_MEMORY_HOST) {
+      const size_t bytes = size_t(row_stride) * size_t(height - 1) + size_t(width * bpp);
+      ws.image.reserve(bytes);
+      check(cudaMemcpyAsync(ws.image.p, pixels, bytes, cudaMemcpyHostToDevice, s), "image upload");
+      dev = ws.image.p;
+    }
+    check(cudaMemsetAsync(ws.state.p, 0, sizeof(QueryState), s), "memset");
+    LevelImage lev0{};
+    ws.lev_v[0].reserve(size_t(width) * size_t(height));
+    lev0.v = ws.lev_v[0].p;
+    lev0.w = int(width);
+    lev0.h = int(height);
+    check(launch_pyramid0(dev, pixel_type, row_stride / bpp, 0, 0, lev0, &ws.state.p->error, s), "pyramid0");
+    const size_t n = size_t(count);
+    ws.adj_poses.reserve(4 * n);
+    ws.adj_score.reserve(n);
+    ws.adj_grad.reserve(4 * n);
+    check(cudaMemcpyAsync(ws.adj_poses.p, poses, 4 * n * sizeof(double), cudaMemcpyHostToDevice, s), "poses");
+    AdjointArgs aa;
+    aa.img = ImageView{lev0.v, lev0.w, lev0.h, nullptr};
+    aa.orig = orig;
+    aa.poses = ws.adj_poses.p;
+    aa.n = int(count);
+    aa.score = ws.adj_score.p;
+    aa.grad = ws.adj_grad.p;
+    aa.absolute = model_id->host.params.ignore_polarity;
+    check(launch_adjoint(aa, s), "adjoint");
+    check(cudaMemcpyAsync(score, ws.adj_score.p, n * sizeof(double), cudaMemcpyDeviceToHost, s), "score");
+    check(cudaMemcpyAsync(gradient, ws.adj_grad.p, 4 * n * sizeof(double), cudaMemcpyDeviceToHost, s), "gradient");
+    check(cudaStreamSynchronize(s), "adjoint");
+  });
+}
+
+int32_t mvg_ncc_refine_similarity(const void* pixels, int32_t pixel_type, int64_t width, int64_t height,
+                                  int64_t row_stride, int32_t location, mvg_ncc_model model_id, double* poses,
+                                  int64_t count, int32_t iterations, double* score, void* stream) {
+  return guarded([&] {
+    if (!model_id) raise(kInvalidArgument, "control handle is not an NCC model");
+    if (pixel_type != 0 && pixel_type != 1) raise(kTypeMismatch, "one byte or uint2 channel required");
+    if (!pixels) raise(kInvalidArgument, "image pixels must not be null");
+    if (count < 0 || (count > 0 && (!poses || !score))) raise(kInvalidArgument, "poses and score arrays required");
+    if (iterations < 0 || iterations > 100) raise(kInvalidArgument, "iterations must be in [0, 100]");
+    if (width <= 0 || height <= 0 || width > std::numeric_limits<int>::max() ||
+        height > std::numeric_limits<int>::max() || height > 32000000 / width)
+      raise(kLimitExceeded, "search image exceeds pixel budget");
+    const int64_t bpp = pixel_type == 1 ? 2 : 1;
+    if (row_stride < width * bpp || row_stride % bpp) raise(kInvalidArgument, "invalid row stride");
+    for (int64_t i = 0; i < 4 * count; ++i)
+      if (!std::isfinite(poses[i])) raise(kInvalidArgument, "poses must be finite");
+    if (count == 0) return;
+    Workspace& ws = workspace();
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ws.own_stream;
+    OriginalView orig;
+    {
+      std::unique_lock<std::mutex> lock(model_id->mutex);
+      ensure_device(*model_id);
+      orig = model_id->original.view();
+    }
+    const void* dev = pixels;
+    if (location == MVG_MEMORY_HOST) {
+      const size_t bytes = size_t(row_stride) * size_t(height - 1) + size_t(width * bpp);
+      ws.image.reserve(bytes);
+      check(cudaMemcpyAsync(ws.image.p, pixels, bytes, cudaMemcpyHostToDevice, s), "image upload");
+      dev = ws.image.p;
+    }
+    check(cudaMemsetAsync(ws.state.p, 0, sizeof(QueryState), s), "memset");
+    LevelImage lev0{};
+    ws.lev_v[0].reserve(size_t(width) * size_t(height));
+    lev0.v = ws.lev_v[0].p;
+    lev0.w = int(width);
+    lev0.h = int(height);
+    check(launch_pyramid0(dev, pixel_type, row_stride / bpp, 0, 0, lev0, &ws.state.p->error, s), "pyramid0");
+    const size_t n = size_t(count);
+    ws.adj_poses.reserve(4 * n);
+    ws.adj_score.reserve(n);
+    check(cudaMemcpyAsync(ws.adj_poses.p, poses, 4 * n * sizeof(double), cudaMemcpyHostToDevice, s), "poses");
+    const HostModel& hm = model_id->host;
+    Refine4Args ra;
+    ra.img = ImageView{lev0.v, lev0.w, lev0.h, nullptr};
+    ra.orig = orig;
+    ra.poses = ws.adj_poses.p;
+    ra.score = ws.adj_score.p;
+    ra.n = int(count);
+    ra.iterations = iterations;
+    ra.absolute = hm.params.ignore_polarity;
+    ra.max_shift = .75;  // as the reference's step limit (matcher.cpp:931)
+    ra.max_angle = hm.params.angle_extent > 0 ? hm.params.angle_step : .01;
+    ra.max_scale = .01;
+    check(launch_refine4(ra, s), "refine4");
+    check(cudaMemcpyAsync(poses, ws.adj_poses.p, 4 * n * sizeof(double), cudaMemcpyDeviceToHost, s), "poses");
+    check(cudaMemcpyAsync(score, ws.adj_score.p, n * sizeof(double), cudaMemcpyDeviceToHost, s), "score");
+    check(cudaStreamSynchronize(s), "refine4");
   });
 }
 

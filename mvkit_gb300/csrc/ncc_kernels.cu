@@ -131,31 +131,56 @@ __device__ __forceinline__ float window_score(float dot, long long s1, long long
 // prefixes: runs first, first + step, ... (step > 1 splits the runs over
 // threads; the caller adds the parts).
 __device__ __forceinline__ void window_moments(const LevelImage& lev, int pitch, int r, int c,
-                                               const int32_t* __restrict__ runs, const int32_t* __restrict__ ends,
-                                               int nruns, long long& s1, long long& s2, int first = 0,
-                                               int step = 1) {
+                                               const int2* __restrict__ runs, int nruns, long long& s1, long long& s2,
+                                               int first = 0, int step = 1) {
   s1 = 0;
   s2 = 0;
   if (lev.prefix32) {
+    // four runs per step, all eight prefix loads issued before the sums
     const uint2* __restrict__ P = lev.prefix32;
-    for (int j = first; j < nruns; j += step) {
-      const int32_t rb = __ldg(runs + j);
-      const int e = __ldg(ends + j);
-      const size_t base = size_t(r + run_row(rb)) * pitch + c;
-      const uint2 hi = P[base + e + 1];
-      const uint2 lo = P[base + run_begin(rb)];
+    int j = first;
+    for (; j + 3 * step < nruns; j += 4 * step) {
+      int2 q[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) q[u] = __ldg(runs + j + u * step);
+      uint2 hi[4], lo[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const size_t base = size_t(r + run_row(q[u].x)) * pitch + c;
+        hi[u] = P[base + q[u].y + 1];
+        lo[u] = P[base + run_begin(q[u].x)];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        s1 += (long long)(hi[u].x - lo[u].x);
+        s2 += (long long)(hi[u].y - lo[u].y);
+      }
+    }
+    for (; j < nruns; j += step) {
+      const int2 q = __ldg(runs + j);
+      const size_t base = size_t(r + run_row(q.x)) * pitch + c;
+      const uint2 hi = P[base + q.y + 1];
+      const uint2 lo = P[base + run_begin(q.x)];
       s1 += (long long)(hi.x - lo.x);
       s2 += (long long)(hi.y - lo.y);
     }
     return;
   }
   const longlong2* __restrict__ P = lev.prefix;
-  for (int j = first; j < nruns; j += step) {
-    const int32_t rb = __ldg(runs + j);
-    const int e = __ldg(ends + j);
-    const size_t base = size_t(r + run_row(rb)) * pitch + c;
-    const longlong2 hi = P[base + e + 1];
-    const longlong2 lo = P[base + run_begin(rb)];
+  int j = first;
+  for (; j + step < nruns; j += 2 * step) {
+    const int2 q0 = __ldg(runs + j), q1 = __ldg(runs + j + step);
+    const size_t b0 = size_t(r + run_row(q0.x)) * pitch + c, b1 = size_t(r + run_row(q1.x)) * pitch + c;
+    const longlong2 h0 = P[b0 + q0.y + 1], l0 = P[b0 + run_begin(q0.x)];
+    const longlong2 h1 = P[b1 + q1.y + 1], l1 = P[b1 + run_begin(q1.x)];
+    s1 += (h0.x - l0.x) + (h1.x - l1.x);
+    s2 += (h0.y - l0.y) + (h1.y - l1.y);
+  }
+  for (; j < nruns; j += step) {
+    const int2 q = __ldg(runs + j);
+    const size_t base = size_t(r + run_row(q.x)) * pitch + c;
+    const longlong2 hi = P[base + q.y + 1];
+    const longlong2 lo = P[base + run_begin(q.x)];
     s1 += hi.x - lo.x;
     s2 += hi.y - lo.y;
   }
@@ -274,7 +299,7 @@ __global__ void __launch_bounds__(256) coarse_kernel(CoarseArgs a) {
       acc0 = fmaf(__int_as_float(x.y), base[off_row(x.x) * TW + off_col(x.x)] - s0, acc0);
     }
     long long s1, s2;
-    window_moments(a.lev, w + 1, r, c, a.view.runs + pd.run_off, a.view.runs_end + pd.run_off, pd.nruns, s1, s2);
+    window_moments(a.lev, w + 1, r, c, a.view.run2 + pd.run_off, pd.nruns, s1, s2);
     score = window_score(acc0 + acc1, s1, s2, pd.n, a.absolute);
   }
   a.planes[(size_t(p) * h + r) * w + c] = score;
@@ -327,7 +352,7 @@ __global__ void coarse_tc_score_kernel(CoarseTcArgs a) {
     const int ci = (src * a.lat_r + r / 5) * a.lat_c + c / 5;
     const int pos = (r % 5) * 5 + c % 5, k = a.k_of[j];
     long long s1, s2;
-    window_moments(a.lev, w + 1, r, c, a.view.runs + pd.run_off, a.view.runs_end + pd.run_off, pd.nruns, s1, s2);
+    window_moments(a.lev, w + 1, r, c, a.view.run2 + pd.run_off, pd.nruns, s1, s2);
     // sum w (S - S0) = sum w S - S0 sum w (first sample S0)
     const int2 f0 = __ldg(a.view.sw + pd.sample_off);
     const float s0 = a.lev.v[size_t(r + off_row(f0.x)) * w + c + off_col(f0.x)];
@@ -569,7 +594,7 @@ __global__ void __launch_bounds__(kTrackThreads, 5) track_kernel(TrackArgs a) {
     // like the samples; otherwise in slice 0
     long long s1 = 0, s2 = 0;
     if (valid && (s_m1 || part == 0))
-      window_moments(a.lev, pitch + 1, r, c, a.view.runs + pd.run_off, a.view.runs_end + pd.run_off, pd.nruns, s1,
+      window_moments(a.lev, pitch + 1, r, c, a.view.run2 + pd.run_off, pd.nruns, s1,
                      s2, s_m1 ? part : 0, s_m1 ? split : 1);
     // combine the slices of one item (threads item + q * items)
     if (split > 1) {
@@ -960,6 +985,306 @@ __global__ void __launch_bounds__(128) score_kernel(ScoreArgs a) {
   const double col = (c.col - a.crop_col - a.phase) / a.scale;
   continuous_pass(a.img, a.orig, row, col, c.angle, a.absolute, sh);
   if (threadIdx.x == 0) a.cand[i].score = sh.score;
+}
+
+// ------------------------------------------------------------- NCC adjoint
+// Scale degree of freedom (no counterpart in the rigid reference).  Sample i
+// of the original (offsets dr, dc from the model origin, weight w) lands at
+//   y = row + s (ca dr - sa dc),  x = col + s (sa dr + ca dc),
+// q_i is the bilinear image value there, and
+//   NCC = D / sqrt(E),  D = sum w q - (sum q / n) sum w,  E = sum q^2 - (sum q)^2 / n
+// (continuous(), src/ncc_matching/matcher.cpp:121-157, with the scale).  With
+// the bilinear cell gradient (gy, gx), dq/dp = gy dy/dp + gx dx/dp for p in
+// (row, col, angle, scale), and
+//   dNCC = dD / sqrt(E) - D dE / (2 E^1.5),
+//   dD = sum w dq - (sum dq / n) sum w,  dE = 2 sum q dq - 2 (sum q)(sum dq) / n.
+// Per-thread sums in FP32 (q centred by the first sample, which changes
+// neither NCC nor its gradient), block totals as FP32 pairs, the final
+// algebra in FP64.
+constexpr int kAdjointThreads = 256;
+
+__global__ void __launch_bounds__(kAdjointThreads) adjoint_kernel(AdjointArgs a) {
+  __shared__ float scratch[17 * 64];
+  __shared__ float s_off;
+  const int k = blockIdx.x;
+  if (k >= a.n) return;
+  const double row = a.poses[4 * k], col = a.poses[4 * k + 1], angle = a.poses[4 * k + 2],
+               scale = a.poses[4 * k + 3];
+  const ImageView img = a.img;
+  const OriginalView orig = a.orig;
+  const double R = floor(row), Cc = floor(col);
+  const int R0 = int(R), C0 = int(Cc);
+  const float fr = float(row - R), fc = float(col - Cc);
+  double sd, cd;
+  sincos(angle, &sd, &cd);
+  const float ca = float(cd), sa = float(sd), sc = float(scale);
+  const float hmin = float(-R0), wmin = float(-C0), hmax = float(img.h - 1 - R0), wmax = float(img.w - 1 - C0);
+  if (threadIdx.x == 0) {
+    float off = 0.f;
+    const float u = ca * orig.dr[0] - sa * orig.dc[0], v = sa * orig.dr[0] + ca * orig.dc[0];
+    const float y = fr + sc * u, x = fc + sc * v;
+    if (y >= hmin && x >= wmin && y <= hmax && x <= wmax) {
+      const float fy0 = floorf(y), fx0 = floorf(x);
+      const int r = R0 + int(fy0), c = C0 + int(fx0);
+      off = bilinear_at(img, r, c, y - fy0, x - fx0, min(r + 1, img.h - 1), min(c + 1, img.w - 1));
+    }
+    s_off = off;
+  }
+  __syncthreads();
+  const float off = s_off;
+  // 0 sum q, 1 sum q^2, 2 sum w q, 3..6 sum dq, 7..10 sum q dq, 11..14 sum w dq, 15 sum w, 16 outside
+  float acc[17];
+#pragma unroll
+  for (int j = 0; j < 17; ++j) acc[j] = 0.f;
+  for (int s = threadIdx.x; s < orig.n; s += blockDim.x) {
+    const float4 p = __ldg(orig.dcw + s);
+    const float u = ca * p.x - sa * p.y, v = sa * p.x + ca * p.y;
+    const float y = fr + sc * u, x = fc + sc * v;
+    acc[15] += p.z;
+    if (!(y >= hmin && x >= wmin && y <= hmax && x <= wmax)) {
+      acc[16] = 1.f;
+      continue;
+    }
+    const float fy0 = floorf(y), fx0 = floorf(x);
+    const float fy = y - fy0, fx = x - fx0;
+    const int r = R0 + int(fy0), c = C0 + int(fx0);
+    const int r1 = min(r + 1, img.h - 1), c1 = min(c + 1, img.w - 1);
+    const float va = __ldg(img.v + size_t(r) * img.w + c), vb = __ldg(img.v + size_t(r) * img.w + c1);
+    const float vd = __ldg(img.v + size_t(r1) * img.w + c), ve = __ldg(img.v + size_t(r1) * img.w + c1);
+    const float q = (1 - fy) * ((1 - fx) * va + fx * vb) + fy * ((1 - fx) * vd + fx * ve) - off;
+    const float gy = (1 - fx) * (vd - va) + fx * (ve - vb), gx = (1 - fy) * (vb - va) + fy * (ve - vd);
+    // dy/dp, dx/dp: row (1, 0), col (0, 1), angle (-s v, s u), scale (u, v)
+    const float dq[4] = {gy, gx, sc * (gx * u - gy * v), gy * u + gx * v};
+    acc[0] += q;
+    acc[1] = fmaf(q, q, acc[1]);
+    acc[2] = fmaf(p.z, q, acc[2]);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      acc[3 + j] += dq[j];
+      acc[7 + j] = fmaf(q, dq[j], acc[7 + j]);
+      acc[11 + j] = fmaf(p.z, dq[j], acc[11 + j]);
+    }
+  }
+  F2 t[17];
+  block_total<17>(acc, t, scratch);
+  if (threadIdx.x == 0) {
+    auto dv = [](const F2& x) { return double(x.hi) + double(x.lo); };
+    const double n = double(orig.n);
+    const double sq = dv(t[0]), sqq = dv(t[1]), swq = dv(t[2]), sw = dv(t[15]);
+    const double D = swq - sq / n * sw, E = sqq - sq * sq / n;
+    double* g = a.grad + 4 * k;
+    if (t[16].hi > 0 || !(E > 0)) {
+      a.score[k] = -INFINITY;
+      g[0] = g[1] = g[2] = g[3] = 0;
+      return;
+    }
+    const double rs = 1 / sqrt(E);
+    double ncc = D * rs;
+    const double sign = a.absolute && ncc < 0 ? -1. : 1.;
+    a.score[k] = sign * ncc;
+    for (int j = 0; j < 4; ++j) {
+      const double sdq = dv(t[3 + j]), sqdq = dv(t[7 + j]), swdq = dv(t[11 + j]);
+      const double dD = swdq - sdq / n * sw, dE = 2 * (sqdq - sq * sdq / n);
+      g[j] = sign * (dD * rs - D * dE * .5 * rs * rs * rs);
+    }
+  }
+}
+
+// Similarity pass for the 4-parameter refinement: per-thread sums of
+// 0 q, 1 q^2, 2 w q, 3..6 g, 7..10 q g, 11..14 w g, 15..24 g_i g_j (i <= j),
+// 25 w, 26 outside, with g = dq / d(row, col, angle, scale).
+constexpr int kSimSums = 27;
+
+__device__ void sim_pass(const ImageView& img, const OriginalView& orig, const double* pose, bool derivs,
+                         float (&acc)[kSimSums], float* s_off) {
+  const double R = floor(pose[0]), Cc = floor(pose[1]);
+  const int R0 = int(R), C0 = int(Cc);
+  const float fr = float(pose[0] - R), fc = float(pose[1] - Cc);
+  double sd, cd;
+  sincos(pose[2], &sd, &cd);
+  const float ca = float(cd), sa = float(sd), sc = float(pose[3]);
+  const float hmin = float(-R0), wmin = float(-C0), hmax = float(img.h - 1 - R0), wmax = float(img.w - 1 - C0);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float off = 0.f;
+    const float u = ca * orig.dr[0] - sa * orig.dc[0], v = sa * orig.dr[0] + ca * orig.dc[0];
+    const float y = fr + sc * u, x = fc + sc * v;
+    if (y >= hmin && x >= wmin && y <= hmax && x <= wmax) {
+      const float fy0 = floorf(y), fx0 = floorf(x);
+      const int r = R0 + int(fy0), c = C0 + int(fx0);
+      off = bilinear_at(img, r, c, y - fy0, x - fx0, min(r + 1, img.h - 1), min(c + 1, img.w - 1));
+    }
+    *s_off = off;
+  }
+  __syncthreads();
+  const float off = *s_off;
+#pragma unroll
+  for (int j = 0; j < kSimSums; ++j) acc[j] = 0.f;
+  for (int s = threadIdx.x; s < orig.n; s += blockDim.x) {
+    const float4 p = __ldg(orig.dcw + s);
+    const float u = ca * p.x - sa * p.y, v = sa * p.x + ca * p.y;
+    const float y = fr + sc * u, x = fc + sc * v;
+    acc[25] += p.z;
+    if (!(y >= hmin && x >= wmin && y <= hmax && x <= wmax)) {
+      acc[26] = 1.f;
+      continue;
+    }
+    const float fy0 = floorf(y), fx0 = floorf(x);
+    const float fy = y - fy0, fx = x - fx0;
+    const int r = R0 + int(fy0), c = C0 + int(fx0);
+    const int r1 = min(r + 1, img.h - 1), c1 = min(c + 1, img.w - 1);
+    const float va = __ldg(img.v + size_t(r) * img.w + c), vb = __ldg(img.v + size_t(r) * img.w + c1);
+    const float vd = __ldg(img.v + size_t(r1) * img.w + c), ve = __ldg(img.v + size_t(r1) * img.w + c1);
+    const float q = (1 - fy) * ((1 - fx) * va + fx * vb) + fy * ((1 - fx) * vd + fx * ve) - off;
+    acc[0] += q;
+    acc[1] = fmaf(q, q, acc[1]);
+    acc[2] = fmaf(p.z, q, acc[2]);
+    if (!derivs) continue;
+    const float gy = (1 - fx) * (vd - va) + fx * (ve - vb), gx = (1 - fy) * (vb - va) + fy * (ve - vd);
+    const float g[4] = {gy, gx, sc * (gx * u - gy * v), gy * u + gx * v};
+    int at = 15;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      acc[3 + i] += g[i];
+      acc[7 + i] = fmaf(q, g[i], acc[7 + i]);
+      acc[11 + i] = fmaf(p.z, g[i], acc[11 + i]);
+#pragma unroll
+      for (int j = i; j < 4; ++j) {
+        acc[at] = fmaf(g[i], g[j], acc[at]);
+        ++at;
+      }
+    }
+  }
+}
+
+// One block per pose.  Each iteration: the normal equations of the NCC in
+// the four parameters (Gauss-Newton on the centred, normalised samples, as
+// the reference's refinement_step), an FP64 Gauss-Jordan solve with partial
+// pivoting, the step clipped to the limits, and up to four halvings; a step
+// is taken only when the score strictly increases.
+constexpr int kRefine4Threads = 256;
+
+__global__ void __launch_bounds__(kRefine4Threads) refine4_kernel(Refine4Args a) {
+  __shared__ float scratch[kSimSums * 64];
+  __shared__ float s_off;
+  __shared__ double s_pose[4], s_try[4], s_delta[4], s_score, s_factor;
+  __shared__ int s_go;
+  const int k = blockIdx.x;
+  if (k >= a.n) return;
+  if (threadIdx.x < 4) s_pose[threadIdx.x] = a.poses[4 * k + threadIdx.x];
+  if (threadIdx.x == 0) s_score = -INFINITY;
+  __syncthreads();
+  float acc[kSimSums];
+  F2 t[kSimSums];
+  auto dv = [](const F2& x) { return double(x.hi) + double(x.lo); };
+  const double n = double(a.orig.n);
+  for (int it = 0; it <= a.iterations; ++it) {
+    sim_pass(a.img, a.orig, s_pose, true, acc, &s_off);
+    block_total<kSimSums>(acc, t, scratch);
+    if (threadIdx.x == 0) {
+      s_go = 0;
+      const double sq = dv(t[0]), sqq = dv(t[1]), swq = dv(t[2]), sw = dv(t[25]);
+      const double E = sqq - sq * sq / n, D = swq - sq / n * sw;
+      if (t[26].hi == 0 && E > 0) {
+        const double rs = 1 / sqrt(E);
+        const double ncc = D * rs, sign = a.absolute && ncc < 0 ? -1. : 1.;
+        s_score = sign * ncc;
+        if (it < a.iterations) {
+          double m[4][5];
+          double gi[4], qi[4];
+          for (int i = 0; i < 4; ++i) {
+            gi[i] = dv(t[3 + i]);
+            qi[i] = dv(t[7 + i]) - sq / n * gi[i];
+          }
+          int at = 15;
+          for (int i = 0; i < 4; ++i)
+            for (int j = i; j < 4; ++j, ++at) {
+              const double e = ((dv(t[at]) - gi[i] * gi[j] / n) - qi[i] * qi[j] / E) / E;
+              m[i][j] = m[j][i] = e;
+            }
+          for (int i = 0; i < 4; ++i)
+            m[i][4] = sign * (dv(t[11 + i]) - gi[i] / n * sw) * rs - s_score * qi[i] / E;
+          bool good = true;
+          for (int i = 0; i < 4 && good; ++i) {
+            int pv = i;
+            for (int j = i + 1; j < 4; ++j)
+              if (fabs(m[j][i]) > fabs(m[pv][i])) pv = j;
+            if (fabs(m[pv][i]) < 1e-14) {
+              good = false;
+              break;
+            }
+            for (int c = i; c < 5; ++c) {
+              const double tmp = m[i][c];
+              m[i][c] = m[pv][c];
+              m[pv][c] = tmp;
+            }
+            const double inv = 1 / m[i][i];
+            for (int c = i; c < 5; ++c) m[i][c] *= inv;
+            for (int j = 0; j < 4; ++j)
+              if (j != i) {
+                const double f = m[j][i];
+                for (int c = i; c < 5; ++c) m[j][c] -= f * m[i][c];
+              }
+          }
+          if (good) {
+            for (int i = 0; i < 4; ++i) s_delta[i] = m[i][4];
+            double f = 1;
+            f = fmin(f, a.max_shift / fmax(1e-20, fabs(s_delta[0])));
+            f = fmin(f, a.max_shift / fmax(1e-20, fabs(s_delta[1])));
+            f = fmin(f, a.max_angle / fmax(1e-20, fabs(s_delta[2])));
+            f = fmin(f, a.max_scale / fmax(1e-20, fabs(s_delta[3])));
+            s_factor = f;
+            s_go = isfinite(f) && isfinite(s_delta[0]) && isfinite(s_delta[1]) && isfinite(s_delta[2]) &&
+                   isfinite(s_delta[3]);
+          }
+        }
+      }
+    }
+    __syncthreads();
+    if (!s_go) break;
+    bool accepted = false;
+    for (int bt = 0; bt < 4 && !accepted; ++bt) {
+      if (threadIdx.x < 4) s_try[threadIdx.x] = s_pose[threadIdx.x] + ldexp(s_factor, -bt) * s_delta[threadIdx.x];
+      __syncthreads();
+      sim_pass(a.img, a.orig, s_try, false, acc, &s_off);
+      block_total<kSimSums>(acc, t, scratch);
+      if (threadIdx.x == 0) {
+        const double sq = dv(t[0]), sqq = dv(t[1]), swq = dv(t[2]), sw = dv(t[25]);
+        const double E = sqq - sq * sq / n, D = swq - sq / n * sw;
+        s_go = 0;
+        if (t[26].hi == 0 && E > 0) {
+          const double ncc = D / sqrt(E), sc = a.absolute ? fabs(ncc) : ncc;
+          if (sc > s_score) {
+            for (int i = 0; i < 4; ++i) s_pose[i] = s_try[i];
+            s_go = 1;
+          }
+        }
+      }
+      __syncthreads();
+      accepted = s_go != 0;
+    }
+    if (!accepted) break;
+    if (threadIdx.x == 0) {
+      const double st = s_factor;
+      s_go = hypot(st * s_delta[0], st * s_delta[1]) >= 1e-4 || fabs(st * s_delta[2]) >= 1e-5 ||
+             fabs(st * s_delta[3]) >= 1e-6;
+    }
+    __syncthreads();
+    if (!s_go) {
+      // converged: the score at the final pose
+      sim_pass(a.img, a.orig, s_pose, false, acc, &s_off);
+      block_total<kSimSums>(acc, t, scratch);
+      if (threadIdx.x == 0) {
+        const double sq = dv(t[0]), sqq = dv(t[1]), swq = dv(t[2]), sw = dv(t[25]);
+        const double E = sqq - sq * sq / n, D = swq - sq / n * sw;
+        s_score = t[26].hi == 0 && E > 0 ? (a.absolute ? fabs(D / sqrt(E)) : D / sqrt(E)) : -INFINITY;
+      }
+      __syncthreads();
+      break;
+    }
+  }
+  if (threadIdx.x < 4) a.poses[4 * k + threadIdx.x] = s_pose[threadIdx.x];
+  if (threadIdx.x == 0) a.score[k] = s_score;
 }
 
 // --------------------------------------------------------------------- sort
@@ -1869,6 +2194,18 @@ cudaError_t launch_dedup(const DedupArgs& a, int max_candidates, cudaStream_t s)
   if (a.snap)
     snap_kernel<<<blocks, 256, 0, s>>>(const_cast<Cand*>(a.in), a.state, a.in_slot, a.height, a.width, a.dom);
   dedup_kernel<<<blocks, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint(const AdjointArgs& a, cudaStream_t s) {
+  if (a.n <= 0) return cudaSuccess;
+  adjoint_kernel<<<a.n, kAdjointThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_refine4(const Refine4Args& a, cudaStream_t s) {
+  if (a.n <= 0) return cudaSuccess;
+  refine4_kernel<<<a.n, kRefine4Threads, 0, s>>>(a);
   return cudaGetLastError();
 }
 

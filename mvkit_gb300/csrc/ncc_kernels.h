@@ -245,6 +245,33 @@ struct ScoreArgs {
   int absolute;
 };
 
+// NCC of the unrotated original raster warped by a similarity pose (row,
+// column, angle, scale; pixel-centre image coordinates, the model origin at
+// (row, column)) and its gradient in the four parameters.  One block per pose.
+struct AdjointArgs {
+  ImageView img;            // level 0: the search image as float
+  OriginalView orig;
+  const double* poses;      // n x 4
+  int n;
+  double* score;            // n (-inf where a sample leaves the image or the window is flat)
+  double* grad;             // n x 4 (0 where the score is -inf)
+  int absolute;             // ignore_global_polarity
+};
+
+// Gauss-Newton refinement of similarity poses (row, column, angle, scale)
+// on the NCC above: the reference's refinement step (3 parameters,
+// src/ncc_matching/matcher.cpp:170-240, 903-982) with scale as a fourth.
+struct Refine4Args {
+  ImageView img;
+  OriginalView orig;
+  double* poses;            // n x 4, refined in place
+  double* score;            // n: score at the final pose (-inf if unscorable)
+  int n;
+  int iterations;           // Gauss-Newton steps (at most)
+  int absolute;
+  double max_shift, max_angle, max_scale;  // step limits per iteration
+};
+
 struct SortArgs {
   const Cand* in;
   Cand* out;
@@ -307,6 +334,8 @@ cudaError_t launch_nms(const NmsArgs& a, cudaStream_t s);
 cudaError_t launch_track(const TrackArgs& a, int max_candidates, cudaStream_t s, size_t smem_limit);
 cudaError_t launch_dedup(const DedupArgs& a, int max_candidates, cudaStream_t s);
 cudaError_t launch_score(const ScoreArgs& a, int max_candidates, cudaStream_t s);
+cudaError_t launch_adjoint(const AdjointArgs& a, cudaStream_t s);
+cudaError_t launch_refine4(const Refine4Args& a, cudaStream_t s);
 cudaError_t launch_sort(const SortArgs& a, cudaStream_t s);
 cudaError_t launch_rects(const Cand* sorted, RectAux* aux, const QueryState* state, RectGeom g, int max_candidates,
                          cudaStream_t s);

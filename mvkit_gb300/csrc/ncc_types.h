@@ -50,6 +50,7 @@ struct LevelView {
   int32_t lin_rows;             // rows of a window that holds any 5x5 placement set
   const int32_t* runs;          // packed row(16) | begin; end in runs_end
   const int32_t* runs_end;
+  const int2* run2;             // the same interleaved: {packed row | begin, end}
   int32_t npatches;
 };
 

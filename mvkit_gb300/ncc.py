@@ -457,6 +457,59 @@ def find_ncc_models(image, models, angle_start, angle_extent, min_score, num_mat
         cap = int(cnt.value)
 
 
+def ncc_score_gradient(image, model: NccModel, poses, stream=None):
+    """NCC of the model's unrotated level-0 raster under similarity poses and
+    its gradient (scale degree of freedom; no counterpart in the reference).
+
+    poses: (n, 4) float64 rows (row, column, angle, scale) in the matcher's
+    pixel-centre image coordinates of the model origin.  Returns (score (n,),
+    gradient (n, 4)): d score / d (row, column, angle, scale)."""
+    op = "ncc_score_gradient"
+    if not isinstance(model, NccModel) or not model.handle:
+        raise MvError(MV_STATUS_TYPE_MISMATCH, "ModelID: NCC model handle required", op)
+    p = np.ascontiguousarray(np.asarray(poses, dtype=np.float64).reshape(-1, 4))
+    if isinstance(image, DeviceImage):
+        ptr, typ, (h, w), stride, loc = image.ptr, image.type, image.shape, image.stride, 1
+    else:
+        a, typ = _image(image, op, "Image")
+        ptr, (h, w), stride, loc = a.ctypes.data, a.shape, a.strides[0], 0
+    n = p.shape[0]
+    score = np.zeros(n)
+    grad = np.zeros((n, 4))
+    lib = load()
+    lib.mvg_ncc_score_gradient.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int32,
+                                           C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.mvg_ncc_score_gradient.restype = C.c_int32
+    _check(lib.mvg_ncc_score_gradient(ptr, typ, w, h, stride, loc, model.handle, p.ctypes.data, n, score.ctypes.data,
+                                      grad.ctypes.data, C.c_void_p(stream) if stream else None), op)
+    return score, grad
+
+
+def ncc_refine_similarity(image, model: NccModel, poses, iterations: int = 20, stream=None):
+    """Gauss-Newton refinement of similarity poses (row, column, angle,
+    scale) on the NCC of ncc_score_gradient.  Returns (refined poses (n, 4),
+    score (n,))."""
+    op = "ncc_refine_similarity"
+    if not isinstance(model, NccModel) or not model.handle:
+        raise MvError(MV_STATUS_TYPE_MISMATCH, "ModelID: NCC model handle required", op)
+    p = np.array(np.asarray(poses, dtype=np.float64).reshape(-1, 4), copy=True, order="C")
+    if isinstance(image, DeviceImage):
+        ptr, typ, (h, w), stride, loc = image.ptr, image.type, image.shape, image.stride, 1
+    else:
+        a, typ = _image(image, op, "Image")
+        ptr, (h, w), stride, loc = a.ctypes.data, a.shape, a.strides[0], 0
+    n = p.shape[0]
+    score = np.zeros(n)
+    lib = load()
+    lib.mvg_ncc_refine_similarity.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int32,
+                                              C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_void_p]
+    lib.mvg_ncc_refine_similarity.restype = C.c_int32
+    _check(lib.mvg_ncc_refine_similarity(ptr, typ, w, h, stride, loc, model.handle, p.ctypes.data, n,
+                                         int(iterations), score.ctypes.data, C.c_void_p(stream) if stream else None),
+           op)
+    return p, score
+
+
 def find_ncc_model_stage(image, model: NccModel, angle_start, angle_extent, min_score, num_matches, max_overlap,
                          subpixel, num_levels, stage: int, domain=None) -> np.ndarray:
     """Candidate list of an internal stage (n x 4: row, column, angle, score;
