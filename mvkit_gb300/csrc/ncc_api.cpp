@@ -478,6 +478,28 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
     protos.push_back(std::move(pr));
   }
   if (protos.empty()) return plan;
+  // costliest groups first: their tiles come first in the tile list, and the
+  // kernel hands tiles out in list order (longest tiles first balances the
+  // blocks' last tiles)
+  {
+    auto cost = [&](const Proto& pr) {
+      return double((pr.kr + pr.rg - 1) / pr.rg) * double(parts * pr.kw + 16) * double(pr.n);
+    };
+    std::vector<int> order(protos.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = int(i);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int x, int y) { return cost(protos[size_t(x)]) > cost(protos[size_t(y)]); });
+    std::vector<int> rank(protos.size());
+    std::vector<Proto> sorted;
+    sorted.reserve(protos.size());
+    for (size_t i = 0; i < order.size(); ++i) {
+      rank[size_t(order[i])] = int(i);
+      sorted.push_back(std::move(protos[size_t(order[i])]));
+    }
+    protos = std::move(sorted);
+    for (int32_t& g : plan->group_of_src)
+      if (g >= 0) g = rank[size_t(g)];
+  }
   // one launch shape for the step: weight buffers from the largest chunk, the
   // window slab as tall as every group allows
   size_t max_chunk = 0;

@@ -316,6 +316,7 @@ __global__ void coarse_lattice_kernel(Cand* cand, int2* rc, int nsrc, int nbr, i
   if (i == 0) {
     state->count[slot] = nsrc * nb;
     tiles->count = nsrc * tps;
+    tiles->next = 0;
   }
   if (i < nsrc * tps) {
     const int src = i / tps, u = i % tps;

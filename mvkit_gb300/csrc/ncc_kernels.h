@@ -165,6 +165,7 @@ struct TcGroup {
 
 struct TcTiles {
   int count;
+  int next;                              // tiles handed out after the first gridDim.x (reset with count)
   int group[kTcMaxTiles], first[kTcMaxTiles], last[kTcMaxTiles];
 };
 

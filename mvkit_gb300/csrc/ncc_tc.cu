@@ -133,6 +133,7 @@ struct __align__(16) TcShared {
   TcGroup grp;
   uint32_t tmem;
   int fail, cnt;
+  int next_tile;     // the block's next tile (dynamic scheduling)
   long long cm, cb;  // weight chunks consumed (MMA thread) / loaded (weight producer)
   int sm, sa;        // window slabs consumed (MMA thread) / staged (window producer)
   int ci[kTcCands], R[kTcCands], C[kTcCands], x0a[kTcCands], delta[kTcCands];
@@ -295,7 +296,9 @@ __device__ void tc_weight_role(const TcArgs& a, TcShared& sh, uint8_t* wbase, Ri
   }
 }
 
-// Persistent and warp-specialised: block b takes tiles b, b + gridDim.x, ...;
+// Persistent and warp-specialised: block b takes tile b first, then the
+// next unclaimed tile from a global counter (tiles differ in cost, so a
+// static stride leaves blocks idle at the end);
 // per tile warp 0 issues the MMAs, warp 1 streams weights, warps 2-5 stage
 // windows, and all six warps run the set-up and the epilogue.  Shared
 // memory: weight ring (stages x stage_bytes) | two window buffers.
@@ -335,7 +338,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const uint32_t tmem = sh.tmem;
   RingPos cm, cb;            // role-local ring positions (MMA thread, weight producer)
   int sm = 0, sa = 0;        // role-local counters (MMA thread, window producer)
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  for (int tile = blockIdx.x; tile < ntiles; tile = sh.next_tile) {
     // tile set-up: the group into shared memory, one candidate per thread
     {
       const int gi = a.tiles->group[tile];
@@ -480,6 +483,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     // generic accesses of the buffers before the next tile's async writes
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (t == 0) sh.next_tile = int(gridDim.x) + atomicAdd(&a.tiles->next, 1);
     __syncthreads();
   }
   __syncthreads();
@@ -562,7 +566,10 @@ __global__ void __launch_bounds__(1024) tc_plan_kernel(const int32_t* counts, in
     }
     at += cg;
   }
-  if (t == 1023) tiles->count = min(s_tile[1023], max_tiles);
+  if (t == 1023) {
+    tiles->count = min(s_tile[1023], max_tiles);
+    tiles->next = 0;
+  }
 }
 
 __global__ void tc_scatter_kernel(const Cand* in, const QueryState* state, int slot, const int32_t* group_of_src,
