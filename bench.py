@@ -9,8 +9,9 @@ A step is one find on each of `--batch` distinct scenes.
 value: images/s with the scenes resident in HBM (CUDA events on the find
 stream, L2 flushed between steps).  e2e: the same through the C ABI with
 page-locked host buffers (upload and result read-back inside the timed
-region).  roofline: the kernel with the largest event-time share, its
-algorithmic multiply-adds over its live event time.  cpu_baseline: the FP64
+region).  roofline: the correlation kernel, its algorithmic multiply-adds
+over its live event time, from a second timed pass of the same steps with
+CUDA events around each kernel group (the value pass carries no events).  cpu_baseline: the FP64
 oracle restatement of the reference on this host's cores (one scene per
 thread).
 
@@ -140,6 +141,22 @@ def cpu_baseline(images, threads: int) -> dict:
     return {"value": len(sample) / dt, "unit": "images/s", "cores": threads, "kind": "port",
             "sample": f"{len(sample)} scenes of {WORKLOAD}, one per thread, FP64 oracle restatement "
                       f"of the reference scalar path ({n} matches)", "seconds": dt}
+
+
+def max_over_ranks(x: float, device: str = "cuda") -> float:
+    """The largest x over the replicas (all-reduce MAX); x itself on one."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(images_per_rank: int, world: int, slowest_ms: float) -> float:
+    """Whole-job images/s: every replica's images over the slowest replica's time."""
+    return images_per_rank * world / (slowest_ms / 1e3)
 
 
 def run_reference(args) -> None:
@@ -291,7 +308,8 @@ def main():
         for _ in range(args.warmup):
             one_step(dev, False)
         torch.cuda.synchronize()
-        other_ms = timed(dev, False, args.steps, profile=True)
+        other_ms = timed(dev, False, args.steps)
+        timed(dev, False, args.steps, profile=True)
         oprof = aggregate()
         other = {"path": path[0], "ms": other_ms,
                  "stages_ms_per_find": {k: round(v["ms"] / max(1, oprof["finds"]), 4) for k, v in oprof.items()
@@ -304,7 +322,11 @@ def main():
     torch.cuda.synchronize()
 
     with ClockSampler(local) as clocks:
-        dev_ms = timed(dev, False, args.steps, profile=True)
+        dev_ms = timed(dev, False, args.steps)
+    # the same steps again with CUDA events around each kernel group on the
+    # find streams: stage times, launch counts and the roofline (the events
+    # stay out of the value pass)
+    timed(dev, False, args.steps, profile=True)
     prof = aggregate()
     host_ms = timed(pinned, True, args.steps)
 
@@ -322,19 +344,12 @@ def main():
 
     iso = pool.submit(isolated).result()
 
-    def maxed(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
-
+    maxed = max_over_ranks
     dev_ms, host_ms = maxed(dev_ms), maxed(host_ms)
     if other is not None:
-        other["value"] = args.steps * args.batch * world / (maxed(other.pop("ms")) / 1e3)
-    images = args.steps * args.batch * world
-    value = images / (dev_ms / 1e3)
-    e2e = images / (host_ms / 1e3)
+        other["value"] = replica_value(args.steps * args.batch, world, maxed(other.pop("ms")))
+    value = replica_value(args.steps * args.batch, world, dev_ms)
+    e2e = replica_value(args.steps * args.batch, world, host_ms)
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
