@@ -368,3 +368,53 @@ def test_model_params(mg):
     assert a0 == case["create"]["angle_start"] and a1 == case["create"]["angle_extent"]
     assert step == GOLDEN["rot3_all"]["angle_step"]
     assert metric == "use_polarity"
+
+
+def _sweep_case(seed):
+    """A seeded small search: image type, size, template, angle range, levels,
+    controls, polarity and an optional search domain drawn from the seed."""
+    rng = np.random.default_rng(1000 + seed)
+    u16 = bool(rng.integers(0, 4) == 0)
+    tsize = int(rng.choice([24, 32, 40, 48]))
+    h, w = int(rng.choice([240, 300])), int(rng.choice([320, 400]))
+    span = float(rng.choice([0.0, math.radians(20), math.radians(60), 2 * math.pi]))
+    start = -span / 2
+    levels = int(rng.integers(2, 4)) if tsize >= 40 else 2
+    gen = dict(seed=200 + seed, height=h, width=w, tsize=tsize, n_poses=int(rng.integers(1, 4)),
+               angle_range=(start * 0.9, (start + span) * 0.9), invert_odd=bool(rng.integers(0, 4) == 0))
+    if u16:
+        gen.update(maxval=4095, noise_sigma=20)
+    create = dict(levels=levels, angle_start=start, angle_extent=span,
+                  ignore_polarity=gen["invert_odd"])
+    find = dict(angle_start=start, angle_extent=span, min_score=float(rng.choice([0.6, 0.7, 0.8])),
+                num_matches=int(rng.integers(0, 4)), max_overlap=float(rng.choice([0.0, 0.3, 0.5])),
+                subpixel=bool(rng.integers(0, 5) != 0), highest=levels, lowest=1)
+    case = dict(gen=gen, create=create, find=find)
+    kind = int(rng.integers(0, 3))  # 0 whole image, 1 rectangle, 2 two rectangles (sparse)
+    if kind:
+        case["domain"] = [("around", 0, int(rng.integers(10, 60)))] + (
+            [("around", min(1, gen["n_poses"] - 1), int(rng.integers(3, 20)))] if kind == 2 else [])
+    return case
+
+
+@pytest.mark.parametrize("seed", list(range(24)))
+def test_find_matches_oracle_random_sweep(mg, orc, seed):
+    """Seeded random searches against the oracle (bit-exact to the reference's
+    scalar build): identical match count and order, poses and scores within
+    the tolerances above."""
+    case = _sweep_case(seed)
+    wl, mask = make_inputs(case)
+    dom = search_domain(case, wl)
+    c, f = case["create"], case["find"]
+    om = orc.create(wl.template, levels=c["levels"], angle_start=c["angle_start"], angle_extent=c["angle_extent"],
+                    ignore_polarity=c["ignore_polarity"])
+    try:
+        want = orc.find(om, wl.image, f["angle_start"], f["angle_extent"], f["min_score"], f["num_matches"],
+                        f["max_overlap"], f["subpixel"], f["highest"], f["lowest"], domain=dom)
+    except oracle_lib.CheckerError as e:
+        with pytest.raises(mg.MvError) as err:
+            gpu_find(mg, gpu_model(mg, case, wl, mask), wl.image, case, domain=dom)
+        assert err.value.status == e.status
+        return
+    got = gpu_find(mg, gpu_model(mg, case, wl, mask), wl.image, case, domain=dom)
+    assert_same_matches(got, want, f"sweep {seed}: {case}")
