@@ -529,6 +529,12 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
                                            (budget - min_windows) / max_chunk}));
   const size_t ring = size_t(stages) * max_chunk + 1024;
   const int rows = std::min(std::min(256, (max_kr + 7 + 7) / 8 * 8), int((budget - ring) / 2 / per_row) / 8 * 8);
+  if (rows < 16) {
+    // a slab must hold at least one chunk of grid rows plus the 7 placement
+    // rows of the window; otherwise the step stays on the CUDA cores
+    plan->group_of_src.assign(nsrc, -1);
+    return plan;
+  }
   plan->stages = stages;
   plan->rows_slab = rows;
   plan->stage_bytes = int(max_chunk);
