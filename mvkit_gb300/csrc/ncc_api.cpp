@@ -867,6 +867,13 @@ DomainHost scan_domain(const uint8_t* mask, int64_t W, int64_t H) {
   return d;
 }
 
+// The device error flag of a find: the pyramid's exact-float check
+// (Unsupported) or a tensor-core wait that ran out (Internal).
+[[noreturn]] void raise_device_error(int32_t status) {
+  raise(status, status == kInternal ? "tensor-core correlation: a pipeline wait ran out (device error flag)"
+                                    : "pyramid sums exceed the exact float range");
+}
+
 // One model's query prepared for a multi-model selection
 // (matcher.cpp:1077-1101): its sorted candidates with finite scores and what
 // refining one of them needs.  The refinement reads the workspace's pyramid,
@@ -1623,7 +1630,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     check(cudaMemcpyAsync(ws.h_state, st, sizeof(QueryState), cudaMemcpyDeviceToHost, s), "state");
     check(cudaStreamSynchronize(s), "sync");
     if (ws.h_state->overflow) raise(kLimitExceeded, "coarse candidate budget exceeded");
-    if (ws.h_state->error) raise(ws.h_state->error, "pyramid sums exceed the exact float range");
+    if (ws.h_state->error) raise_device_error(ws.h_state->error);
     const int n = std::max(0, std::min(ws.h_state->sorted_count, kMaxCandidates));
     prep->cands.resize(size_t(n));
     if (n > 0)
@@ -1691,7 +1698,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   t_prof.issued_tc += double(hs.tc_issued);
   t_prof.work[kStScore] += double(hs.count[slot]) * double(orig.n);
   if (hs.overflow) raise(kLimitExceeded, "coarse candidate budget exceeded");
-  if (hs.error) raise(hs.error, "pyramid sums exceed the exact float range");
+  if (hs.error) raise_device_error(hs.error);
   std::vector<Cand> acc(size_t(hs.accepted));
   if (hs.accepted > 0) {
     check(cudaMemcpyAsync(acc.data(), ws.accepted.p, acc.size() * sizeof(Cand), cudaMemcpyDeviceToHost, s), "result");
