@@ -81,6 +81,13 @@ MVG_API int32_t mvg_deserialize_ncc_model(const char* bytes, int64_t size, mvg_n
  * on the host. */
 MVG_API int32_t mvg_set_model_build(int32_t where);
 
+/* Test hook for the bounded waits of the tensor-core kernel (calling
+ * thread's finds): on = 1 makes the kernel load no weights, so the MMA
+ * thread's mbarrier wait runs out after one second, the kernel sets the
+ * device error flag and leaves, and the find returns Internal (-1000); the
+ * context stays usable.  on = 0 restores normal operation. */
+MVG_API int32_t mvg_test_withhold_tensor_weights(int32_t on);
+
 /* FNV-1a 64 digest of a model's find tables (patch descriptors, angles,
  * sample, weight and run tables of every level, trained patches only):
  * equal digests mean bit-identical tables.  Uploads the tables first. */

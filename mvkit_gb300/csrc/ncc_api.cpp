@@ -229,6 +229,10 @@ struct mvg_ncc_model_s {
 namespace mvg {
 namespace {
 
+// Test hook (this thread's finds): the tensor-core kernel loads no weights, so
+// its bounded waits run out and the find reports the device error flag.
+thread_local int t_withhold_weights = 0;
+
 // Where models are built: 0 = the rotated rasters on the device when one is
 // present, 1 = on the host (the reference's order in FP64 on the CPU).
 std::atomic<int> g_model_build{0};
@@ -1317,6 +1321,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     tca.plane_pitch = pitch;
     tca.rc = ws.coarse_rc.p;
     tca.error = &st->error;
+    tca.withhold_weights = t_withhold_weights;
     {
       Span spp(kStTcPrep, s, 2);
       check(launch_tc_planes(lev[top], ws.tc_planes.p, pitch, P.parts, P.offset, s), "tc planes");
@@ -1478,6 +1483,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
         tca.plane_pitch = pitch;
         tca.rc = nullptr;
         tca.error = &st->error;
+        tca.withhold_weights = t_withhold_weights;
         {
           Span spp(kStTcPrep, s, 4);
           check(launch_tc_planes(lev[t], ws.tc_planes.p, pitch, P.parts, P.offset, s), "tc planes");
@@ -2083,6 +2089,10 @@ int32_t mvg_create_ncc_model(const void* pixels, int32_t pixel_type, int64_t wid
     finish_model(*m);
     *model_id = m.release();
   });
+}
+
+int32_t mvg_test_withhold_tensor_weights(int32_t on) {
+  return guarded([&] { t_withhold_weights = on != 0; });
 }
 
 int32_t mvg_set_model_build(int32_t where) {

@@ -191,6 +191,7 @@ struct TcArgs {
   int plane_pitch;                       // elements per plane row
   const int2* rc;                        // candidate lattice positions given directly (nullable)
   int32_t* error;
+  int withhold_weights;                  // test hook: load no weights (waits run out, error flag set)
 };
 
 // fp16 planes of a level for the tensor-core tracking: parts x 8 shifted

@@ -46,7 +46,7 @@ constexpr int kTcThreads = 192;     // warp 0 MMA, warp 1 weights, warps 2-5 win
 constexpr int kTcWindowThreads = 128;
 constexpr int kTcRows = 128;                  // MMA M
 constexpr uint32_t kTmemCols = 512 / kTcBlocksPerSm;  // accumulator sets x columns per set
-constexpr long long kSpinLimit = 1ll << 22;   // mbarrier polls before giving up
+constexpr unsigned long long kWaitNs = 1000000000ull;  // an mbarrier wait gives up after one second
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
 
@@ -84,8 +84,17 @@ __device__ __forceinline__ void expect_tx(uint64_t* bar, uint32_t bytes) {
 }
 
 // bounded wait for the completion of the phase with parity `parity`
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Waits for the phase with the given parity; false once kWaitNs passed
+// without it (the caller records the failure and leaves).
 __device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity) {
-  for (long long it = 0; it < kSpinLimit; ++it) {
+  unsigned long long start = 0;
+  for (;;) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -93,8 +102,12 @@ __device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity) {
         : "r"(smem_u32(bar)), "r"(parity)
         : "memory");
     if (done) return true;
+    const unsigned long long now = global_ns();
+    if (!start)
+      start = now;
+    else if (now - start > kWaitNs)
+      return false;
   }
-  return false;
 }
 
 __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
@@ -279,6 +292,7 @@ __device__ void tc_window_role(const TcArgs& a, TcShared& sh, uint8_t* abase, in
 // Weight producer (one thread): the tile's grid-row chunks through the ring,
 // as far ahead as the ring allows.
 __device__ void tc_weight_role(const TcArgs& a, TcShared& sh, uint8_t* wbase, RingPos& cb) {
+  if (a.withhold_weights) return;  // test hook: the MMA thread's weight wait runs out
   const TcGroup& G = sh.grp;
   const TcShape sp(G);
   const int S = a.stages;
