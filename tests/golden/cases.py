@@ -109,6 +109,12 @@ CASES = {
                    create=dict(levels=4, angle_start=-D(12), angle_extent=D(24)),
                    find=dict(angle_start=-D(12), angle_extent=D(24), min_score=0.7, num_matches=2, max_overlap=0.5,
                              subpixel=True, highest=4, lowest=1)),
+    # shaped like the reference's demo (examples/ncc_matching.cpp:6-31):
+    # automatic levels, an explicit angle step, NumLevels 0, one match
+    "demo_like": dict(gen=dict(seed=30, height=320, width=480, tsize=56, n_poses=1, angle_range=(-0.3, 0.3)),
+                      create=dict(levels=0, angle_start=-0.35, angle_extent=0.7, angle_step=0.025),
+                      find=dict(angle_start=-0.35, angle_extent=0.7, min_score=0.75, num_matches=1,
+                                max_overlap=0.5, subpixel=True, highest=0, lowest=1)),
 }
 
 # Reduced search domains (ROI, image.domain() in src/ncc_matching/matcher.cpp:
