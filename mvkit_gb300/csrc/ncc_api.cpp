@@ -1257,9 +1257,14 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   }
   QueryState* st = ws.state.p;
   int32_t* err_flag = &st->error;
+  // an fp16-exact level 0 that is also the finest: its half2 pairs come with it
+  const bool pairs0 = finest == 0 && (type == 1 ? 65535.0 : 255.0) <= 2048.0;
+  if (pairs0) ws.pairs.reserve(size_t(lw[0]) * size_t(lh[0]));
   {
     Span sp(kStPyramid, s, int(level_count));
-    check(launch_pyramid0(dev_pixels, type, pitch_elems, int(crop_row), int(crop_col), lev[0], err_flag, s), "pyramid0");
+    check(launch_pyramid0(dev_pixels, type, pitch_elems, int(crop_row), int(crop_col), lev[0], err_flag, s,
+                          pairs0 ? ws.pairs.p : nullptr),
+          "pyramid0");
     for (size_t l = 1; l < level_count; ++l) check(launch_pyramid(lev[l - 1], lev[l], err_flag, s), "pyramid");
   }
   const size_t first_target = std::max(finest, size_t(opt.subpixel ? 1 : 0));
@@ -1536,9 +1541,11 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   if ((type == 1 ? 65535.0 : 255.0) * std::ldexp(1., int(2 * finest)) <= 2048.0) {
     // fp16-exact level: half2 pairs halve the bilinear loads of the
     // continuous score and the Gauss-Newton passes
-    ws.pairs.reserve(size_t(lw[finest]) * size_t(lh[finest]));
-    Span sp(kStScore, s, 1);
-    check(launch_pairs(lev[finest].v, lw[finest], lh[finest], ws.pairs.p, s), "pairs");
+    if (!pairs0) {
+      ws.pairs.reserve(size_t(lw[finest]) * size_t(lh[finest]));
+      Span sp(kStScore, s, 1);
+      check(launch_pairs(lev[finest].v, lw[finest], lh[finest], ws.pairs.p, s), "pairs");
+    }
     fine.pairs = ws.pairs.p;
     ws.pairs_level = int(finest);
   }

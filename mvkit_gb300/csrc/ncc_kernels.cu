@@ -192,12 +192,21 @@ __device__ __forceinline__ bool better(float s, int o, float bs, int bo) {
 }
 
 // ------------------------------------------------------------------ pyramid
+// Level 0: the crop as float; with `pairs`, also the fp16 pairs (v[x],
+// v[x+1]) of pairs_kernel (last column repeated) for an fp16-exact level 0.
 template <class T>
-__global__ void pyramid0_kernel(const T* __restrict__ src, int64_t pitch, int crop_row, int crop_col, LevelImage dst) {
+__global__ void pyramid0_kernel(const T* __restrict__ src, int64_t pitch, int crop_row, int crop_col, LevelImage dst,
+                                uint32_t* __restrict__ pairs) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   const int r = blockIdx.y * blockDim.y + threadIdx.y;
   if (c >= dst.w || r >= dst.h) return;
-  dst.v[size_t(r) * dst.w + c] = float(src[(int64_t(crop_row) + r) * pitch + crop_col + c]);
+  const T* row = src + (int64_t(crop_row) + r) * pitch + crop_col;
+  const float v = float(row[c]);
+  dst.v[size_t(r) * dst.w + c] = v;
+  if (pairs) {
+    const __half a = __float2half_rn(v), b = __float2half_rn(float(row[c + 1 < dst.w ? c + 1 : c]));
+    pairs[size_t(r) * dst.w + c] = uint32_t(__half_as_ushort(a)) | (uint32_t(__half_as_ushort(b)) << 16);
+  }
 }
 
 // level k+1 from level k: 2x2 sums with the reference's clamped neighbours
@@ -2127,13 +2136,15 @@ cudaError_t reserve_dynamic_smem(const void* kernel, size_t bytes) {
 }
 
 cudaError_t launch_pyramid0(const void* src, int type, int64_t pitch_elems, int crop_row, int crop_col, LevelImage dst,
-                            int32_t* error_flag, cudaStream_t s) {
+                            int32_t* error_flag, cudaStream_t s, uint32_t* pairs) {
   (void)error_flag;
   const dim3 block(32, 8), grid((dst.w + 31) / 32, (dst.h + 7) / 8);
   if (type == 1)
-    pyramid0_kernel<uint16_t><<<grid, block, 0, s>>>(static_cast<const uint16_t*>(src), pitch_elems, crop_row, crop_col, dst);
+    pyramid0_kernel<uint16_t><<<grid, block, 0, s>>>(static_cast<const uint16_t*>(src), pitch_elems, crop_row, crop_col,
+                                                     dst, pairs);
   else
-    pyramid0_kernel<uint8_t><<<grid, block, 0, s>>>(static_cast<const uint8_t*>(src), pitch_elems, crop_row, crop_col, dst);
+    pyramid0_kernel<uint8_t><<<grid, block, 0, s>>>(static_cast<const uint8_t*>(src), pitch_elems, crop_row, crop_col,
+                                                    dst, pairs);
   return cudaGetLastError();
 }
 

@@ -327,8 +327,9 @@ struct RefineArgs {
   DomainView dom;
 };
 
+// Level 0 (float crop); with `pairs`, also its fp16 pairs (launch_pairs' output)
 cudaError_t launch_pyramid0(const void* src, int type, int64_t pitch_elems, int crop_row, int crop_col, LevelImage dst,
-                            int32_t* error_flag, cudaStream_t s);
+                            int32_t* error_flag, cudaStream_t s, uint32_t* pairs = nullptr);
 cudaError_t launch_pyramid(const LevelImage& src, LevelImage dst, int32_t* error_flag, cudaStream_t s);
 cudaError_t launch_prefix(const LevelImage& lev, cudaStream_t s);
 cudaError_t launch_coarse(const CoarseArgs& a, int max_bh, int max_bw, cudaStream_t s, size_t smem_limit);
