@@ -237,6 +237,27 @@ __global__ void prefix_kernel(LevelImage lev) {
     else
       out[0] = make_longlong2(0, 0);
   }
+  if (out32) {
+    // modulo 2^32: the same stored values from 32-bit sums and shuffles
+    uint32_t c1 = 0, c2 = 0;
+    for (int base = 0; base < lev.w; base += 32) {
+      const int c = base + lane;
+      const uint32_t s = c < lev.w ? uint32_t(row[c]) : 0u;
+      uint32_t a = s, b = s * s;
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t ua = __shfl_up_sync(0xffffffffu, a, o);
+        const uint32_t ub = __shfl_up_sync(0xffffffffu, b, o);
+        if (lane >= o) {
+          a += ua;
+          b += ub;
+        }
+      }
+      if (c < lev.w) out32[c + 1] = make_uint2(c1 + a, c2 + b);
+      c1 += __shfl_sync(0xffffffffu, a, 31);
+      c2 += __shfl_sync(0xffffffffu, b, 31);
+    }
+    return;
+  }
   long long c1 = 0, c2 = 0;
   for (int base = 0; base < lev.w; base += 32) {
     const int c = base + lane;
@@ -250,12 +271,7 @@ __global__ void prefix_kernel(LevelImage lev) {
         b += ub;
       }
     }
-    if (c < lev.w) {
-      if (out32)
-        out32[c + 1] = make_uint2(uint32_t(c1 + a), uint32_t(c2 + b));
-      else
-        out[c + 1] = make_longlong2(c1 + a, c2 + b);
-    }
+    if (c < lev.w) out[c + 1] = make_longlong2(c1 + a, c2 + b);
     c1 += __shfl_sync(0xffffffffu, a, 31);
     c2 += __shfl_sync(0xffffffffu, b, 31);
   }
@@ -985,7 +1001,7 @@ __device__ void continuous_pass(const ImageView& img, const OriginalView& orig, 
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(128) score_kernel(ScoreArgs a) {
+__global__ void __launch_bounds__(128, 12) score_kernel(ScoreArgs a) {
   __shared__ PoseShared sh;
   const int i = blockIdx.x;
   if (i >= live_count(a.state, a.slot)) return;
