@@ -7,9 +7,10 @@ FindNccModel MinScore 0.7, NumMatches 5, MaxOverlap 0.5, SubPixel true.
 A step is one find on each of `--batch` distinct scenes.
 
 value: images/s with the scenes resident in HBM (CUDA events on the find
-stream, L2 flushed between steps).  e2e: the same through the C ABI with
-page-locked host buffers (upload and result read-back inside the timed
-region).  roofline: the correlation kernel, its algorithmic multiply-adds
+stream, L2 flushed between steps).  e2e: the same scenes through the batched
+operator (mvg_find_ncc_models_batch) from page-locked host buffers, wall
+clock around each step (upload, the finds on the library's host threads and
+the result read-back inside the timed region).  roofline: the correlation kernel, its algorithmic multiply-adds
 over its live event time, from a second timed pass of the same steps with
 CUDA events around each kernel group (the value pass carries no events).  cpu_baseline: the FP64
 oracle restatement of the reference on this host's cores (one scene per
@@ -316,10 +317,30 @@ def main():
                                         if isinstance(v, dict)}}
         path[0] = args.path
 
+    host_images = [pb.array for pb in pinned]
+
+    def batch_step():
+        # the batched operator on host images: uploads, finds on the
+        # library's host threads (one stream each) and result read-back
+        return mg.find_ncc_models_batch(host_images, [model], *ctl, workers=threads)
+
     for _ in range(args.warmup):
         one_step(dev, False)
-        one_step(pinned, True)
+        batch_step()
     torch.cuda.synchronize()
+
+    def timed_batch(steps: int):
+        total = 0.0
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            if world > 1:
+                torch.distributed.barrier()
+            t0 = time.perf_counter()
+            batch_step()
+            torch.cuda.synchronize()
+            total += (time.perf_counter() - t0) * 1e3
+        return total
 
     with ClockSampler(local) as clocks:
         dev_ms = timed(dev, False, args.steps)
@@ -328,7 +349,7 @@ def main():
     # stay out of the value pass)
     timed(dev, False, args.steps, profile=True)
     prof = aggregate()
-    host_ms = timed(pinned, True, args.steps)
+    host_ms = timed_batch(args.steps)
 
     # the same finds one at a time (untimed): per-kernel event times without
     # other streams' kernels interleaved
@@ -396,7 +417,9 @@ def main():
                             else "plain FP32 CUDA-core correlation")},
         "e2e": {"value": e2e, "unit": "images/s",
                 "h2d_bytes_per_step": int(sum(w.image.nbytes for w in wls)),
-                "d2h_bytes_per_step": int(args.batch * (4 * 8 * FIND["num_matches"] + 128))},
+                "d2h_bytes_per_step": int(args.batch * (4 * 8 * FIND["num_matches"] + 128)),
+                "api": "find_ncc_models_batch (mvg_find_ncc_models_batch) on pinned host images, "
+                       f"{threads} library host threads; wall clock per step, synchronized on both sides"},
         "roofline": roof,
         "gpu_launches": int(launches_total),
         "clocks": clocks.summary(),

@@ -144,6 +144,35 @@ MVG_API int32_t mvg_find_ncc_models(const void* pixels, int32_t pixel_type, int6
                                     double* row, double* column, double* angle, double* score, int64_t* model,
                                     int64_t capacity, int64_t* count, void* stream);
 
+/* Batched FindNccModels (no reference counterpart: a caller of the
+ * reference loops over its images, one mv_find_ncc_models call each,
+ * src/c_api/ncc_matching_api.cpp:191-201).  Searches num_images images for
+ * the same models and controls as mvg_find_ncc_models, on `workers` (1..256)
+ * host threads of the library, each with its own stream and workspace, so
+ * several finds are in flight on the GPU.  Image i is images[i],
+ * pixel_types[i], widths[i], heights[i], row_strides[i] (location shared:
+ * all in host or all in device memory); domains is NULL or holds one mask
+ * pointer (or NULL) per image.  Each image's result equals that of
+ * mvg_find_ncc_models on it.  Matches are written image after image:
+ * image i's occupy [image_offsets[i], image_offsets[i + 1]) (num_images + 1
+ * entries) of row/column/angle/score/model, entries past capacity dropped;
+ * *count receives the total.  statuses[i] receives image i's status (a
+ * failed image has no matches).  Returns 0 when every image succeeded, else
+ * the first failed image's status, with "image <i>: <message>" as the last
+ * error; the outputs are filled either way. */
+MVG_API int32_t mvg_find_ncc_models_batch(const void* const* images, const int32_t* pixel_types,
+                                          const int64_t* widths, const int64_t* heights,
+                                          const int64_t* row_strides, int64_t num_images, int32_t location,
+                                          const uint8_t* const* domains, const mvg_ncc_model* model_ids,
+                                          int64_t num_models, const double* angle_start, int64_t n_angle_start,
+                                          const double* angle_extent, int64_t n_angle_extent,
+                                          const double* min_score, int64_t n_min_score, const int64_t* num_matches,
+                                          int64_t n_num_matches, const double* max_overlap, int64_t n_max_overlap,
+                                          const int32_t* subpixel, int64_t n_subpixel, const int32_t* num_levels,
+                                          int64_t n_num_levels, int32_t workers, double* row, double* column,
+                                          double* angle, double* score, int64_t* model, int64_t capacity,
+                                          int64_t* image_offsets, int32_t* statuses, int64_t* count);
+
 /* NCC adjoint with a scale degree of freedom (no counterpart in the rigid
  * reference).  For each of `count` poses (row, column, angle, scale; 4
  * doubles each, the matcher's pixel-centre image coordinates of the model

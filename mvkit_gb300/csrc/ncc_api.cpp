@@ -10,6 +10,7 @@
 #include <array>
 #include <atomic>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
 #include <limits>
 #include <map>
@@ -17,6 +18,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/mvkit_gb300_ncc.h"
@@ -2064,6 +2066,153 @@ FindParams make_params(double angle_start, double angle_extent, double min_score
   return p;
 }
 
+// Model handles and control tuples of a FindNccModels call, checked as
+// ncc_models and NccControls do (src/c_api/ncc_matching_api.cpp:112-162).
+struct MultiControls {
+  std::vector<mvg_ncc_model_s*> models;
+  std::vector<FindParams> opts;
+  Selection sel;
+};
+
+MultiControls multi_controls(const mvg_ncc_model* model_ids, int64_t num_models, const double* angle_start,
+                             int64_t n_angle_start, const double* angle_extent, int64_t n_angle_extent,
+                             const double* min_score, int64_t n_min_score, const int64_t* num_matches,
+                             int64_t n_num_matches, const double* max_overlap, int64_t n_max_overlap,
+                             const int32_t* subpixel, int64_t n_subpixel, const int32_t* num_levels,
+                             int64_t n_num_levels) {
+  if (!model_ids || num_models <= 0 || num_models > 4096)
+    raise(kInvalidArgument, "one model or a nonempty model array (maximum 4096) required");
+  const size_t n = size_t(num_models);
+  MultiControls mc;
+  std::vector<mvg_ncc_model_s*>& models = mc.models;
+  models.resize(n);
+  for (size_t i = 0; i < n; ++i) {
+    if (!model_ids[i]) raise(kTypeMismatch, "control handle is not an NCC model");
+    models[i] = model_ids[i];
+  }
+  auto card = [&](const void* p, int64_t k, const char* name) {
+    if (!p || (k != 1 && k != num_models))
+      raise(kInvalidArgument, std::string(name) + ": one value or one value per model required");
+  };
+  card(angle_start, n_angle_start, "AngleStart");
+  card(angle_extent, n_angle_extent, "AngleExtent");
+  card(min_score, n_min_score, "MinScore");
+  card(num_matches, n_num_matches, "NumMatches");
+  card(max_overlap, n_max_overlap, "MaxOverlap");
+  card(subpixel, n_subpixel, "SubPixel");
+  if (!num_levels ||
+      (n_num_levels != 1 && n_num_levels != 2 && n_num_levels != num_models && n_num_levels != 2 * num_models))
+    raise(kInvalidArgument, "NumLevels: highest level or shared/per-model level pairs required");
+  auto number = [&](const double* v, int64_t k, size_t i, double lo, double hi, const char* name) {
+    const double x = v[k == 1 ? 0 : i];
+    if (!std::isfinite(x) || x < lo || x > hi)
+      raise(kInvalidArgument, std::string(name) + ": numeric control outside allowed range");
+    return x;
+  };
+  std::vector<FindParams>& opts = mc.opts;
+  opts.resize(n);
+  for (size_t i = 0; i < n; ++i) {
+    FindParams& q = opts[i];
+    q.angle_start = number(angle_start, n_angle_start, i, -std::numeric_limits<double>::max(),
+                           std::numeric_limits<double>::max(), "AngleStart");
+    q.angle_extent = number(angle_extent, n_angle_extent, i, 0, 6.28318530717958647692, "AngleExtent");
+    q.min_score = number(min_score, n_min_score, i, 0, 1, "MinScore");
+    q.max_overlap = number(max_overlap, n_max_overlap, i, 0, 1, "MaxOverlap");
+    const int64_t quota = num_matches[n_num_matches == 1 ? 0 : i];
+    if (quota < 0) raise(kInvalidArgument, "NumMatches: match count must be nonnegative");
+    q.num_matches = quota;
+    const int32_t sp = subpixel[n_subpixel == 1 ? 0 : i];
+    if (sp != 0 && sp != 1) raise(kInvalidArgument, "SubPixel: expected true or false");
+    q.subpixel = sp != 0;
+    size_t hi_at = 0, lo_at = 0;
+    bool pair = false;
+    if (n_num_levels == num_models && num_models > 1) {
+      hi_at = i;
+    } else if (n_num_levels == 2 * num_models) {
+      hi_at = 2 * i;
+      lo_at = hi_at + 1;
+      pair = true;
+    } else if (n_num_levels == 2) {
+      lo_at = 1;
+      pair = true;
+    }
+    const int64_t highest = num_levels[hi_at], lowest = pair ? num_levels[lo_at] : 1;
+    if (highest < 0 || lowest < 0) raise(kInvalidArgument, "NumLevels: invalid highest/lowest level pair");
+    q.highest = int(highest);
+    q.lowest = int(std::max<int64_t>(1, lowest));
+  }
+  Selection& sel = mc.sel;
+  sel.num_matches = n_num_matches == 1 ? opts.front().num_matches : -1;
+  sel.max_overlap = n_max_overlap == 1 ? opts.front().max_overlap : -1;
+  return mc;
+}
+
+// Host threads of the batched find.  They live as long as the process, so
+// each keeps its workspace, stream and device buffers from one batch to the
+// next (a thread of its own per find in flight, as the finds share nothing
+// but the read-only models).  One batch runs at a time.
+class FindPool {
+ public:
+  // Runs job(worker) on `workers` pool threads and returns when all are done.
+  template <class Job> void run(int workers, Job& job) {
+    std::lock_guard<std::mutex> one_batch(batch_);
+    std::unique_lock<std::mutex> lk(m_);
+    while (int(threads_.size()) < workers) {
+      const int id = int(threads_.size());
+      threads_.emplace_back([this, id] { loop(id); });
+      threads_.back().detach();
+    }
+    call_ = [](void* j, int w) { (*static_cast<Job*>(j))(w); };
+    job_ = &job;
+    want_ = workers;
+    done_ = 0;
+    ++generation_;
+    wake_.notify_all();
+    finished_.wait(lk, [&] { return done_ == want_; });
+    job_ = nullptr;
+  }
+
+ private:
+  void loop(int id) {
+    uint64_t seen = 0;
+    std::unique_lock<std::mutex> lk(m_);
+    for (;;) {
+      wake_.wait(lk, [&] { return generation_ != seen; });
+      seen = generation_;
+      if (id >= want_) continue;
+      void (*call)(void*, int) = call_;
+      void* job = job_;
+      lk.unlock();
+      try {
+        call(job, id);
+      } catch (...) {
+      }
+      lk.lock();
+      if (++done_ == want_) finished_.notify_all();
+    }
+  }
+
+  std::mutex batch_, m_;
+  std::condition_variable wake_, finished_;
+  std::vector<std::thread> threads_;
+  void (*call_)(void*, int) = nullptr;
+  void* job_ = nullptr;
+  int want_ = 0, done_ = 0;
+  uint64_t generation_ = 0;
+};
+
+FindPool& find_pool() {
+  static FindPool* pool = new FindPool;  // never destroyed: its threads outlive static destruction
+  return *pool;
+}
+
+// One image of a batch: its matches, or the status and message of its failure.
+struct BatchImage {
+  std::vector<MultiCand> matches;
+  int32_t status = 0;
+  std::string message;
+};
+
 }  // namespace
 
 // Thread-local error message shared by every entry point of the library.
@@ -2248,68 +2397,13 @@ int32_t mvg_find_ncc_models(const void* pixels, int32_t pixel_type, int64_t widt
   return guarded([&] {
     if (!count) raise(kInvalidArgument, "count must not be null");
     *count = 0;
-    // ncc_models and NccControls (src/c_api/ncc_matching_api.cpp:112-162)
-    if (!model_ids || num_models <= 0 || num_models > 4096)
-      raise(kInvalidArgument, "one model or a nonempty model array (maximum 4096) required");
-    const size_t n = size_t(num_models);
-    std::vector<mvg_ncc_model_s*> models(n);
-    for (size_t i = 0; i < n; ++i) {
-      if (!model_ids[i]) raise(kTypeMismatch, "control handle is not an NCC model");
-      models[i] = model_ids[i];
-    }
-    auto card = [&](const void* p, int64_t k, const char* name) {
-      if (!p || (k != 1 && k != num_models))
-        raise(kInvalidArgument, std::string(name) + ": one value or one value per model required");
-    };
-    card(angle_start, n_angle_start, "AngleStart");
-    card(angle_extent, n_angle_extent, "AngleExtent");
-    card(min_score, n_min_score, "MinScore");
-    card(num_matches, n_num_matches, "NumMatches");
-    card(max_overlap, n_max_overlap, "MaxOverlap");
-    card(subpixel, n_subpixel, "SubPixel");
-    if (!num_levels ||
-        (n_num_levels != 1 && n_num_levels != 2 && n_num_levels != num_models && n_num_levels != 2 * num_models))
-      raise(kInvalidArgument, "NumLevels: highest level or shared/per-model level pairs required");
-    auto number = [&](const double* v, int64_t k, size_t i, double lo, double hi, const char* name) {
-      const double x = v[k == 1 ? 0 : i];
-      if (!std::isfinite(x) || x < lo || x > hi)
-        raise(kInvalidArgument, std::string(name) + ": numeric control outside allowed range");
-      return x;
-    };
-    std::vector<FindParams> opts(n);
-    for (size_t i = 0; i < n; ++i) {
-      FindParams& q = opts[i];
-      q.angle_start = number(angle_start, n_angle_start, i, -std::numeric_limits<double>::max(),
-                             std::numeric_limits<double>::max(), "AngleStart");
-      q.angle_extent = number(angle_extent, n_angle_extent, i, 0, 6.28318530717958647692, "AngleExtent");
-      q.min_score = number(min_score, n_min_score, i, 0, 1, "MinScore");
-      q.max_overlap = number(max_overlap, n_max_overlap, i, 0, 1, "MaxOverlap");
-      const int64_t quota = num_matches[n_num_matches == 1 ? 0 : i];
-      if (quota < 0) raise(kInvalidArgument, "NumMatches: match count must be nonnegative");
-      q.num_matches = quota;
-      const int32_t sp = subpixel[n_subpixel == 1 ? 0 : i];
-      if (sp != 0 && sp != 1) raise(kInvalidArgument, "SubPixel: expected true or false");
-      q.subpixel = sp != 0;
-      size_t hi_at = 0, lo_at = 0;
-      bool pair = false;
-      if (n_num_levels == num_models && num_models > 1) {
-        hi_at = i;
-      } else if (n_num_levels == 2 * num_models) {
-        hi_at = 2 * i;
-        lo_at = hi_at + 1;
-        pair = true;
-      } else if (n_num_levels == 2) {
-        lo_at = 1;
-        pair = true;
-      }
-      const int64_t highest = num_levels[hi_at], lowest = pair ? num_levels[lo_at] : 1;
-      if (highest < 0 || lowest < 0) raise(kInvalidArgument, "NumLevels: invalid highest/lowest level pair");
-      q.highest = int(highest);
-      q.lowest = int(std::max<int64_t>(1, lowest));
-    }
-    Selection sel;
-    sel.num_matches = n_num_matches == 1 ? opts.front().num_matches : -1;
-    sel.max_overlap = n_max_overlap == 1 ? opts.front().max_overlap : -1;
+    const MultiControls mc = multi_controls(model_ids, num_models, angle_start, n_angle_start, angle_extent,
+                                            n_angle_extent, min_score, n_min_score, num_matches, n_num_matches,
+                                            max_overlap, n_max_overlap, subpixel, n_subpixel, num_levels,
+                                            n_num_levels);
+    const std::vector<mvg_ncc_model_s*>& models = mc.models;
+    const std::vector<FindParams>& opts = mc.opts;
+    const Selection& sel = mc.sel;
     const std::vector<MultiCand> r = run_find_models(models, pixels, pixel_type, width, height, row_stride, location,
                                                      domain, opts, sel, static_cast<cudaStream_t>(stream));
     *count = int64_t(r.size());
@@ -2324,6 +2418,97 @@ int32_t mvg_find_ncc_models(const void* pixels, int32_t pixel_type, int64_t widt
       if (model) model[i] = r[i].model;
     }
   });
+}
+
+int32_t mvg_find_ncc_models_batch(const void* const* images, const int32_t* pixel_types, const int64_t* widths,
+                                  const int64_t* heights, const int64_t* row_strides, int64_t num_images,
+                                  int32_t location, const uint8_t* const* domains, const mvg_ncc_model* model_ids,
+                                  int64_t num_models, const double* angle_start, int64_t n_angle_start,
+                                  const double* angle_extent, int64_t n_angle_extent, const double* min_score,
+                                  int64_t n_min_score, const int64_t* num_matches, int64_t n_num_matches,
+                                  const double* max_overlap, int64_t n_max_overlap, const int32_t* subpixel,
+                                  int64_t n_subpixel, const int32_t* num_levels, int64_t n_num_levels,
+                                  int32_t workers, double* row, double* column, double* angle, double* score,
+                                  int64_t* model, int64_t capacity, int64_t* image_offsets, int32_t* statuses,
+                                  int64_t* count) {
+  std::string first_failure;
+  int32_t first_status = kOk;
+  const int32_t st = guarded([&] {
+    if (!count || !image_offsets || !statuses) raise(kInvalidArgument, "count, offsets and statuses required");
+    *count = 0;
+    if (num_images < 0 || num_images > (int64_t(1) << 24)) raise(kInvalidArgument, "invalid image count");
+    image_offsets[0] = 0;
+    if (num_images == 0) return;
+    if (!images || !pixel_types || !widths || !heights || !row_strides)
+      raise(kInvalidArgument, "image arrays must not be null");
+    if (workers < 1 || workers > 256) raise(kInvalidArgument, "workers must be 1..256");
+    const MultiControls mc = multi_controls(model_ids, num_models, angle_start, n_angle_start, angle_extent,
+                                            n_angle_extent, min_score, n_min_score, num_matches, n_num_matches,
+                                            max_overlap, n_max_overlap, subpixel, n_subpixel, num_levels,
+                                            n_num_levels);
+    int device = 0;
+    check(cudaGetDevice(&device), "batch");
+    const int path = t_path;
+    std::vector<BatchImage> done(static_cast<size_t>(num_images));
+    std::atomic<int64_t> next{0};
+    auto job = [&](int) {
+      if (cudaSetDevice(device) != cudaSuccess) return;
+      t_path = path;
+      for (int64_t i; (i = next.fetch_add(1)) < num_images;) {
+        BatchImage& b = done[size_t(i)];
+        b.status = guarded([&] {
+          const uint8_t* dom = domains ? domains[i] : nullptr;
+          if (mc.models.size() > 1) {
+            b.matches = run_find_models(mc.models, images[i], pixel_types[i], widths[i], heights[i],
+                                        row_strides[i], location, dom, mc.opts, mc.sel, nullptr);
+            return;
+          }
+          // one model: find_models reduces to find (same quota and overlap
+          // rule), whose selection and refinement stay on the device
+          const FindOutput r = run_find(*mc.models[0], images[i], pixel_types[i], widths[i], heights[i],
+                                        row_strides[i], location, dom, mc.opts[0], nullptr, -2);
+          for (const Match& mt : r.matches) {
+            MultiCand m{};
+            m.c.row = mt.row;
+            m.c.col = mt.col;
+            m.c.angle = mt.angle;
+            m.c.score = mt.score;
+            b.matches.push_back(m);
+          }
+        });
+        if (b.status != kOk) b.message = g_last_error;
+      }
+    };
+    find_pool().run(int(std::min<int64_t>(workers, num_images)), job);
+    if (next.load() < num_images) raise(kInternal, "batch worker could not select the device");
+    int64_t at = 0;
+    for (int64_t i = 0; i < num_images; ++i) {
+      const BatchImage& b = done[size_t(i)];
+      statuses[i] = b.status;
+      if (b.status != kOk && first_status == kOk) {
+        first_status = b.status;
+        first_failure = "image " + std::to_string(i) + ": " + b.message;
+      }
+      for (const MultiCand& m : b.matches) {
+        if (at < capacity) {
+          // edge-centred pose convention (src/c_api/ncc_matching_api.cpp:171-176)
+          const Cand& c = m.c;
+          const double cs = std::cos(c.angle), sn = std::sin(c.angle);
+          if (row) row[at] = c.row + .5 * (1 - cs + sn);
+          if (column) column[at] = c.col + .5 * (1 - cs - sn);
+          if (angle) angle[at] = c.angle;
+          if (score) score[at] = c.score;
+          if (model) model[at] = m.model;
+        }
+        ++at;
+      }
+      image_offsets[i + 1] = at;
+    }
+    *count = at;
+  });
+  if (st != kOk || first_status == kOk) return st;
+  g_last_error = first_failure;
+  return first_status;
 }
 
 int32_t mvg_ncc_score_gradient(const void* pixels, int32_t pixel_type, int64_t width, int64_t height,

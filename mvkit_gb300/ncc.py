@@ -79,6 +79,10 @@ def load() -> C.CDLL:
     lib.mvg_find_ncc_models.argtypes = ([C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int32,
                                         C.c_void_p, C.c_void_p, C.c_int64] + [C.c_void_p, C.c_int64] * 7 +
                                        [C.c_void_p] * 5 + [C.c_int64, _i64p, C.c_void_p])
+    lib.mvg_find_ncc_models_batch.argtypes = ([C.c_void_p] * 5 + [C.c_int64, C.c_int32, C.c_void_p, C.c_void_p,
+                                                                   C.c_int64] +
+                                             [C.c_void_p, C.c_int64] * 7 + [C.c_int32] + [C.c_void_p] * 5 +
+                                             [C.c_int64, C.c_void_p, C.c_void_p, _i64p])
     lib.mvg_last_error.restype = C.c_char_p
     lib.mvg_host_alloc.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
     lib.mvg_host_free.argtypes = [C.c_void_p]
@@ -93,7 +97,8 @@ def load() -> C.CDLL:
     for name in ("mvg_create_ncc_model", "mvg_get_ncc_model_params", "mvg_clear_ncc_model", "mvg_find_ncc_model",
                  "mvg_find_ncc_model_stage", "mvg_ncc_pyramid_level", "mvg_host_alloc", "mvg_host_free",
                  "mvg_device_alloc", "mvg_device_free", "mvg_copy_to_device", "mvg_write_ncc_model", "mvg_read_ncc_model",
-                 "mvg_serialize_ncc_model", "mvg_deserialize_ncc_model", "mvg_find_ncc_models"):
+                 "mvg_serialize_ncc_model", "mvg_deserialize_ncc_model", "mvg_find_ncc_models",
+                 "mvg_find_ncc_models_batch"):
         getattr(lib, name).restype = C.c_int32
     _LIB = lib
     return lib
@@ -382,15 +387,11 @@ def find_ncc_model(image, model: NccModel, angle_start, angle_extent, min_score,
         cap = int(cnt.value)
 
 
-def find_ncc_models(image, models, angle_start, angle_extent, min_score, num_matches, max_overlap, subpixel,
-                    num_levels, stream=None, domain=None):
-    """FindNccModels (src/c_api/ncc_matching_api.cpp:191-201).
-
-    models: one NccModel or a sequence of 1..4096.  Each control takes one
-    value (shared) or one per model; num_levels takes 1, 2, len(models) or
-    2*len(models) values.  Returns (Row, Column, Angle, Score, Model), Model
-    being the index into `models`."""
-    op = "find_ncc_models"
+def _models_controls(op, models, angle_start, angle_extent, min_score, num_matches, max_overlap, subpixel,
+                     num_levels):
+    """Model handles and control arrays of FindNccModels (NccControls,
+    src/c_api/ncc_matching_api.cpp:126-162): (models, ctypes handle array,
+    control arrays in C-ABI order, match quotas)."""
     ms = list(models) if isinstance(models, (list, tuple)) else [models]
     if not ms or len(ms) > 4096:
         raise MvError(MV_STATUS_INVALID_ARGUMENT, "one model or a nonempty model array (maximum 4096) required", op)
@@ -429,6 +430,22 @@ def find_ncc_models(image, models, angle_start, angle_extent, min_score, num_mat
     if (levels < 0).any() or (levels > 2**31 - 1).any():
         raise MvError(MV_STATUS_INVALID_ARGUMENT, "invalid highest/lowest level pair", op)
     levels = levels.astype(np.int32)
+    ids = (C.c_void_p * n)(*[m.handle for m in ms])
+    return ms, ids, (starts, extents, scores, quotas, overlaps, modes, levels), quotas
+
+
+def find_ncc_models(image, models, angle_start, angle_extent, min_score, num_matches, max_overlap, subpixel,
+                    num_levels, stream=None, domain=None):
+    """FindNccModels (src/c_api/ncc_matching_api.cpp:191-201).
+
+    models: one NccModel or a sequence of 1..4096.  Each control takes one
+    value (shared) or one per model; num_levels takes 1, 2, len(models) or
+    2*len(models) values.  Returns (Row, Column, Angle, Score, Model), Model
+    being the index into `models`."""
+    op = "find_ncc_models"
+    ms, ids, arrs, quotas = _models_controls(op, models, angle_start, angle_extent, min_score, num_matches,
+                                             max_overlap, subpixel, num_levels)
+    n = len(ms)
     if isinstance(image, DeviceImage):
         ptr, typ, (h, w), stride, loc = image.ptr, image.type, image.shape, image.stride, 1
     else:
@@ -438,10 +455,8 @@ def find_ncc_models(image, models, angle_start, angle_extent, min_score, num_mat
             return e, e.copy(), e.copy(), e.copy(), np.zeros(0, dtype=np.int64)
         ptr, (h, w), stride, loc = a.ctypes.data, a.shape, a.strides[0], 0
     dom = _domain(domain, (h, w), op)
-    ids = (C.c_void_p * n)(*[m.handle for m in ms])
     lib = load()
     cap = max(64, int(quotas.sum()))
-    arrs = (starts, extents, scores, quotas, overlaps, modes, levels)
     args = []
     for arr in arrs:
         args += [arr.ctypes.data, len(arr)]
@@ -455,6 +470,90 @@ def find_ncc_models(image, models, angle_start, angle_extent, min_score, num_mat
         if cnt.value <= cap:
             return tuple(o[: cnt.value] for o in out)
         cap = int(cnt.value)
+
+
+def find_ncc_models_batch(images, models, angle_start, angle_extent, min_score, num_matches, max_overlap,
+                          subpixel, num_levels, domains=None, workers: int = 8, raise_errors: bool = True):
+    """FindNccModels over a batch of images of any sizes, several finds in
+    flight on the library's own host threads (mvg_find_ncc_models_batch).
+
+    images: 2-D uint8/uint16 host arrays, or DeviceImage objects (not mixed).
+    domains: None, or one mask (or None) per image.  Controls as for
+    find_ncc_models, shared by all images.  Returns one entry per image:
+    (Row, Column, Angle, Score, Model) as find_ncc_models returns it, or,
+    with raise_errors=False, the MvError of an image that failed.  With
+    raise_errors=True the first failed image's error is raised."""
+    op = "find_ncc_models_batch"
+    imgs = list(images)
+    ms, ids, arrs, quotas = _models_controls(op, models, angle_start, angle_extent, min_score, num_matches,
+                                             max_overlap, subpixel, num_levels)
+    if isinstance(workers, bool) or not isinstance(workers, (int, np.integer)) or not 1 <= int(workers) <= 256:
+        raise MvError(MV_STATUS_INVALID_ARGUMENT, "workers must be 1..256", op)
+    n_img = len(imgs)
+    if n_img == 0:
+        return []
+    on_device = [isinstance(x, DeviceImage) for x in imgs]
+    if any(on_device) and not all(on_device):
+        raise MvError(MV_STATUS_INVALID_ARGUMENT, "images must all be in host or all in device memory", op)
+    keep, ptrs, types, ws, hs, strides = [], [], [], [], [], []
+    for x in imgs:
+        if isinstance(x, DeviceImage):
+            ptrs.append(x.ptr.value)
+            types.append(x.type)
+            h, w = x.shape
+            strides.append(x.stride)
+        else:
+            a, typ = _image(x, op, "Image")
+            keep.append(a)
+            ptrs.append(a.ctypes.data)
+            types.append(typ)
+            h, w = a.shape
+            strides.append(a.strides[0])
+        hs.append(h)
+        ws.append(w)
+    dom_ptrs = None
+    if domains is not None:
+        ds = list(domains)
+        if len(ds) != n_img:
+            raise MvError(MV_STATUS_INVALID_ARGUMENT, "one domain (or None) per image required", op)
+        dom_ptrs = (C.c_void_p * n_img)()
+        for i, d in enumerate(ds):
+            m = _domain(d, (hs[i], ws[i]), op)
+            if m is not None:
+                keep.append(m)
+                dom_ptrs[i] = m.ctypes.data
+    c_imgs = (C.c_void_p * n_img)(*ptrs)
+    c_types = np.array(types, dtype=np.int32)
+    c_w, c_h, c_s = (np.array(v, dtype=np.int64) for v in (ws, hs, strides))
+    args = []
+    for arr in arrs:
+        args += [arr.ctypes.data, len(arr)]
+    lib = load()
+    per_image = max(16, int(quotas.sum()))
+    cap = per_image * n_img
+    offsets = np.zeros(n_img + 1, dtype=np.int64)
+    statuses = np.zeros(n_img, dtype=np.int32)
+    while True:
+        out = [np.zeros(cap) for _ in range(4)] + [np.zeros(cap, dtype=np.int64)]
+        cnt = C.c_int64()
+        st = lib.mvg_find_ncc_models_batch(c_imgs, c_types.ctypes.data, c_w.ctypes.data, c_h.ctypes.data,
+                                           c_s.ctypes.data, n_img, 1 if on_device[0] else 0, dom_ptrs, ids,
+                                           len(ms), *args, int(workers),
+                                           *[o.ctypes.data for o in out], cap, offsets.ctypes.data,
+                                           statuses.ctypes.data, C.byref(cnt))
+        if st != 0 and (raise_errors or not statuses.any()):
+            _check(st, op)
+        if cnt.value <= cap:
+            break
+        cap = int(cnt.value)
+    results = []
+    for i in range(n_img):
+        if statuses[i] != 0:
+            results.append(MvError(int(statuses[i]), f"image {i} failed", op))
+            continue
+        a, b = int(offsets[i]), int(offsets[i + 1])
+        results.append(tuple(o[a:b].copy() for o in out))
+    return results
 
 
 def ncc_score_gradient(image, model: NccModel, poses, stream=None):

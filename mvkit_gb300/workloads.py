@@ -222,15 +222,19 @@ class MultiWorkload:
 
 def make_multi_workload(seed: int, height: int, width: int, tsizes: tuple, n_poses: tuple,
                         angle_range: tuple = (0.0, 0.0), noise_sigma: int = 3, shapes: int = 40,
-                        maxval: int = 255) -> MultiWorkload:
+                        maxval: int = 255, contrast: float = 0.0,
+                        template_seed: int | None = None) -> MultiWorkload:
     """One scene holding several different templates (FindNccModels): template
     k (side tsizes[k], cropped from its own source scene) is pasted n_poses[k]
-    times; no two pastes overlap."""
+    times; no two pastes overlap.  contrast > 0 scales each paste by
+    U[1-c, 1+c]; template_seed (default: seed) makes the templates, so scenes
+    of one batch can share them."""
     dtype = np.uint8 if maxval <= 255 else np.uint16
+    tseed = seed if template_seed is None else template_seed
     templates = []
     for k, ts in enumerate(tsizes):
-        rng_t = np.random.default_rng([seed, 100 + k])
-        src = scene(seed * 7919 + 31 * k + 5, max(2 * ts, 64), max(2 * ts, 64), shapes=max(8, shapes // 4),
+        rng_t = np.random.default_rng([tseed, 100 + k])
+        src = scene(tseed * 7919 + 31 * k + 5, max(2 * ts, 64), max(2 * ts, 64), shapes=max(8, shapes // 4),
                     maxval=maxval)
         ty = int(rng_t.integers(0, src.shape[0] - ts + 1))
         tx = int(rng_t.integers(0, src.shape[1] - ts + 1))
@@ -253,7 +257,10 @@ def make_multi_workload(seed: int, height: int, width: int, tsizes: tuple, n_pos
             lo, hi = angle_range
             ang = lo + float(rng.integers(0, 1 << 20)) / (1 << 20) * (hi - lo)
             if all(math.hypot(row - r, col - c) > (diag + d) / 2 + 4 for r, c, d in placed):
-                poses[k].append(Pose(row, col, ang, 1.0))
+                gain = 1.0
+                if contrast > 0:
+                    gain = 1.0 - contrast + 2 * contrast * float(rng.integers(0, 1 << 20)) / (1 << 20)
+                poses[k].append(Pose(row, col, ang, gain))
                 placed.append((row, col, diag))
     for k, t in enumerate(templates):
         tf = t.astype(np.float64)
@@ -286,3 +293,20 @@ CONFIGS = {
 
 def config_workload(name: str, seed: int) -> Workload:
     return make_workload(seed, **CONFIGS[name]["gen"])
+
+
+def make_batch_workloads(seed: int, n_images: int, sizes: tuple, tsizes: tuple, max_pastes: int,
+                         angle_range: tuple = (-math.pi, math.pi), contrast: float = 0.1, noise_sigma: int = 5,
+                         maxval: int = 255) -> list:
+    """A batch of scenes of uneven size sharing one template set (one model
+    per template searches every scene): scene i has a size drawn from
+    `sizes` ((height, width) pairs) and each template pasted 1..max_pastes
+    times, with contrast U[1-c, 1+c] and noise `noise_sigma`."""
+    rng = np.random.default_rng([seed, 7])
+    batch = []
+    for i in range(n_images):
+        h, w = sizes[int(rng.integers(0, len(sizes)))]
+        n = tuple(int(rng.integers(1, max_pastes + 1)) for _ in tsizes)
+        batch.append(make_multi_workload(seed * 1000 + i + 1, h, w, tsizes, n, angle_range, noise_sigma,
+                                         maxval=maxval, contrast=contrast, template_seed=seed))
+    return batch

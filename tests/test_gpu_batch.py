@@ -1,0 +1,124 @@
+"""Batched FindNccModels (mvg_find_ncc_models_batch): scenes of uneven size
+searched for one model set on the library's host threads, several finds in
+flight.  Each image's status and matches equal the reference's find_models
+on that image (golden/batch.json; tolerances as test_gpu_parity: same count,
+order and model indices, |drow|,|dcol| <= 0.05 px, |dangle| <= 0.05 deg,
+|dscore| <= 1e-4) and, bit for bit, the single-image find_ncc_models."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from golden.batch_cases import BATCH_CASES, make_batch_inputs
+from golden.make_batch import template_digest
+from test_gpu_parity import assert_same_matches
+
+pytestmark = pytest.mark.gpu
+
+BATCH = json.loads((Path(__file__).parent / "golden" / "batch.json").read_text())["cases"]
+
+
+@pytest.fixture(scope="module")
+def mg():
+    import mvkit_gb300
+    from mvkit_gb300 import build
+    build.build()
+    mvkit_gb300.load()
+    return mvkit_gb300
+
+
+def batch_models(mg, case, batch):
+    c = case["create"]
+    return [mg.create_ncc_model(t, c["levels"], c["angle_start"], c["angle_extent"], "auto", "use_polarity")
+            for t in batch[0].templates]
+
+
+def controls(case):
+    f = case["find"]
+    return (f["angle_start"], f["angle_extent"], f["min_score"], f["num_matches"], f["max_overlap"], f["subpixel"],
+            f["num_levels"])
+
+
+@pytest.mark.parametrize("name", sorted(BATCH_CASES))
+def test_batch_matches_reference(mg, name):
+    case = BATCH_CASES[name]
+    batch = make_batch_inputs(case)
+    want = BATCH[name]
+    assert template_digest(batch[0].templates) == want["templates"]
+    assert [wl.digest() for wl in batch] == [w["digest"] for w in want["images"]]
+    models = batch_models(mg, case, batch)
+    got = mg.find_ncc_models_batch([wl.image for wl in batch], models, *controls(case), workers=4,
+                                   raise_errors=False)
+    assert len(got) == len(batch)
+    for i, (g, w) in enumerate(zip(got, want["images"])):
+        label = f"{name} image {i}"
+        if w["status"] != 0:
+            assert isinstance(g, mg.MvError) and g.status == w["status"], f"{label}: {g} vs status {w['status']}"
+            continue
+        assert not isinstance(g, mg.MvError), f"{label}: {g}"
+        wm = np.array(w["matches"]).reshape(-1, 5)
+        assert list(g[4]) == [int(x) for x in wm[:, 4]], f"{label}: model indices {list(g[4])} vs {wm[:, 4]}"
+        assert_same_matches(g[:4], wm[:, :4], label)
+
+
+def test_batch_equals_single_finds(mg):
+    """Every image of a batch, host or device memory, one or eight workers,
+    with and without a domain: the single-image result, bit for bit."""
+    case = BATCH_CASES["batch_uneven"]
+    batch = make_batch_inputs(case)
+    models = batch_models(mg, case, batch)
+    ctl = controls(case)
+    images = [wl.image for wl in batch]
+    domains = []
+    for k, im in enumerate(images):
+        d = None
+        if k % 2:
+            d = np.zeros(im.shape, np.uint8)
+            d[:, : im.shape[1] * 2 // 3] = 1
+        domains.append(d)
+    single = [mg.find_ncc_models(im, models, *ctl, domain=d) for im, d in zip(images, domains)]
+    dev = [mg.DeviceImage(im) for im in images]
+    for imgs, workers in ((images, 1), (images, 8), (dev, 3)):
+        got = mg.find_ncc_models_batch(imgs, models, *ctl, domains=domains, workers=workers)
+        for i, (g, s) in enumerate(zip(got, single)):
+            assert len(g[0]) == len(s[0]) and len(s[0]) > 0, f"image {i}, {workers} workers"
+            for x, y in zip(g, s):
+                np.testing.assert_array_equal(x, y)
+
+
+def test_batch_errors(mg):
+    """A failed image: its status per image, or the first failure raised
+    with its index; bad batch arguments raise the reference's statuses."""
+    case = BATCH_CASES["batch_360"]
+    batch = make_batch_inputs(case)
+    models = batch_models(mg, case, batch)
+    images = [wl.image for wl in batch]
+    with pytest.raises(mg.MvError) as e:
+        mg.find_ncc_models_batch(images, models, *controls(case), workers=2)
+    first = next(i for i, w in enumerate(BATCH["batch_360"]["images"]) if w["status"] != 0)
+    assert e.value.status == -103 and f"image {first}:" in e.value.message
+    with pytest.raises(mg.MvError) as e:
+        mg.find_ncc_models_batch(images, models, *controls(case), workers=0)
+    assert e.value.status == -1
+    with pytest.raises(mg.MvError) as e:
+        mg.find_ncc_models_batch(images[:1], models, *controls(case), domains=[None, None])
+    assert e.value.status == -1
+    assert mg.find_ncc_models_batch([], models, *controls(case)) == []
+
+
+def test_single_model_batch_equals_find(mg):
+    """One model: every image's matches are find_ncc_model's, bit for bit
+    (find_models with one model is find)."""
+    case = BATCH_CASES["batch_uneven"]
+    batch = make_batch_inputs(case)
+    model = batch_models(mg, case, batch)[1]
+    f = case["find"]
+    ctl = (f["angle_start"][0], f["angle_extent"][0], f["min_score"][0], 0, f["max_overlap"][0], "true",
+           f["num_levels"][0])
+    got = mg.find_ncc_models_batch([wl.image for wl in batch], [model], *ctl, workers=4)
+    for i, wl in enumerate(batch):
+        one = mg.find_ncc_model(wl.image, model, *ctl)
+        assert len(one[0]) > 0 and (got[i][4] == 0).all()
+        for x, y in zip(got[i][:4], one):
+            np.testing.assert_array_equal(x, y)

@@ -418,3 +418,31 @@ def test_find_matches_oracle_random_sweep(mg, orc, seed):
         return
     got = gpu_find(mg, gpu_model(mg, case, wl, mask), wl.image, case, domain=dom)
     assert_same_matches(got, want, f"sweep {seed}: {case}")
+
+
+def test_large_configuration_statuses(mg, orc, host_build):
+    """The large split-precision configuration (8192x8192 uint16 12-bit
+    image; 512x512 template over 360 degrees, NumLevels 6) is outside the
+    reference's budgets: the image exceeds its 32 M pixel search budget and
+    the model its 16 M raster-sample budget.  Both give the reference's
+    status and message here and in the oracle."""
+    big = np.zeros((8192, 8192), np.uint16)
+    case = CASES["cfg1_s1"]
+    wl, mask = make_inputs(case)
+    model = gpu_model(mg, case, wl, mask)
+    with pytest.raises(mg.MvError) as e:
+        mg.find_ncc_model(big, model, 0.0, 0.0, 0.5, 20, 0.3, "true", 3)
+    assert e.value.status == -103 and "pixel budget" in e.value.message
+    om = orc.create(wl.template, levels=3)
+    with pytest.raises(oracle_lib.CheckerError) as oe:
+        orc.find(om, big, 0.0, 0.0, 0.5, 20, 0.3, True, 3, 1)
+    assert oe.value.status == -103 and "pixel budget" in oe.value.message
+    tmpl = (np.random.default_rng(5).integers(0, 4096, (512, 512))).astype(np.uint16)
+    for where in ("device", "host"):
+        mg.ncc.set_model_build(where)
+        with pytest.raises(mg.MvError) as e:
+            mg.create_ncc_model(tmpl, 6, -math.pi, 2 * math.pi, "auto", "use_polarity")
+        assert e.value.status == -103 and "budget" in e.value.message
+    with pytest.raises(oracle_lib.CheckerError) as oe:
+        orc.create(tmpl, levels=6, angle_start=-math.pi, angle_extent=2 * math.pi)
+    assert oe.value.status == -103 and "budget" in oe.value.message
