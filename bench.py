@@ -59,8 +59,12 @@ def peaks() -> dict:
 
 
 def scenes(n: int, template_seed: int = 1):
+    """n distinct seeded scenes sharing one template (generated on host threads)."""
+    from concurrent.futures import ThreadPoolExecutor
+
     from mvkit_gb300 import workloads as W
-    return [W.make_workload(1000 + i, template_seed=template_seed, **GEN) for i in range(n)]
+    with ThreadPoolExecutor(max(1, min(n, os.cpu_count() or 1))) as ex:
+        return list(ex.map(lambda i: W.make_workload(1000 + i, template_seed=template_seed, **GEN), range(n)))
 
 
 class ClockSampler:
@@ -198,8 +202,8 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--batch", type=int, default=8, help="scenes per step")
-    ap.add_argument("--streams", type=int, default=8, help="finds in flight (host threads, one stream each)")
+    ap.add_argument("--batch", type=int, default=32, help="scenes per step")
+    ap.add_argument("--streams", type=int, default=32, help="finds in flight (host threads, one stream each)")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--path", default="tensor", choices=["tensor", "plain"],
                     help="correlation path of the headline line (tensor cores or FP32 CUDA cores)")
