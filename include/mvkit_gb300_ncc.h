@@ -159,7 +159,10 @@ MVG_API int32_t mvg_find_ncc_models(const void* pixels, int32_t pixel_type, int6
  * *count receives the total.  statuses[i] receives image i's status (a
  * failed image has no matches).  Returns 0 when every image succeeded, else
  * the first failed image's status, with "image <i>: <message>" as the last
- * error; the outputs are filled either way. */
+ * error; the outputs are filled either way.  The calling thread's
+ * correlation path (mvg_set_correlation_path) and current device carry over
+ * to the workers; its stage profile (mvg_profile_*) does not record the
+ * batch's finds.  Concurrent batch calls run one after the other. */
 MVG_API int32_t mvg_find_ncc_models_batch(const void* const* images, const int32_t* pixel_types,
                                           const int64_t* widths, const int64_t* heights,
                                           const int64_t* row_strides, int64_t num_images, int32_t location,
