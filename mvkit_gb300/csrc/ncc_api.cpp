@@ -2457,6 +2457,9 @@ int32_t mvg_find_ncc_models_batch(const void* const* images, const int32_t* pixe
       for (int64_t i; (i = next.fetch_add(1)) < num_images;) {
         BatchImage& b = done[size_t(i)];
         b.status = guarded([&] {
+          // an empty image finds nothing (the operator commits empty outputs,
+          // src/c_api/ncc_matching_api.cpp:178-190)
+          if (widths[i] == 0 || heights[i] == 0) return;
           const uint8_t* dom = domains ? domains[i] : nullptr;
           if (mc.models.size() > 1) {
             b.matches = run_find_models(mc.models, images[i], pixel_types[i], widths[i], heights[i],

@@ -122,3 +122,20 @@ def test_single_model_batch_equals_find(mg):
         assert len(one[0]) > 0 and (got[i][4] == 0).all()
         for x, y in zip(got[i][:4], one):
             np.testing.assert_array_equal(x, y)
+
+
+def test_batch_empty_image(mg):
+    """An empty image in a batch finds nothing (the operator commits empty
+    outputs); the other images are unaffected."""
+    case = BATCH_CASES["batch_uneven"]
+    batch = make_batch_inputs(case)[:2]
+    models = batch_models(mg, case, batch)
+    ctl = controls(case)
+    imgs = [batch[0].image, np.zeros((0, 0), np.uint8), batch[1].image]
+    got = mg.find_ncc_models_batch(imgs, models, *ctl, workers=2)
+    assert len(got) == 3 and all(len(x) == 0 for x in got[1])
+    for g, im in zip((got[0], got[2]), (batch[0].image, batch[1].image)):
+        s = mg.find_ncc_models(im, models, *ctl)
+        assert len(s[0]) > 0
+        for x, y in zip(g, s):
+            np.testing.assert_array_equal(x, y)
