@@ -122,3 +122,51 @@ def test_reference_reads_our_files():
         t = rng.integers(0, 200, size=shape).astype(dt)
         ours = mg.serialize_ncc_model(mg.create_ncc_model(t, "auto", -0.7, 1.4, "auto", "use_polarity"))
         assert ref.serialize(ref.deserialize(ours)) == ours
+
+
+@pytest.mark.parametrize("name", ["tiny16", "u16_circle"])
+def test_reader_matches_reference_on_mutated_files(name):
+    """Seeded mutations of a stored file's body (a byte replaced, a digit
+    changed, a byte inserted, the body cut short), re-checksummed so that the
+    parser sees them: the status, the message and, for accepted files, the
+    bytes written back equal the compiled reference's reader's.  Runs where
+    the reference build exists (this container)."""
+    oracle_lib = pytest.importorskip("oracle_lib")
+    ref = oracle_lib.reference("scalar")
+    if ref is None:
+        pytest.skip("reference build absent")
+    from golden.model_cases import rehash, split
+
+    magic, _, body = split((FILES / f"{name}.ncm").read_bytes())
+    digits = [i for i, c in enumerate(body) if 48 <= c <= 57]
+    rng = np.random.default_rng(11)
+
+    def ours(data):
+        try:
+            return 0, "", mg.serialize_ncc_model(mg.deserialize_ncc_model(data))
+        except mg.MvError as e:
+            return e.status, e.message, None
+
+    def theirs(data):
+        try:
+            return 0, "", ref.serialize(ref.deserialize(data))
+        except oracle_lib.CheckerError as e:
+            return e.status, e.message, None
+
+    seen = set()
+    for k in range(400):
+        b = bytearray(body)
+        kind = k % 4
+        if kind == 0:
+            b[int(rng.integers(0, len(b)))] = int(rng.integers(0, 256))
+        elif kind == 1:
+            b[digits[int(rng.integers(0, len(digits)))]] = int(rng.integers(48, 58))
+        elif kind == 2:
+            b.insert(int(rng.integers(0, len(b))), int(rng.choice([10, 32, 43, 45, 46, 48, 49, 101])))
+        else:
+            b = b[: int(rng.integers(0, len(b)))]
+        data = rehash(magic, bytes(b))
+        got, want = ours(data), theirs(data)
+        assert got == want, (k, kind, got[:2], want[:2])
+        seen.add(want[0])
+    assert 0 in seen and len(seen) >= 2  # both accepted and rejected files were exercised
