@@ -50,6 +50,18 @@ MVG_API int32_t mvg_create_ncc_model(const void* pixels, int32_t pixel_type, int
                              double angle_start, double angle_extent, double angle_step, int32_t metric,
                              mvg_ncc_model* model_id);
 
+/* One FP64 raster of a model, as the model build made it
+ * (the Patch of src/ncc_matching/model.hpp:30-43; model.cpp:39-242): level >= 0
+ * and index select the rotated raster of that level and trained angle (the
+ * reference's order), level < 0 the unrotated level-0 raster.  Fills
+ * meta[0..3] = angle, origin row, origin column, weight sum, and *count =
+ * samples; rows/cols (sample offsets as the model stores them) and weights
+ * are written when count <= capacity.  A model whose rasters were built on
+ * the device gets host copies built on the first call. */
+MVG_API int32_t mvg_ncc_model_raster(mvg_ncc_model model_id, int32_t level, int32_t index, int32_t* rows,
+                                     int32_t* cols, double* weights, int64_t capacity, double* meta,
+                                     int64_t* count);
+
 /* Replaces mv_get_ncc_model_params (include/mvkit/c/mv_ncc_matching.h:46-47).
  * angle_step is 0 for a model without angle range, as the reference reports. */
 MVG_API int32_t mvg_get_ncc_model_params(mvg_ncc_model model_id, int32_t* num_levels, double* angle_start,

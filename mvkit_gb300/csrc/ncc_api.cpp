@@ -2353,6 +2353,42 @@ int32_t mvg_get_ncc_model_params(mvg_ncc_model model_id, int32_t* num_levels, do
   });
 }
 
+int32_t mvg_ncc_model_raster(mvg_ncc_model model_id, int32_t level, int32_t index, int32_t* rows, int32_t* cols,
+                             double* weights, int64_t capacity, double* meta, int64_t* count) {
+  return guarded([&] {
+    if (!model_id || !count) raise(kInvalidArgument, "model and count must not be null");
+    *count = 0;
+    std::unique_lock<std::mutex> lock(model_id->mutex);
+    HostModel& h = model_id->host;
+    const Raster* r = nullptr;
+    if (level < 0) {
+      r = &h.original;
+    } else {
+      if (size_t(level) >= h.levels.size()) raise(kInvalidArgument, "level out of range");
+      // a model whose rasters were built on the device gets host copies here
+      if (!h.rasters) {
+        build_rasters(h);
+        h.rasters = true;
+      }
+      const auto& ps = h.levels[size_t(level)].patches;
+      if (index < 0 || size_t(index) >= ps.size()) raise(kInvalidArgument, "raster index out of range");
+      r = &ps[size_t(index)];
+    }
+    if (meta) {
+      meta[0] = r->angle;
+      meta[1] = r->orow;
+      meta[2] = r->ocol;
+      meta[3] = r->wsum;
+    }
+    const int64_t n = int64_t(r->size());
+    *count = n;
+    if (n > capacity || !rows || !cols || !weights) return;
+    std::copy(r->rows.begin(), r->rows.end(), rows);
+    std::copy(r->cols.begin(), r->cols.end(), cols);
+    std::copy(r->w.begin(), r->w.end(), weights);
+  });
+}
+
 int32_t mvg_clear_ncc_model(mvg_ncc_model model_id) {
   return guarded([&] { delete model_id; });
 }

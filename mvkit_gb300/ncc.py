@@ -660,6 +660,31 @@ class PinnedBuffer:
 PROFILE_STAGES = 13
 
 
+def ncc_model_raster(model: NccModel, level: int, index: int = 0) -> dict:
+    """One FP64 raster of the model as its build made it (the Patch of
+    src/ncc_matching/model.hpp:30-43): level >= 0 and index select the
+    rotated raster of that level and trained angle, level < 0 the unrotated
+    level-0 raster.  Returns angle, origin_row, origin_column, weight_sum
+    and the rows, cols and weights arrays."""
+    op = "ncc_model_raster"
+    if not isinstance(model, NccModel) or not model.handle:
+        raise MvError(MV_STATUS_TYPE_MISMATCH, "ModelID: NCC model handle required", op)
+    lib = load()
+    f = lib.mvg_ncc_model_raster
+    f.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                  _i64p]
+    f.restype = C.c_int32
+    meta = np.zeros(4)
+    cnt = C.c_int64()
+    _check(f(model.handle, int(level), int(index), None, None, None, 0, meta.ctypes.data, C.byref(cnt)), op)
+    n = int(cnt.value)
+    rows, cols, w = np.zeros(n, np.int32), np.zeros(n, np.int32), np.zeros(n)
+    _check(f(model.handle, int(level), int(index), rows.ctypes.data, cols.ctypes.data, w.ctypes.data, n,
+             meta.ctypes.data, C.byref(cnt)), op)
+    return dict(angle=meta[0], origin_row=meta[1], origin_column=meta[2], weight_sum=meta[3], rows=rows, cols=cols,
+                weights=w)
+
+
 def set_model_build(where: str) -> None:
     """'device' (default): models' rotated rasters are built on the GPU when
     one is present; 'host': in FP64 on the CPU.  Same weights bit for bit."""
