@@ -78,6 +78,10 @@ def test_rasters_equal_oracle_and_reference(host_build, name):
                         ignore_polarity=c.get("ignore", False), mask=mask)
         info = om.info()
         assert info["levels"] == levels
+        # the operator reports step 0 for a model without angle range
+        # (src/c_api/ncc_matching_api.cpp:85-96)
+        step = mg.get_ncc_model_params(model)[3]
+        assert step == (info["angle_step"] if c["ext"] != 0 else 0.0)
         same(ncc.ncc_model_raster(model, -1), om.patch(-1, 0), f"{name} original")
         per_level = info["patches"]  # one raster per trained angle on every level
         for lv in range(levels):
