@@ -325,7 +325,9 @@ def main():
 
     def batch_step():
         # the batched operator on host images: uploads, finds on the
-        # library's host threads (one stream each) and result read-back
+        # library's host threads (one stream each, the calling thread's
+        # correlation path) and result read-back
+        mg.set_correlation_path(args.path)
         return mg.find_ncc_models_batch(host_images, [model], *ctl, workers=threads)
 
     for _ in range(args.warmup):
