@@ -244,15 +244,24 @@ MVG_API int32_t mvg_ncc_pyramid_level(const void* pixels, int32_t pixel_type, in
  * with a device-memory budget fixed at start-up.  No counterpart in the
  * reference (its pyramid is an internal step of the find).
  *
- * pixels: the image in device memory (row_stride bytes apart); out: a device
- * buffer of out_capacity floats that receives the level, row-major,
- * *out_width x *out_height.  Allocates nothing: the levels below the
+ * pixels: the image in device memory of the current device (row_stride
+ * bytes apart, aligned to the pixel size); out: a device buffer of the same
+ * device, 4-byte aligned, of out_capacity floats that receives the level,
+ * row-major, *out_width x *out_height.  A host pointer (pageable or
+ * page-locked), a pointer into another device's memory or a misaligned
+ * pointer is rejected with MV_STATUS_INVALID_ARGUMENT (-1) before anything
+ * is launched; images taller than 524280 rows (the pyramid grid's limit)
+ * with MV_STATUS_LIMIT_EXCEEDED.  Level sums at or above 2^24 (uint16 from
+ * level 5) are not exact in float: the call returns MV_STATUS_UNSUPPORTED
+ * (-6), as mvg_ncc_pyramid_level does.  Allocates nothing: the levels below the
  * requested one are built in one fixed device array of 6 Mi floats (24 MiB)
  * that the library holds on every GPU that loads it until the process exits;
  * images whose lower levels need more than that are rejected with
  * MV_STATUS_LIMIT_EXCEEDED (-103).  The first call on a device looks the
  * array's device address up (cudaGetSymbolAddress) with that device current;
- * make that first call before any stream capture.  All calls share the
+ * make that first call before any stream capture.  The address stays cached
+ * for the process's life: after a cudaDeviceReset of a device, do not call
+ * this entry point on that device again.  All calls share the
  * array: calls that overlap on the GPU (concurrent streams or threads on one
  * device) race and must be serialised by the caller.  stream: a cudaStream_t
  * or NULL; the call returns when the level is complete. */

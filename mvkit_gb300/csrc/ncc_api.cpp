@@ -2737,7 +2737,9 @@ int32_t mvg_ncc_pyramid_level(const void* pixels, int32_t pixel_type, int64_t wi
     }
     if (int64_t(w) * h > capacity) raise(kInvalidArgument, "output capacity too small");
     check(cudaMemcpyAsync(out, lev[level].v, size_t(w) * size_t(h) * sizeof(float), cudaMemcpyDeviceToHost, s), "copy");
+    check(cudaMemcpyAsync(ws.h_state, ws.state.p, sizeof(QueryState), cudaMemcpyDeviceToHost, s), "state");
     check(cudaStreamSynchronize(s), "sync");
+    if (ws.h_state->error) raise_device_error(ws.h_state->error);
     const uint8_t* px = static_cast<const uint8_t*>(pixels);
     geom[0] = w;
     geom[1] = h;

@@ -26,6 +26,7 @@ namespace {
 
 constexpr size_t kScratchFloats = size_t(6) * 1024 * 1024;  // levels 0..L-1 of the requested level
 constexpr int kMaxDevices = 64;
+constexpr int kMaxRows = 65535 * 8;  // pyramid grid: 8 rows per block, 65535 blocks in y
 
 // Shared by every call on a device; a call clears what it needs before use.
 static __device__ __align__(256) float g_level_scratch[kScratchFloats];
@@ -39,15 +40,12 @@ struct DeviceScratch {
 std::mutex g_setup_mutex;
 DeviceScratch g_scratch[kMaxDevices];
 
-// Device addresses of the scratch arrays on the current device, looked up
-// once per device with that device current.
-int32_t scratch_of_current_device(DeviceScratch* out, std::string* why) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) {
-    *why = std::string("cudaGetDevice: ") + cudaGetErrorString(e);
-    return kInternal;
-  }
+// Device addresses of the scratch arrays on device `dev` (current), looked up
+// once per device with that device current.  A cudaDeviceReset destroys the
+// context that holds them; the process must not call this entry point on
+// that device again afterwards.
+int32_t scratch_of_device(int dev, DeviceScratch* out, std::string* why) {
+  cudaError_t e = cudaSuccess;
   if (dev < 0 || dev >= kMaxDevices) {
     *why = "device index beyond the scratch table";
     return kUnsupported;
@@ -78,6 +76,28 @@ int32_t fail(int32_t status, const std::string& message) {
   return status;
 }
 
+// True when `p` is device (or managed) memory of device `dev`.  A host
+// pointer, pageable or pinned, would make the kernels fault or, where the GPU
+// can reach host memory, read and write the wrong memory.
+bool on_device(const void* p, int dev, std::string* why) {
+  cudaPointerAttributes a{};
+  const cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *why = std::string("cudaPointerGetAttributes: ") + cudaGetErrorString(e);
+    return false;
+  }
+  if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged) {
+    *why = "not device memory";
+    return false;
+  }
+  if (a.device != dev) {
+    *why = "memory of device " + std::to_string(a.device) + ", not of the current device " + std::to_string(dev);
+    return false;
+  }
+  return true;
+}
+
 }  // namespace
 }  // namespace mvg
 
@@ -94,7 +114,12 @@ extern "C" MVG_API int32_t mvg_ncc_pyramid_level_noalloc(const void* pixels, int
   if (width <= 0 || height <= 0 || width > (1 << 30) || height > (1 << 30) || row_stride < width * bpp ||
       row_stride % bpp)
     return fail(kInvalidArgument, "invalid image geometry");
+  if (reinterpret_cast<uintptr_t>(pixels) % uintptr_t(bpp))
+    return fail(kInvalidArgument, "pixels must be aligned to the pixel size");
+  if (reinterpret_cast<uintptr_t>(out) % alignof(float)) return fail(kInvalidArgument, "out must be 4-byte aligned");
   if (level < 0 || level > 15) return fail(kInvalidArgument, "level must be 0..15");
+  // the pyramid kernels run one block per 8 rows; the grid's y extent is 65535
+  if (height > int64_t(kMaxRows)) return fail(kLimitExceeded, "image taller than " + std::to_string(kMaxRows) + " rows");
   // level geometry (2x2 sums, floor, never below one pixel) and the scratch
   // the levels below the requested one need
   int64_t w = width, h = height, below = 0;
@@ -108,12 +133,20 @@ extern "C" MVG_API int32_t mvg_ncc_pyramid_level_noalloc(const void* pixels, int
                                     std::to_string(below) + " floats, the scratch holds " +
                                     std::to_string(kScratchFloats));
   if (w * h > out_capacity) return fail(kInvalidArgument, "output capacity too small for the level");
-  DeviceScratch sc;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(kInternal, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  }
   std::string why;
-  const int32_t st = scratch_of_current_device(&sc, &why);
+  if (!on_device(pixels, dev, &why)) return fail(kInvalidArgument, "pixels: " + why);
+  if (!on_device(out, dev, &why)) return fail(kInvalidArgument, "out: " + why);
+  DeviceScratch sc;
+  const int32_t st = scratch_of_device(dev, &sc, &why);
   if (st != kOk) return fail(st, why);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  cudaError_t e = cudaMemsetAsync(sc.flag, 0, sizeof(int32_t), s);
+  e = cudaMemsetAsync(sc.flag, 0, sizeof(int32_t), s);
   if (e != cudaSuccess) return fail(kInternal, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
   LevelImage prev;
   int64_t at = 0, lw = width, lh = height;

@@ -87,3 +87,26 @@ def test_find_controls_rejected_like_reference(over, status):
 def test_find_controls_accept_level_pair():
     r = ncc._find_controls("find_ncc_model", 0.0, 0.1, 0.7, 0, 0.5, "false", [3, 2])
     assert r == (0.0, 0.1, 0.7, 0, 0.5, 0, 3, 2)
+
+
+def test_noalloc_pyramid_refuses_misaligned_and_host_pointers_without_launching():
+    """The no-allocation pyramid checks its pointers on the host: misaligned
+    pointers are refused before any CUDA call, host memory before any launch
+    (here, without a GPU, the pointer query itself fails)."""
+    import ctypes as C
+    lib = mg.load()
+    f = lib.mvg_ncc_pyramid_level_noalloc
+    f.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int32, C.c_void_p, C.c_int64,
+                  C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_void_p]
+    f.restype = C.c_int32
+    img = np.zeros(64 * 64 + 8, np.uint16)
+    out = np.zeros(64 * 64 + 4, np.float32)
+    ow, oh = C.c_int64(), C.c_int64()
+    base, obase = img.ctypes.data, out.ctypes.data
+    assert f(base + 1, 1, 64, 64, 128, 1, obase, 64 * 64, C.byref(ow), C.byref(oh), None) == -1
+    assert b"aligned" in lib.mvg_last_error()
+    assert f(base, 1, 64, 64, 128, 1, obase + 2, 64 * 64, C.byref(ow), C.byref(oh), None) == -1
+    assert b"aligned" in lib.mvg_last_error()
+    assert f(base, 0, 64, 600000, 64, 0, obase, 64 * 64, C.byref(ow), C.byref(oh), None) == -103
+    st = f(base, 1, 64, 64, 128, 1, obase, 64 * 64, C.byref(ow), C.byref(oh), None)
+    assert st in (-1, -1000) and lib.mvg_last_error()
