@@ -17,7 +17,10 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_lib"
 LIB = OUT / "libmvkit_gb300.so"
+# the reference-signature C layer (include/mvkit_gb300_mv.h), linked against LIB
+MV_LIB = OUT / "libmvkit_gb300_mv.so"
 SOURCES = ["ncc_kernels.cu", "ncc_tc.cu", "ncc_api.cpp", "ncc_model.cpp", "ncc_persist.cpp", "ncc_build.cu", "ncc_noalloc.cu"]
+MV_SOURCES = ["mv_objects.cpp", "mv_ncc.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -39,8 +42,10 @@ def _flags(src: str) -> list[str]:
 
 def build(verbose: bool = False, force: bool = False) -> Path:
     OUT.mkdir(exist_ok=True)
-    deps = [CSRC / s for s in SOURCES] + list(CSRC.glob("*.h")) + [PKG.parent / "include" / "mvkit_gb300_ncc.h"]
-    if LIB.exists() and not force and all(d.stat().st_mtime <= LIB.stat().st_mtime for d in deps):
+    deps = ([CSRC / s for s in SOURCES + MV_SOURCES] + list(CSRC.glob("*.h")) +
+            list((PKG.parent / "include").glob("*.h")))
+    if (LIB.exists() and MV_LIB.exists() and not force and
+            all(d.stat().st_mtime <= min(LIB.stat().st_mtime, MV_LIB.stat().st_mtime) for d in deps)):
         return LIB
     cc = nvcc()
 
@@ -56,14 +61,17 @@ def build(verbose: bool = False, force: bool = False) -> Path:
             print(r.stdout, r.stderr, file=sys.stderr)
         return obj
 
-    with ThreadPoolExecutor(len(SOURCES)) as ex:
-        objs = list(ex.map(compile_one, SOURCES))
-    link = [cc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart"]
-    if verbose:
-        print(" ".join(link), flush=True)
-    r = subprocess.run(link, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    with ThreadPoolExecutor(len(SOURCES) + len(MV_SOURCES)) as ex:
+        objs = list(ex.map(compile_one, SOURCES + MV_SOURCES))
+    link = [cc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs[:len(SOURCES)]), "-lcudart"]
+    mv_link = ["g++", "-shared", "-o", str(MV_LIB), *map(str, objs[len(SOURCES):]), f"-L{OUT}", "-lmvkit_gb300",
+               "-Wl,-rpath,$ORIGIN", "-Wl,--no-undefined"]
+    for cmd in (link, mv_link):
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     return LIB
 
 

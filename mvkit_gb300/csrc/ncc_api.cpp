@@ -2052,8 +2052,22 @@ template <class Fn> int32_t guarded(Fn&& fn) {
   }
 }
 
+// Controls of a single-model find, checked as NccControls checks them
+// (src/c_api/ncc_matching_api.cpp:140-157): AngleExtent within [0, 2 pi],
+// lowest level 0 read as 1.
 FindParams make_params(double angle_start, double angle_extent, double min_score, int64_t num_matches,
                        double max_overlap, int32_t subpixel, int32_t highest, int32_t lowest) {
+  auto number = [](double x, double lo, double hi, const char* name) {
+    if (!std::isfinite(x) || x < lo || x > hi)
+      raise(kInvalidArgument, std::string(name) + ": numeric control outside allowed range");
+  };
+  number(angle_start, -std::numeric_limits<double>::max(), std::numeric_limits<double>::max(), "AngleStart");
+  number(angle_extent, 0, 6.28318530717958647692, "AngleExtent");
+  number(min_score, 0, 1, "MinScore");
+  number(max_overlap, 0, 1, "MaxOverlap");
+  if (num_matches < 0) raise(kInvalidArgument, "NumMatches: match count must be nonnegative");
+  if (subpixel != 0 && subpixel != 1) raise(kInvalidArgument, "SubPixel: expected true or false");
+  if (highest < 0 || lowest < 0) raise(kInvalidArgument, "NumLevels: invalid highest/lowest level pair");
   FindParams p;
   p.angle_start = angle_start;
   p.angle_extent = angle_extent;
