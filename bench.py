@@ -132,20 +132,82 @@ def traffic_from_profiles(kernel: str):
     return None
 
 
-def cpu_baseline(images, threads: int) -> dict:
+def cpu_baseline(images, threads: int):
+    """The oracle on this host's cores, one scene per thread (the first
+    `threads` scenes); returns the baseline and each scene's matches."""
+    from concurrent.futures import ThreadPoolExecutor
+
     import oracle_lib
     orc = oracle_lib.oracle()
     wl = images[0]
     model = orc.create(wl.template, levels=CREATE["num_levels"], angle_start=CREATE["angle_start"],
                        angle_extent=CREATE["angle_extent"])
     sample = [images[i % len(images)].image for i in range(threads)]
-    t0 = time.perf_counter()
-    n = orc.find_many(model, sample, threads, FIND["angle_start"], FIND["angle_extent"], FIND["min_score"],
-                      FIND["num_matches"], FIND["max_overlap"], True, 4, 1)
-    dt = time.perf_counter() - t0
-    return {"value": len(sample) / dt, "unit": "images/s", "cores": threads, "kind": "port",
+
+    def one(im):  # the ctypes call releases the GIL: the finds run in parallel
+        return orc.find(model, im, FIND["angle_start"], FIND["angle_extent"], FIND["min_score"],
+                        FIND["num_matches"], FIND["max_overlap"], True, 4, 1)
+
+    with ThreadPoolExecutor(threads) as ex:
+        t0 = time.perf_counter()
+        results = list(ex.map(one, sample))
+        dt = time.perf_counter() - t0
+    n = sum(len(r) for r in results)
+    base = {"value": len(sample) / dt, "unit": "images/s", "cores": threads, "kind": "port",
             "sample": f"{len(sample)} scenes of {WORKLOAD}, one per thread, FP64 oracle restatement "
                       f"of the reference scalar path ({n} matches)", "seconds": dt}
+    return base, [oracle_lib.to_halcon(r) for r in results[:min(threads, len(images))]]
+
+
+def halcon(row, col, angle):
+    """The operator's edge-centred pose of a matcher pose (ncc_matching_api.cpp:171-176)."""
+    c, s = math.cos(angle), math.sin(angle)
+    return row + .5 * (1 - c + s), col + .5 * (1 - c - s)
+
+
+def pose_error(found, images, oracle=None) -> dict:
+    """Pose errors of the timed finds: against each scene's pasted poses (the
+    generator's ground truth, nearest match per pose) and, on the oracle's
+    sample, against the FP64 oracle (same count and order required)."""
+    dr, dc, da, missing = [], [], [], 0
+    for (rows, cols, angles, scores), wl in zip(found, images):
+        got = np.stack([rows, cols, angles], axis=1) if len(rows) else np.zeros((0, 3))
+        for p in wl.poses:
+            r, c = halcon(p.row, p.column, p.angle)
+            if not len(got):
+                missing += 1
+                continue
+            k = int(np.argmin(np.hypot(got[:, 0] - r, got[:, 1] - c)))
+            if math.hypot(got[k, 0] - r, got[k, 1] - c) > 2.0:
+                missing += 1
+                continue
+            dr.append(abs(got[k, 0] - r))
+            dc.append(abs(got[k, 1] - c))
+            da.append(abs(math.degrees(got[k, 2] - p.angle)))
+    out = {"vs_truth": {"scenes": len(images), "poses": sum(len(w.poses) for w in images), "unmatched": missing,
+                        "max_drow": max(dr, default=None), "max_dcol": max(dc, default=None),
+                        "max_dangle_deg": max(da, default=None),
+                        "note": "nearest match per pasted pose: the NCC optimum of a noisy bilinear paste lies "
+                                "off the pasted pose, for the FP64 oracle as well (oracle_on_its_sample)"}}
+    if oracle is not None:
+        o = pose_error([(r[:, 0], r[:, 1], r[:, 2], r[:, 3]) for r in oracle], images[:len(oracle)])["vs_truth"]
+        out["vs_truth"]["oracle_on_its_sample"] = {k: o[k] for k in ("scenes", "unmatched", "max_drow", "max_dcol",
+                                                                     "max_dangle_deg")}
+    if oracle is not None:
+        same, d = True, np.zeros(4)
+        for (rows, cols, angles, scores), want in zip(found, oracle):
+            got = np.stack([rows, cols, angles, scores], axis=1) if len(rows) else np.zeros((0, 4))
+            if got.shape != want.shape:
+                same = False
+                continue
+            if len(got):
+                d = np.maximum(d, np.abs(got - want).max(axis=0))
+        out["vs_oracle"] = {"scenes": len(oracle), "count_and_order_equal": same, "max_drow": float(d[0]),
+                            "max_dcol": float(d[1]), "max_dangle_deg": math.degrees(float(d[2])),
+                            "max_dscore": float(d[3]),
+                            "within_tolerance": bool(same and d[0] <= .05 and d[1] <= .05 and
+                                                     math.degrees(d[2]) <= .05 and d[3] <= 1e-4)}
+    return out
 
 
 def max_over_ranks(x: float, device: str = "cuda") -> float:
@@ -335,6 +397,8 @@ def main():
         batch_step()
     torch.cuda.synchronize()
 
+    batch_found = []
+
     def timed_batch(steps: int):
         total = 0.0
         for _ in range(steps):
@@ -343,9 +407,10 @@ def main():
             if world > 1:
                 torch.distributed.barrier()
             t0 = time.perf_counter()
-            batch_step()
+            out = batch_step()
             torch.cuda.synchronize()
             total += (time.perf_counter() - t0) * 1e3
+        batch_found[:] = out
         return total
 
     with ClockSampler(local) as clocks:
@@ -436,8 +501,14 @@ def main():
     }
     if other is not None:
         line["compare"] = other
+    oracle = None
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(wls, os.cpu_count() or 1)
+        line["cpu_baseline"], oracle = cpu_baseline(wls, os.cpu_count() or 1)
+    line["pose_error"] = pose_error(found, wls, oracle)
+    # the e2e pass (batched operator, host images) returns the value pass's matches
+    line["pose_error"]["e2e_equals_value_pass"] = bool(
+        len(batch_found) == len(found) and
+        all(all(np.array_equal(a, b) for a, b in zip(x[:4], y[:4])) for x, y in zip(batch_found, found)))
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

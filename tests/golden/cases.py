@@ -167,12 +167,14 @@ def search_domain(case: dict, wl):
     return m
 
 
-# Large single-GPU throughput case, checked against the oracle at full size.
+# The throughput configuration (2048^2 u8, one 128^2 template pasted 5 times
+# at U[-30, 30] degrees), five seeds, checked against the reference at full size.
 LARGE = {
-    "cfg2_s1": dict(gen=dict(seed=1, height=2048, width=2048, tsize=128, n_poses=5, angle_range=(-D(30), D(30))),
-                    create=dict(levels=4, angle_start=-D(30), angle_extent=D(60)),
-                    find=dict(angle_start=-D(30), angle_extent=D(60), min_score=0.7, num_matches=5,
-                              max_overlap=0.5, subpixel=True, highest=4, lowest=1)),
+    f"cfg2_s{k}": dict(gen=dict(seed=k, height=2048, width=2048, tsize=128, n_poses=5, angle_range=(-D(30), D(30))),
+                       create=dict(levels=4, angle_start=-D(30), angle_extent=D(60)),
+                       find=dict(angle_start=-D(30), angle_extent=D(60), min_score=0.7, num_matches=5,
+                                 max_overlap=0.5, subpixel=True, highest=4, lowest=1))
+    for k in range(1, 6)
 }
 
 

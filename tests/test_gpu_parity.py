@@ -207,13 +207,14 @@ def test_find_models_single_equals_find(mg):
         np.testing.assert_array_equal(a, b)
 
 
-def test_find_matches_reference_2048(mg):
-    case = LARGE["cfg2_s1"]
+@pytest.mark.parametrize("name", list(LARGE))
+def test_find_matches_reference_2048(mg, name):
+    case = LARGE[name]
     wl, mask = make_inputs(case)
-    assert wl.digest() == GOLDEN["cfg2_s1"]["digest"]
+    assert wl.digest() == GOLDEN[name]["digest"]
     model = gpu_model(mg, case, wl, mask)
     got = gpu_find(mg, model, wl.image, case)
-    assert_same_matches(got, GOLDEN["cfg2_s1"]["matches"], "cfg2_s1")
+    assert_same_matches(got, GOLDEN[name]["matches"], name)
 
 
 @pytest.mark.parametrize("seed", [31, 32, 33])
@@ -259,9 +260,10 @@ def path(mg, request):
 
 @pytest.mark.parametrize("path", ["tensor", "plain"], indirect=True)
 @pytest.mark.parametrize("name", ["cfg1_s1", "rot3_all", "rot_l4_2", "u16_rot", "polarity", "full_circle",
-                                  "u16_12bit", "tiny16", "roi_two", "roi_ring", "roi_strips", "roi_no_subpixel"])
+                                  "u16_12bit", "tiny16", "roi_two", "roi_ring", "roi_strips", "roi_no_subpixel",
+                                  "cfg2_s1"])
 def test_candidate_stages_match_oracle(mg, orc, name, path):
-    case = CASES[name]
+    case = {**CASES, **LARGE}[name]
     wl, mask = make_inputs(case)
     c, f = case["create"], case["find"]
     om = orc.create(wl.template, levels=c["levels"], angle_start=c["angle_start"], angle_extent=c["angle_extent"],
@@ -277,7 +279,9 @@ def test_candidate_stages_match_oracle(mg, orc, name, path):
         got = mg.find_ncc_model_stage(wl.image, model, *ctl, stage=stage, domain=dom)
         a, b = pose_set(got), pose_set(want)
         sym = len(a ^ b)
-        assert sym <= max(2, len(b) // 100), f"{name} stage {stage}: {len(a)} vs {len(b)} candidates, {sym} differ"
+        # identical sets on every case measured; at most a near-tie pair
+        # (two candidates whose FP32 and FP64 scores order differently) may swap
+        assert sym <= 2, f"{name} stage {stage}: {len(a)} vs {len(b)} candidates, {sym} differ"
         # scores of the common candidates agree to FP32 precision
         ws = {(r[0], r[1], r[2]): r[3] for r in want}
         for r in got:
@@ -291,7 +295,7 @@ def test_candidate_stages_match_oracle(mg, orc, name, path):
     want = want[np.isfinite(want[:, 3])]   # the find loop skips unscorable candidates
     ws = {(r[0], r[1], r[2]): r[3] for r in want}
     common = [r for r in got if (r[0], r[1], r[2]) in ws]
-    assert len(common) >= 0.98 * len(want)
+    assert len(common) >= len(want) - 2 and len(got) <= len(want) + 2
     assert np.all(np.diff(got[:, 3]) <= 0), "sorted by score"
     for r in common:
         assert abs(r[3] - ws[(r[0], r[1], r[2])]) < 1e-4

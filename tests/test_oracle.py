@@ -56,12 +56,13 @@ def test_oracle_matches_reference_golden(orc, name):
 
 
 @pytest.mark.slow
-def test_oracle_matches_reference_golden_large(orc):
-    case = LARGE["cfg2_s1"]
+@pytest.mark.parametrize("name", list(LARGE))
+def test_oracle_matches_reference_golden_large(orc, name):
+    case = LARGE[name]
     wl, mask = make_inputs(case)
-    assert wl.digest() == GOLDEN["cfg2_s1"]["digest"]
+    assert wl.digest() == GOLDEN[name]["digest"]
     _, res = run(orc, case, wl, mask)
-    np.testing.assert_array_equal(res, np.array(GOLDEN["cfg2_s1"]["matches"]).reshape(-1, 4))
+    np.testing.assert_array_equal(res, np.array(GOLDEN[name]["matches"]).reshape(-1, 4))
 
 
 def test_avx2_reference_agrees_with_scalar_within_fp64_noise():
