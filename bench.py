@@ -6,15 +6,17 @@ AngleStart -30 deg, AngleExtent 60 deg, automatic angle step, NumLevels 4;
 FindNccModel MinScore 0.7, NumMatches 5, MaxOverlap 0.5, SubPixel true.
 A step is one find on each of `--batch` distinct scenes.
 
-value: images/s with the scenes resident in HBM (CUDA events on the find
-stream, L2 flushed between steps).  e2e: the same scenes through the batched
-operator (mvg_find_ncc_models_batch) from page-locked host buffers, wall
-clock around each step (upload, the finds on the library's host threads and
-the result read-back inside the timed region).  roofline: the correlation kernel, its algorithmic multiply-adds
-over its live event time, from a second timed pass of the same steps with
-CUDA events around each kernel group (the value pass carries no events).  cpu_baseline: the FP64
-oracle restatement of the reference on this host's cores (one scene per
-thread).
+value: images/s with the scenes resident in HBM, through the batched operator
+(mvg_find_ncc_models_batch: 32 finds in flight on the library's host
+threads, their tensor-core launches merged), CUDA events around each step's
+call, L2 flushed between steps.  e2e: the same calls on page-locked host
+images, wall clock around each step (upload, the finds and the result
+read-back inside the timed region).  roofline: the merged tensor-core
+launches of the value pass, all finds' algorithmic multiply-adds over the
+launches' event time; beside it the same kernel launched per find.
+cpu_baseline: the FP64 oracle restatement of the reference on this host's
+cores (one scene per thread); its matches are the parity check of the value
+pass's poses.
 
 --impl reference: the reference's CPU implementation of the path (the oracle
 port here; the reference itself when it was compiled on this machine), all
@@ -210,6 +212,12 @@ def pose_error(found, images, oracle=None) -> dict:
     return out
 
 
+def same_results(a, b) -> bool:
+    """Two passes' per-scene (Row, Column, Angle, Score) are bit-identical."""
+    return bool(len(a) == len(b) and
+                all(all(np.array_equal(u, v) for u, v in zip(x[:4], y[:4])) for x, y in zip(a, b)))
+
+
 def max_over_ranks(x: float, device: str = "cuda") -> float:
     """The largest x over the replicas (all-reduce MAX); x itself on one."""
     import torch
@@ -270,6 +278,8 @@ def main():
     ap.add_argument("--path", default="tensor", choices=["tensor", "plain"],
                     help="correlation path of the headline line (tensor cores or FP32 CUDA cores)")
     ap.add_argument("--no-compare", action="store_true", help="skip timing the other correlation path")
+    ap.add_argument("--cohorts", type=int, default=0,
+                    help="groups of finds in flight whose tensor-core launches are merged (0: per find)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -368,14 +378,47 @@ def main():
         profiles.clear()
         return prof
 
+    host_images = [pb.array for pb in pinned]
+
+    def batch_step(images, merge=None):
+        # the batched operator: finds on the library's host threads (one
+        # stream each, the calling thread's correlation path), tensor-core
+        # launches merged across the finds in flight; results read back
+        mg.set_correlation_path(path[0])
+        mg.set_batch_merge(args.cohorts if merge is None else merge)
+        return mg.find_ncc_models_batch(images, [model], *ctl, workers=threads)
+
+    batch_found = []
+
+    def timed_batch(images, steps: int, merge=None, events=True):
+        """Per step: L2 flush, then one batched call between CUDA events
+        (device-resident images) or wall-clock stamps (host images); the call
+        returns once its results are on the host."""
+        total = 0.0
+        st = streams[0]
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            if world > 1:
+                torch.distributed.barrier()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            t0 = time.perf_counter()
+            e0.record(st)
+            out = batch_step(images, merge)
+            e1.record(st)
+            torch.cuda.synchronize()
+            total += e0.elapsed_time(e1) if events else (time.perf_counter() - t0) * 1e3
+        batch_found[:] = out
+        return total
+
     # the other correlation path, device-resident scenes, same protocol
     other = None
     if not args.no_compare:
         path[0] = "plain" if args.path == "tensor" else "tensor"
         for _ in range(args.warmup):
-            one_step(dev, False)
+            batch_step(dev)
         torch.cuda.synchronize()
-        other_ms = timed(dev, False, args.steps)
+        other_ms = timed_batch(dev, args.steps)
         timed(dev, False, args.steps, profile=True)
         oprof = aggregate()
         other = {"path": path[0], "ms": other_ms,
@@ -383,44 +426,31 @@ def main():
                                         if isinstance(v, dict)}}
         path[0] = args.path
 
-    host_images = [pb.array for pb in pinned]
-
-    def batch_step():
-        # the batched operator on host images: uploads, finds on the
-        # library's host threads (one stream each, the calling thread's
-        # correlation path) and result read-back
-        mg.set_correlation_path(args.path)
-        return mg.find_ncc_models_batch(host_images, [model], *ctl, workers=threads)
-
     for _ in range(args.warmup):
-        one_step(dev, False)
-        batch_step()
+        batch_step(dev)
+        batch_step(host_images)
     torch.cuda.synchronize()
 
-    batch_found = []
-
-    def timed_batch(steps: int):
-        total = 0.0
-        for _ in range(steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            if world > 1:
-                torch.distributed.barrier()
-            t0 = time.perf_counter()
-            out = batch_step()
-            torch.cuda.synchronize()
-            total += (time.perf_counter() - t0) * 1e3
-        batch_found[:] = out
-        return total
-
+    mg.batch_profile_reset()
     with ClockSampler(local) as clocks:
-        dev_ms = timed(dev, False, args.steps)
-    # the same steps again with CUDA events around each kernel group on the
-    # find streams: stage times, launch counts and the roofline (the events
-    # stay out of the value pass)
+        dev_ms = timed_batch(dev, args.steps)
+    merged = mg.batch_profile_read()
+    value_found = [r[:4] for r in batch_found]
+    # ablation: the same steps with the other launch policy (merged within
+    # one cohort of all finds in flight, or one launch per find)
+    alt_cohorts = (1 if args.cohorts == 0 else 0) if args.path == "tensor" else None
+    alt_ms, alt_same, alt_merged = None, None, None
+    if alt_cohorts is not None:
+        mg.batch_profile_reset()
+        alt_ms = timed_batch(dev, args.steps, merge=alt_cohorts)
+        alt_merged = mg.batch_profile_read()
+        alt_same = same_results(batch_found, value_found)
+    # the same steps again from per-find host threads with CUDA events around
+    # each kernel group on the find streams: stage times and launch counts
+    # (the events stay out of the value pass)
     timed(dev, False, args.steps, profile=True)
     prof = aggregate()
-    host_ms = timed_batch(args.steps)
+    host_ms = timed_batch(host_images, args.steps, events=False)
 
     # the same finds one at a time (untimed): per-kernel event times without
     # other streams' kernels interleaved
@@ -458,24 +488,48 @@ def main():
     # the CUDA-core tracking kernel
     rstage = "track_tc" if args.path == "tensor" and stages.get("track_tc", {}).get("ms") else "track"
     d = stages[rstage]
-    achieved = 2.0 * d["work"] / (d["ms"] / 1e3) / 1e12 if d["ms"] else None
+    achieved_sep = 2.0 * d["work"] / (d["ms"] / 1e3) / 1e12 if d["ms"] else None
     di = iso[rstage]
     achieved_iso = 2.0 * di["work"] / (di["ms"] / 1e3) / 1e12 if di["ms"] else None
-    roof = {"bound": "tensor", "achieved": achieved, "peak": pk["tflops_sustained"], "unit": "TFLOP/s",
-            "frac": achieved / pk["tflops_sustained"] if achieved else None,
+    peak = pk["tflops_sustained"]
+    def merged_roof(m):
+        a = 2.0 * m["macs"] / (m["ms"] / 1e3) / 1e12
+        return {"achieved": a, "frac": a / peak, "launches": m["launches"], "find_jobs": m["jobs"],
+                "ms_per_launch": m["ms"] / max(1, m["launches"]), "ms_per_find_job": m["ms"] / max(1, m["jobs"])}
+
+    if rstage == "track_tc" and merged["ms"] > 0:
+        # the value pass's merged launches: all finds' tensor-core work over
+        # the launches' event time on the batcher's stream
+        achieved = 2.0 * merged["macs"] / (merged["ms"] / 1e3) / 1e12
+        note = (f"value pass: algorithmic correlation FLOPs (2 x MACs) of all finds over the event time of the "
+                f"merged tc_track_kernel launches ({merged['launches']} launches, {merged['jobs']} find jobs); "
+                f"peak = {pk['source']} dense bf16 sustained; fp16 operands (exact integer halves), FP32 "
+                f"accumulation in tensor memory; issued/algorithmic MACs = "
+                f"{merged['issued'] / max(1.0, merged['macs']):.2f}")
+        ms_per_launch = merged["ms"] / max(1, merged["launches"])
+    else:
+        achieved = achieved_sep
+        note = (f"algorithmic correlation FLOPs (2 x MACs) over the stage's event time; peak = {pk['source']} "
+                f"dense bf16 sustained; FP32 CUDA cores")
+        ms_per_launch = d["ms"] / max(1, d["launches"])
+    roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak if achieved else None,
             "traffic": traffic_from_profiles(kernel_names[rstage]),
             "kernel": kernel_names[rstage],
-            "stage_share": d["ms"] / sum(v["ms"] for v in stages.values()),
+            "ms_per_launch": ms_per_launch,
+            "per_find_launches": {"achieved": achieved_sep, "frac": achieved_sep / peak if achieved_sep else None,
+                                  "note": "each find launching its own tc_track_kernel, 32 finds in flight "
+                                          "(stage events on the find streams)"},
+            "merged_launches": (dict(merged_roof(alt_merged), cohorts=alt_cohorts,
+                                     note="ablation pass: the finds' launches merged, one launch per step for the "
+                                          "cohort; event time on the batcher's stream")
+                                if alt_merged and alt_merged["ms"] > 0 else None),
             "isolated": {"achieved": achieved_iso,
-                         "frac": achieved_iso / pk["tflops_sustained"] if achieved_iso else None,
+                         "frac": achieved_iso / peak if achieved_iso else None,
                          "ms_per_launch": di["ms"] / max(1, di["launches"]),
-                         "note": "same finds one at a time on one stream (untimed pass)"},
-            "note": f"algorithmic correlation FLOPs (2 x MACs) over the stage's event time; peak = {pk['source']} "
-                    f"dense bf16 sustained; " + (
-                        f"fp16 operands (exact integer halves), FP32 accumulation in tensor memory; issued/"
-                        f"algorithmic MACs = {prof['tensor_issued_macs'] / max(1.0, d['work']):.2f}"
-                        if rstage == "track_tc" else "FP32 CUDA cores")}
-    matches = [len(r[0]) for r in found]
+                         "note": "same finds one at a time on one stream, one launch per find step (untimed pass)"},
+            "note": note}
+    matches = [len(r[0]) for r in value_found]
     line = {
         "metric": METRIC, "value": value, "unit": "images/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -483,7 +537,7 @@ def main():
         "config": {"workload": WORKLOAD, "image": "2048x2048 u8", "template": "128x128", "poses": 5,
                    "angle_range_deg": [-30, 30], "num_levels": 4, "min_score": 0.7, "num_matches": 5,
                    "max_overlap": 0.5, "scenes_per_step": args.batch, "l2": "flushed (256 MiB write) between steps",
-                   "finds_in_flight": threads, "parallelism": f"replicas x{world}",
+                   "finds_in_flight": threads, "merge_cohorts": args.cohorts, "parallelism": f"replicas x{world}",
                    "path": ("tensor-core (tcgen05) tracking correlation" if args.path == "tensor"
                             else "plain FP32 CUDA-core correlation")},
         "e2e": {"value": e2e, "unit": "images/s",
@@ -492,7 +546,10 @@ def main():
                 "api": "find_ncc_models_batch (mvg_find_ncc_models_batch) on pinned host images, "
                        f"{threads} library host threads; wall clock per step, synchronized on both sides"},
         "roofline": roof,
-        "gpu_launches": int(launches_total),
+        # kernels of the value pass: every find's own launches, its tensor-core
+        # launches replaced by the merged ones
+        "gpu_launches": int(launches_total - stages.get("track_tc", {}).get("launches", 0) + merged["launches"]
+                            if merged["launches"] else launches_total),
         "clocks": clocks.summary(),
         "stages_ms_per_find": {k: round(v["ms"] / max(1, prof["finds"]), 4) for k, v in stages.items()},
         "stages_ms_per_find_isolated": {k: round(v["ms"] / max(1, iso["finds"]), 4) for k, v in iso.items()
@@ -501,14 +558,22 @@ def main():
     }
     if other is not None:
         line["compare"] = other
+    if alt_ms is not None:
+        line["merge_ablation"] = {
+            "value_pass_cohorts": args.cohorts, "value_images_per_s": value,
+            "other_cohorts": alt_cohorts,
+            "other_images_per_s": replica_value(args.steps * args.batch, world, maxed(alt_ms)),
+            "note": "cohorts 0: every find launches its own tensor-core kernels; k > 0: the finds in flight "
+                    "form k groups whose launches are merged"}
     oracle = None
     if not args.no_cpu_baseline:
         line["cpu_baseline"], oracle = cpu_baseline(wls, os.cpu_count() or 1)
-    line["pose_error"] = pose_error(found, wls, oracle)
-    # the e2e pass (batched operator, host images) returns the value pass's matches
-    line["pose_error"]["e2e_equals_value_pass"] = bool(
-        len(batch_found) == len(found) and
-        all(all(np.array_equal(a, b) for a, b in zip(x[:4], y[:4])) for x, y in zip(batch_found, found)))
+    line["pose_error"] = pose_error(value_found, wls, oracle)
+    # the other passes return the value pass's matches bit for bit
+    line["pose_error"]["e2e_equals_value_pass"] = same_results(batch_found, value_found)
+    line["pose_error"]["per_find_threads_equal_value_pass"] = same_results(found, value_found)
+    if alt_same is not None:
+        line["pose_error"]["ablation_equals_value_pass"] = alt_same
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

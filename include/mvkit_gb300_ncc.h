@@ -291,6 +291,25 @@ MVG_API int32_t mvg_profile_reset(void);
 MVG_API int32_t mvg_profile_read(int32_t stage, const char** name, double* ms, int64_t* launches, double* work,
                                  int64_t* finds);
 
+/* Batched calls (mvg_find_ncc_models_batch) made from this thread can merge
+ * the tensor-core correlation launches of their finds in flight.  The
+ * workers form `cohorts` groups (worker w in group w mod cohorts; 1..16);
+ * each tracking step and coarse scan of a find waits until every worker of
+ * its group has reached one, then a single launch per launch shape covers
+ * all of their tiles.  cohorts = 0 (default): every find launches its own,
+ * which gives the higher throughput on the 2048^2 workload: merged finds move
+ * in step and lose the overlap of their other kernels.  Results are the same
+ * either way. */
+MVG_API int32_t mvg_set_batch_merge(int32_t cohorts);
+
+/* Merged tensor-core launches of batched calls since the last reset (any
+ * thread): summed CUDA-event time of the launches on the batcher's stream
+ * (ms), their count, the finds' jobs they carried, and the algorithmic and
+ * issued multiply-adds of those finds' tensor-core work. */
+MVG_API int32_t mvg_batch_profile_reset(void);
+MVG_API int32_t mvg_batch_profile_read(double* ms, int64_t* launches, int64_t* jobs, double* macs,
+                                       double* issued);
+
 /* Multiply-adds the tensor cores were issued by the profiled finds of this
  * thread (M x N x K of every MMA, padding rows and columns included); the
  * track_tc stage's work is the algorithmic part of it. */

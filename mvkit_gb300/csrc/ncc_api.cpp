@@ -19,6 +19,7 @@
 #include <new>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include "../../include/mvkit_gb300_ncc.h"
@@ -334,6 +335,9 @@ size_t tc_launch_smem(const TcPlan& P, size_t optin) {
 // Correlation path of this thread's finds: tensor cores where applicable
 // (0) or FP32 CUDA cores only (1).
 thread_local int t_path = 0;
+// Batched calls from this thread: cohorts of workers whose finds' tensor-core
+// launches are merged (0, default: every find launches its own).
+thread_local int t_merge_tc = 0;
 
 uint16_t half_bits(double x) {
   const _Float16 h = static_cast<_Float16>(x);
@@ -688,9 +692,11 @@ struct Workspace {
   int32_t* h_error = nullptr;
   size_t smem_optin = 0;
   int sm_count = 0;
+  cudaEvent_t tc_ready = nullptr;    // this find's tensor-core inputs are complete (merged launches)
   ~Workspace() {
     if (h_tables) cudaFreeHost(h_tables);
     if (h_state) cudaFreeHost(h_state);
+    if (tc_ready) cudaEventDestroy(tc_ready);
     if (own_stream) cudaStreamDestroy(own_stream);
   }
   void init() {
@@ -699,6 +705,7 @@ struct Workspace {
     if (device == dev) return;
     device = dev;
     check(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    check(cudaEventCreateWithFlags(&tc_ready, cudaEventDisableTiming), "cudaEventCreate");
     check(cudaMallocHost(&h_state, sizeof(QueryState)), "cudaMallocHost");
     int optin = 0;
     check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "attribute");
@@ -811,6 +818,203 @@ struct Span {
   ~Span() { t_prof.close(index, stream); }
 };
 
+// ----------------------------------------------------- merged tensor-core launches
+// The tensor-core correlation launches of the finds a batched call keeps in
+// flight, merged: each find (one host thread, its own stream) submits its
+// tracking step or coarse scan as a job and waits; when every member thread
+// of the batch is waiting, the jobs are launched together, one
+// tc_track_kernel per launch shape (jobs of the same plan share it), after
+// the events of the jobs' streams, and each stream then waits for its
+// launch.  A member that will submit nothing more leaves.  A single launch
+// then covers the tiles of all finds in flight: its blocks stay busy and its
+// tail is one launch's instead of one per find.  Statistics of the merged
+// launches (CUDA events on the batcher's stream) serve the measurement.
+class TcBatcher {
+ public:
+  struct Stats {
+    double ms = 0;
+    int64_t launches = 0, jobs = 0;
+    double macs = 0, issued = 0;  // algorithmic / issued multiply-adds of the merged jobs' finds
+  };
+
+  // Tensor-core work of a completed find of the batch.
+  void add_work(double macs, double issued) {
+    std::lock_guard<std::mutex> lk(m_);
+    macs_ += macs;
+    issued_ += issued;
+  }
+
+  // Start of a batch: `members` threads on `device` (current).
+  void begin(int members, int device, int sm_count) {
+    std::lock_guard<std::mutex> lk(m_);
+    members_ = members;
+    waiting_ = 0;
+    pending_.clear();
+    sm_count_ = sm_count;
+    if (device_ != device) {
+      device_ = device;
+      check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+      jobs_.reserve(size_t(kTcMaxJobs) * kDoneSlots);
+      next_.reserve(kDoneSlots);
+      for (int i = 0; i < 2 * kDoneSlots; ++i) check(cudaEventCreateWithFlags(&done_[i], cudaEventDisableTiming), "event");
+    }
+  }
+
+  // One find's launch: returns once it is enqueued; `s` then waits for it.
+  // `ready` is recorded on `s` (the job's inputs are complete there).
+  void submit(const TcArgs& job, size_t smem, cudaStream_t s, cudaEvent_t ready) {
+    check(cudaEventRecord(ready, s), "cudaEventRecord");
+    std::unique_lock<std::mutex> lk(m_);
+    Pending p{job, smem, ready, nullptr};
+    pending_.push_back(&p);
+    const uint64_t round = round_;
+    if (++waiting_ >= members_) {
+      launch_locked();
+    } else {
+      // a member that never arrives would stall the others: after a minute
+      // the waiting jobs are launched without it
+      if (!cv_.wait_for(lk, std::chrono::seconds(60), [&] { return round_ != round; })) launch_locked();
+    }
+    if (p.error) raise(kInternal, p.error);
+    check(cudaStreamWaitEvent(s, p.done, 0), "cudaStreamWaitEvent");
+  }
+
+  // A member that submits no more jobs.
+  void leave() {
+    std::lock_guard<std::mutex> lk(m_);
+    --members_;
+    if (waiting_ > 0 && waiting_ >= members_) launch_locked();
+  }
+
+  // Event time, launches and jobs of the merged launches since begin(); waits
+  // for them.
+  Stats stats() {
+    std::lock_guard<std::mutex> lk(m_);
+    Stats st;
+    for (auto& t : timing_) {
+      float ms = 0;
+      if (cudaEventSynchronize(t.second) == cudaSuccess && cudaEventElapsedTime(&ms, t.first, t.second) == cudaSuccess)
+        st.ms += ms;
+    }
+    st.launches = launches_;
+    st.jobs = jobs_count_;
+    st.macs = macs_;
+    st.issued = issued_;
+    return st;
+  }
+  void reset_stats() {
+    std::lock_guard<std::mutex> lk(m_);
+    launches_ = jobs_count_ = 0;
+    macs_ = issued_ = 0;
+    for (auto& t : timing_) {
+      cudaEventDestroy(t.first);
+      cudaEventDestroy(t.second);
+    }
+    timing_.clear();
+  }
+
+ private:
+  static constexpr int kDoneSlots = 8;  // launches per round (distinct shapes) before slots repeat
+  struct Pending {
+    TcArgs job;
+    size_t smem;
+    cudaEvent_t ready, done;
+    const char* error = nullptr;
+  };
+
+  // Launches every pending job, grouped by launch shape (at most kTcMaxJobs
+  // a launch), and wakes the waiters.  Done events alternate between two
+  // halves by round: a round's events are re-recorded two rounds later, when
+  // every waiter of that round has passed its cudaStreamWaitEvent.
+  void launch_locked() {
+    std::vector<Pending*> todo;
+    todo.swap(pending_);
+    std::stable_sort(todo.begin(), todo.end(), [](const Pending* x, const Pending* y) {
+      return std::make_tuple(x->smem, x->job.stages, x->job.stage_bytes, x->job.abuf_bytes, x->job.sets,
+                             x->job.npad) < std::make_tuple(y->smem, y->job.stages, y->job.stage_bytes,
+                                                            y->job.abuf_bytes, y->job.sets, y->job.npad);
+    });
+    int slot = 0;
+    const int half = int(round_ & 1) * kDoneSlots;
+    for (size_t b = 0; b < todo.size();) {
+      size_t e = b + 1;
+      auto same = [&](const Pending* x) {
+        const Pending* y = todo[b];
+        return x->smem == y->smem && x->job.stages == y->job.stages && x->job.stage_bytes == y->job.stage_bytes &&
+               x->job.abuf_bytes == y->job.abuf_bytes && x->job.sets == y->job.sets && x->job.npad == y->job.npad;
+      };
+      while (e < todo.size() && e - b < size_t(kTcMaxJobs) && same(todo[e])) ++e;
+      const char* err = nullptr;
+      if (slot >= kDoneSlots) {
+        err = "tensor-core batch: too many launch shapes in one round";
+      } else {
+        std::vector<TcArgs> jobs;
+        for (size_t i = b; i < e; ++i) {
+          jobs.push_back(todo[i]->job);
+          if (cudaStreamWaitEvent(stream_, todo[i]->ready, 0) != cudaSuccess) err = "cudaStreamWaitEvent";
+        }
+        TcArgs* dev_jobs = jobs_.p + size_t(slot) * kTcMaxJobs;
+        // pageable source: staged by the driver before the call returns
+        if (!err && cudaMemcpyAsync(dev_jobs, jobs.data(), jobs.size() * sizeof(TcArgs), cudaMemcpyHostToDevice,
+                                    stream_) != cudaSuccess)
+          err = "tensor-core batch: job upload";
+        cudaEvent_t t0 = nullptr, t1 = nullptr;
+        if (!err) {
+          cudaEventCreate(&t0);
+          cudaEventCreate(&t1);
+          cudaEventRecord(t0, stream_);
+          TcLaunch l{};
+          l.jobs = dev_jobs;
+          l.njobs = int(jobs.size());
+          l.next = next_.p + slot;
+          if (launch_tc_track(l, todo[b]->smem, std::min(kTcMaxTiles, sm_count_ * kTcBlocksPerSm), stream_) !=
+              cudaSuccess)
+            err = "tensor-core batch: launch";
+          cudaEventRecord(t1, stream_);
+          timing_.emplace_back(t0, t1);
+          ++launches_;
+          jobs_count_ += int64_t(jobs.size());
+        }
+        if (!err && cudaEventRecord(done_[half + slot], stream_) != cudaSuccess) err = "cudaEventRecord";
+      }
+      for (size_t i = b; i < e; ++i) {
+        todo[i]->done = done_[half + std::min(slot, kDoneSlots - 1)];
+        todo[i]->error = err;
+      }
+      ++slot;
+      b = e;
+    }
+    waiting_ = 0;
+    ++round_;
+    cv_.notify_all();
+  }
+
+  std::mutex m_;
+  std::condition_variable cv_;
+  int members_ = 0, waiting_ = 0, device_ = -1, sm_count_ = 1;
+  uint64_t round_ = 0;
+  std::vector<Pending*> pending_;
+  cudaStream_t stream_ = nullptr;
+  DevBuf<TcArgs> jobs_;
+  DevBuf<int> next_;
+  cudaEvent_t done_[2 * kDoneSlots] = {};
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> timing_;
+  int64_t launches_ = 0, jobs_count_ = 0;
+  double macs_ = 0, issued_ = 0;
+};
+
+// Cohorts of a batch's workers: worker w merges with the workers of cohort
+// w mod cohorts only, so cohorts drift out of phase and one cohort's
+// merged launch overlaps other cohorts' other kernels.
+constexpr int kMaxCohorts = 16;
+TcBatcher& tc_batcher(int cohort) {
+  static TcBatcher* b = new TcBatcher[kMaxCohorts];  // live with the find pool's threads
+  return b[cohort];
+}
+
+// The batcher of this thread's finds (worker threads of a batched call), or none.
+thread_local TcBatcher* t_batcher = nullptr;
+
 struct Match {
   double row, col, angle, score;
 };
@@ -878,6 +1082,21 @@ DomainHost scan_domain(const uint8_t* mask, int64_t W, int64_t H) {
 [[noreturn]] void raise_device_error(int32_t status) {
   raise(status, status == kInternal ? "tensor-core correlation: a pipeline wait ran out (device error flag)"
                                     : "pyramid sums exceed the exact float range");
+}
+
+// A find's tensor-core launch: merged with the other finds of a batched
+// call (TcBatcher), or on its own stream.
+void tc_launch(Workspace& ws, const TcArgs& job, size_t smem, cudaStream_t s) {
+  if (t_batcher) {
+    t_batcher->submit(job, smem, s, ws.tc_ready);
+    return;
+  }
+  TcLaunch l{};
+  l.jobs = nullptr;
+  l.njobs = 1;
+  l.next = &ws.tc_tiles.p->next;
+  l.single = job;
+  check(launch_tc_track(l, smem, std::min(kTcMaxTiles, ws.sm_count * kTcBlocksPerSm), s), "tc track");
 }
 
 // One model's query prepared for a multi-model selection
@@ -1338,9 +1557,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     }
     {
       Span spt(kStTrackTc, s);
-      check(launch_tc_track(tca, tc_launch_smem(P, ws.smem_optin), std::min(kTcMaxTiles, ws.sm_count * kTcBlocksPerSm),
-                            s),
-            "tc coarse");
+      tc_launch(ws, tca, tc_launch_smem(P, ws.smem_optin), s);
     }
     CoarseTcArgs cs;
     cs.lev = lev[top];
@@ -1419,6 +1636,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   }
   if (stage == 0) {
     fetch_stage(ws, s, ws.cand_a.p, 0, out);
+    if (ws.h_state->error) raise_device_error(ws.h_state->error);
     if (ws.h_state->overflow) raise(kLimitExceeded, "coarse candidate budget exceeded");
     return out;
   }
@@ -1499,9 +1717,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
         }
         {
           Span spt(kStTrackTc, s);
-          check(launch_tc_track(tca, tc_launch_smem(P, ws.smem_optin),
-                                std::min(kTcMaxTiles, ws.sm_count * kTcBlocksPerSm), s),
-                "tc track");
+          tc_launch(ws, tca, tc_launch_smem(P, ws.smem_optin), s);
         }
         ta.tc_dots = ws.tc_dots.p;
         ta.tc_group_of_src = d_tc_gsrc[t];
@@ -1644,8 +1860,8 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     // tables to buffers of the prepared query (the workspace's are reused)
     check(cudaMemcpyAsync(ws.h_state, st, sizeof(QueryState), cudaMemcpyDeviceToHost, s), "state");
     check(cudaStreamSynchronize(s), "sync");
-    if (ws.h_state->overflow) raise(kLimitExceeded, "coarse candidate budget exceeded");
     if (ws.h_state->error) raise_device_error(ws.h_state->error);
+    if (ws.h_state->overflow) raise(kLimitExceeded, "coarse candidate budget exceeded");
     const int n = std::max(0, std::min(ws.h_state->sorted_count, kMaxCandidates));
     prep->cands.resize(size_t(n));
     if (n > 0)
@@ -1712,8 +1928,11 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   t_prof.work[kStTrackTc] += double(hs.tc_macs);
   t_prof.issued_tc += double(hs.tc_issued);
   t_prof.work[kStScore] += double(hs.count[slot]) * double(orig.n);
-  if (hs.overflow) raise(kLimitExceeded, "coarse candidate budget exceeded");
+  if (t_batcher) t_batcher->add_work(double(hs.tc_macs), double(hs.tc_issued));
+  // the device error flag first: after a failed kernel the later stages
+  // read incomplete data (an overflow then is a consequence)
   if (hs.error) raise_device_error(hs.error);
+  if (hs.overflow) raise(kLimitExceeded, "coarse candidate budget exceeded");
   std::vector<Cand> acc(size_t(hs.accepted));
   if (hs.accepted > 0) {
     check(cudaMemcpyAsync(acc.data(), ws.accepted.p, acc.size() * sizeof(Cand), cudaMemcpyDeviceToHost, s), "result");
@@ -2501,9 +2720,30 @@ int32_t mvg_find_ncc_models_batch(const void* const* images, const int32_t* pixe
     const int path = t_path;
     std::vector<BatchImage> done(static_cast<size_t>(num_images));
     std::atomic<int64_t> next{0};
-    auto job = [&](int) {
+    const int nworkers = int(std::min<int64_t>(workers, num_images));
+    // the workers' tensor-core launches are merged (one launch per step for
+    // all finds in flight) unless the calling thread asked for separate ones
+    const int cohorts = path == 0 ? std::min(t_merge_tc, nworkers) : 0;
+    // batched calls run one after the other (the pool and the batchers serve one)
+    static std::mutex one_call;
+    std::lock_guard<std::mutex> serial(one_call);
+    if (cohorts > 0) {
+      int sms = 0;
+      check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "attribute");
+      for (int c = 0; c < cohorts; ++c) tc_batcher(c).begin(nworkers / cohorts + (c < nworkers % cohorts), device, sms);
+    }
+    auto job = [&](int w) {
+      TcBatcher* batcher = cohorts > 0 ? &tc_batcher(w % cohorts) : nullptr;
+      struct Member {
+        TcBatcher* b;
+        ~Member() {
+          t_batcher = nullptr;
+          if (b) b->leave();
+        }
+      } member{batcher};
       if (cudaSetDevice(device) != cudaSuccess) return;
       t_path = path;
+      t_batcher = batcher;
       for (int64_t i; (i = next.fetch_add(1)) < num_images;) {
         BatchImage& b = done[size_t(i)];
         b.status = guarded([&] {
@@ -2532,7 +2772,7 @@ int32_t mvg_find_ncc_models_batch(const void* const* images, const int32_t* pixe
         if (b.status != kOk) b.message = g_last_error;
       }
     };
-    find_pool().run(int(std::min<int64_t>(workers, num_images)), job);
+    find_pool().run(nworkers, job);
     if (next.load() < num_images) raise(kInternal, "batch worker could not select the device");
     int64_t at = 0;
     for (int64_t i = 0; i < num_images; ++i) {
@@ -2789,6 +3029,40 @@ int32_t mvg_profile_read(int32_t stage, const char** name, double* ms, int64_t* 
     if (launches) *launches = t_prof.launches[stage];
     if (work) *work = t_prof.work[stage];
     if (finds) *finds = t_prof.finds;
+  });
+}
+
+int32_t mvg_set_batch_merge(int32_t cohorts) {
+  if (cohorts < 0 || cohorts > kMaxCohorts) {
+    g_last_error = "cohorts must be 0..16";
+    return kInvalidArgument;
+  }
+  t_merge_tc = cohorts;
+  return kOk;
+}
+
+int32_t mvg_batch_profile_reset(void) {
+  return guarded([&] {
+    for (int c = 0; c < kMaxCohorts; ++c) tc_batcher(c).reset_stats();
+  });
+}
+
+int32_t mvg_batch_profile_read(double* ms, int64_t* launches, int64_t* jobs, double* macs, double* issued) {
+  return guarded([&] {
+    TcBatcher::Stats sum;
+    for (int c = 0; c < kMaxCohorts; ++c) {
+      const TcBatcher::Stats st = tc_batcher(c).stats();
+      sum.ms += st.ms;
+      sum.launches += st.launches;
+      sum.jobs += st.jobs;
+      sum.macs += st.macs;
+      sum.issued += st.issued;
+    }
+    if (ms) *ms = sum.ms;
+    if (launches) *launches = sum.launches;
+    if (jobs) *jobs = sum.jobs;
+    if (macs) *macs = sum.macs;
+    if (issued) *issued = sum.issued;
   });
 }
 

@@ -165,7 +165,7 @@ struct TcGroup {
 
 struct TcTiles {
   int count;
-  int next;                              // tiles handed out after the first gridDim.x (reset with count)
+  int next;                              // unused (tiles are handed out per launch, TcLaunch::next)
   int group[kTcMaxTiles], first[kTcMaxTiles], last[kTcMaxTiles];
 };
 
@@ -194,6 +194,18 @@ struct TcArgs {
   int withhold_weights;                  // test hook: load no weights (waits run out, error flag set)
 };
 
+// One tensor-core launch: the tiles of `njobs` jobs (a job is one find's
+// tracking step or coarse scan, TcArgs in device memory), handed out in job
+// order from one counter.  Every job of a launch has the same launch shape
+// (stages, stage_bytes, abuf_bytes, sets, npad, dynamic shared memory).
+constexpr int kTcMaxJobs = 64;
+struct TcLaunch {
+  const TcArgs* jobs;  // nullptr: the one job `single`
+  int njobs;
+  int* next;           // tiles handed out after the first gridDim.x; zeroed by launch_tc_track
+  TcArgs single;
+};
+
 // fp16 planes of a level for the tensor-core tracking: parts x 8 shifted
 // copies (plane d holds level column x - kTcPlaneMargin + d at x), `pitch`
 // elements per row (a multiple of 8, at least the level width + 8).
@@ -203,7 +215,7 @@ size_t tc_kernel_static_smem();
 // Groups the step's candidates into tiles (counts, tile list, order).
 cudaError_t launch_tc_group(const TcArgs& a, int ngroups, int32_t* counts, int32_t* offsets, int32_t* cursor,
                             int max_candidates, cudaStream_t s);
-cudaError_t launch_tc_track(const TcArgs& a, size_t smem, int grid, cudaStream_t s);
+cudaError_t launch_tc_track(const TcLaunch& l, size_t smem, int grid, cudaStream_t s);
 
 // Pseudo-candidates in source order, their lattice centres, the identity
 // order and the tile list (16 consecutive candidates of one source per tile).

@@ -143,6 +143,9 @@ __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a,
 struct __align__(16) TcShared {
   uint64_t a_full[2], slab_done[2], drain;
   uint64_t b_full[kTcMaxStages], b_empty[kTcMaxStages];
+  TcArgs job;              // the current tile's job
+  int job_base[kTcMaxJobs + 1];  // first launch tile of each job
+  int job_of;              // index of `job` (-1: none loaded)
   TcGroup grp;
   uint32_t tmem;
   int fail, cnt;
@@ -310,22 +313,38 @@ __device__ void tc_weight_role(const TcArgs& a, TcShared& sh, uint8_t* wbase, Ri
   }
 }
 
-// Persistent and warp-specialised: block b takes tile b first, then the
-// next unclaimed tile from a global counter (tiles differ in cost, so a
-// static stride leaves blocks idle at the end);
-// per tile warp 0 issues the MMAs, warp 1 streams weights, warps 2-5 stage
-// windows, and all six warps run the set-up and the epilogue.  Shared
-// memory: weight ring (stages x stage_bytes) | two window buffers.
+// Persistent and warp-specialised: the launch's tiles are those of its jobs
+// in job order; block b takes tile b first, then the next unclaimed tile
+// from a global counter (tiles differ in cost, so a static stride leaves
+// blocks idle at the end); per tile warp 0 issues the MMAs, warp 1 streams
+// weights, warps 2-5 stage windows, and all six warps run the set-up and the
+// epilogue.  Shared memory: weight ring (stages x stage_bytes) | two window
+// buffers, the same for every job of the launch.
 __global__ void __launch_bounds__(kTcThreads, 1)
-    tc_track_kernel(const __grid_constant__ TcArgs a) {
+    tc_track_kernel(const __grid_constant__ TcLaunch L) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ TcShared sh;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  const int ntiles = a.tiles->count;
+  const TcArgs* jobs = L.jobs ? L.jobs : &L.single;
+  // first launch tile of each job (the jobs' tile lists were planned on the device)
+  if (t == 0) {
+    int n = 0;
+    for (int j = 0; j < L.njobs; ++j) {
+      sh.job_base[j] = n;
+      n += jobs[j].tiles->count;
+    }
+    sh.job_base[L.njobs] = n;
+    sh.job_of = -1;
+  }
+  __syncthreads();
+  const int ntiles = sh.job_base[L.njobs];
   if (int(blockIdx.x) >= ntiles) return;
+  const TcArgs& a = sh.job;
+  // launch shape: equal for every job
+  const int stages = jobs[0].stages, stage_bytes = jobs[0].stage_bytes;
   uint8_t* smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
   uint8_t* wbase = smem;
-  uint8_t* abase = smem + size_t(a.stages) * a.stage_bytes;
+  uint8_t* abase = smem + size_t(stages) * stage_bytes;
   if (t == 0) {
     bar_init(&sh.a_full[0], kTcWindowThreads);
     bar_init(&sh.a_full[1], kTcWindowThreads);
@@ -352,7 +371,19 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const uint32_t tmem = sh.tmem;
   RingPos cm, cb;            // role-local ring positions (MMA thread, weight producer)
   int sm = 0, sa = 0;        // role-local counters (MMA thread, window producer)
-  for (int tile = blockIdx.x; tile < ntiles; tile = sh.next_tile) {
+  for (int gtile = blockIdx.x; gtile < ntiles; gtile = sh.next_tile) {
+    // the tile's job into shared memory (when it changes)
+    int jb = 0;
+    while (gtile >= sh.job_base[jb + 1]) ++jb;
+    if (jb != sh.job_of) {
+      __syncthreads();
+      const uint32_t* src = reinterpret_cast<const uint32_t*>(jobs + jb);
+      uint32_t* dst = reinterpret_cast<uint32_t*>(&sh.job);
+      for (int w = t; w < int(sizeof(TcArgs) / 4); w += kTcThreads) dst[w] = src[w];
+      __syncthreads();
+      if (t == 0) sh.job_of = jb;
+    }
+    const int tile = gtile - sh.job_base[jb];
     // tile set-up: the group into shared memory, one candidate per thread
     {
       const int gi = a.tiles->group[tile];
@@ -497,7 +528,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     // generic accesses of the buffers before the next tile's async writes
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    if (t == 0) sh.next_tile = int(gridDim.x) + atomicAdd(&a.tiles->next, 1);
+    if (t == 0) sh.next_tile = int(gridDim.x) + atomicAdd(L.next, 1);
     __syncthreads();
   }
   __syncthreads();
@@ -618,9 +649,11 @@ cudaError_t launch_tc_group(const TcArgs& a, int ngroups, int32_t* counts, int32
   return cudaGetLastError();
 }
 
-cudaError_t launch_tc_track(const TcArgs& a, size_t smem, int grid, cudaStream_t s) {
+cudaError_t launch_tc_track(const TcLaunch& l, size_t smem, int grid, cudaStream_t s) {
+  if (l.njobs < 1 || l.njobs > kTcMaxJobs) return cudaErrorInvalidValue;
   if (cudaError_t e = reserve_dynamic_smem(reinterpret_cast<const void*>(tc_track_kernel), smem)) return e;
-  tc_track_kernel<<<grid, kTcThreads, smem, s>>>(a);
+  if (cudaError_t e = cudaMemsetAsync(l.next, 0, sizeof(int), s)) return e;
+  tc_track_kernel<<<grid, kTcThreads, smem, s>>>(l);
   return cudaGetLastError();
 }
 

@@ -714,6 +714,33 @@ def set_correlation_path(path: str) -> None:
     _check(lib.mvg_set_correlation_path(0 if path == "tensor" else 1), "set_correlation_path")
 
 
+def set_batch_merge(cohorts: int = 0) -> None:
+    """Batched calls from this thread merge their finds' tensor-core launches
+    within `cohorts` groups of workers; 0 (the library's default) launches
+    them per find."""
+    lib = load()
+    lib.mvg_set_batch_merge.argtypes = [C.c_int32]
+    lib.mvg_set_batch_merge.restype = C.c_int32
+    _check(lib.mvg_set_batch_merge(int(cohorts)), "set_batch_merge")
+
+
+def batch_profile_reset() -> None:
+    _check(load().mvg_batch_profile_reset(), "batch_profile")
+
+
+def batch_profile_read() -> dict:
+    """Merged tensor-core launches of batched calls since the last reset:
+    {ms, launches, jobs, macs, issued} (event time on the batcher's stream)."""
+    lib = load()
+    ms, macs, issued = C.c_double(), C.c_double(), C.c_double()
+    launches, jobs = C.c_int64(), C.c_int64()
+    lib.mvg_batch_profile_read.argtypes = [_dp, _i64p, _i64p, _dp, _dp]
+    _check(lib.mvg_batch_profile_read(C.byref(ms), C.byref(launches), C.byref(jobs), C.byref(macs),
+                                      C.byref(issued)), "batch_profile")
+    return {"ms": ms.value, "launches": launches.value, "jobs": jobs.value, "macs": macs.value,
+            "issued": issued.value}
+
+
 def profile_enable(on: bool = True) -> None:
     """Per-thread stage timing of finds (CUDA events on the find's stream)."""
     _check(load().mvg_profile_enable(1 if on else 0), "profile")

@@ -139,3 +139,70 @@ def test_batch_empty_image(mg):
         assert len(s[0]) > 0
         for x, y in zip(g, s):
             np.testing.assert_array_equal(x, y)
+
+
+def test_merged_tensor_core_launches_equal_per_find_launches(mg):
+    """A batch merges its finds' tensor-core launches (fewer launches than
+    find jobs); every image's matches equal those of the same batch with one
+    launch per find, bit for bit."""
+    case = BATCH_CASES["batch_uneven"]
+    batch = make_batch_inputs(case)
+    models = batch_models(mg, case, batch)
+    ctl = controls(case)
+    images = [wl.image for wl in batch]
+    mg.set_batch_merge(1)  # all four workers in one cohort
+    try:
+        mg.batch_profile_reset()
+        merged = mg.find_ncc_models_batch(images, models, *ctl, workers=4)
+        st = mg.batch_profile_read()
+        assert st["jobs"] > st["launches"] > 0, st
+        mg.set_batch_merge(0)
+        mg.batch_profile_reset()
+        separate = mg.find_ncc_models_batch(images, models, *ctl, workers=4)
+        assert mg.batch_profile_read()["launches"] == 0
+        mg.set_batch_merge(2)  # two cohorts of two
+        cohorts = mg.find_ncc_models_batch(images, models, *ctl, workers=4)
+    finally:
+        mg.set_batch_merge(0)
+    for i, (a, b, c) in enumerate(zip(merged, separate, cohorts)):
+        assert len(a[0]) > 0, f"image {i}"
+        for x, y, z in zip(a, b, c):
+            np.testing.assert_array_equal(x, y)
+            np.testing.assert_array_equal(x, z)
+
+
+def test_merged_batch_of_2048_scenes(mg):
+    """Eight 2048^2 scenes sharing one 128^2 template (5 poses each, +-30
+    degrees: the throughput workload) in one batch with merged tensor-core
+    launches: every image's matches equal find_ncc_model's on it, bit for
+    bit, and, for two of them, the FP64 oracle's (count, order, 0.05 px,
+    0.05 deg, 1e-4)."""
+    import math
+    from concurrent.futures import ThreadPoolExecutor
+
+    import oracle_lib
+    from mvkit_gb300 import workloads as W
+    D = math.radians
+    gen = dict(height=2048, width=2048, tsize=128, n_poses=5, angle_range=(-D(30), D(30)))
+    wls = [W.make_workload(2000 + i, template_seed=1, **gen) for i in range(8)]
+    model = mg.create_ncc_model(wls[0].template, 4, -D(30), D(60), "auto", "use_polarity")
+    ctl = (-D(30), D(60), 0.7, 5, 0.5, "true", 4)
+    mg.set_batch_merge(2)
+    try:
+        mg.batch_profile_reset()
+        got = mg.find_ncc_models_batch([w.image for w in wls], [model], *ctl, workers=8)
+        st = mg.batch_profile_read()
+    finally:
+        mg.set_batch_merge(0)
+    assert st["jobs"] > st["launches"] > 0 and st["macs"] > 0, st
+    for i, w in enumerate(wls):
+        one = mg.find_ncc_model(w.image, model, *ctl)
+        assert len(one[0]) == 5, f"scene {i}"
+        for x, y in zip(got[i][:4], one):
+            np.testing.assert_array_equal(x, y)
+    orc = oracle_lib.oracle()
+    om = orc.create(wls[0].template, levels=4, angle_start=-D(30), angle_extent=D(60))
+    with ThreadPoolExecutor(2) as ex:
+        want = list(ex.map(lambda w: orc.find(om, w.image, -D(30), D(60), 0.7, 5, 0.5, True, 4, 1), wls[:2]))
+    for i in range(2):
+        assert_same_matches(got[i][:4], want[i], f"scene {i} vs oracle")
