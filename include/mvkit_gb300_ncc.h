@@ -93,6 +93,22 @@ MVG_API int32_t mvg_deserialize_ncc_model(const char* bytes, int64_t size, mvg_n
  * on the host. */
 MVG_API int32_t mvg_set_model_build(int32_t where);
 
+/* Extended mode: budgets of the calling thread's model builds and finds
+ * (batched calls pass them to their workers).  The defaults (0) are the
+ * reference's, and a model or search beyond one fails with
+ * MV_STATUS_LIMIT_EXCEEDED as the reference's does: samples = rotated-raster
+ * samples of a model, 16 000 000 (src/ncc_matching/model.cpp:15,237);
+ * pixels = pixels of a search image, 32 000 000 (matcher.cpp:373-374);
+ * candidates = coarse candidates of a find, 10 000 (model.hpp:21,
+ * matcher.cpp:591).  Raising them lets templates of 160^2 and more over a
+ * full circle, images such as 8192 x 8192, and searches with more coarse
+ * candidates run where the reference refuses them; searches within the
+ * default budgets give the same results either way.  Limits: samples <=
+ * 2^31 - 1, pixels <= 2^30, candidates <= 262144.  A model keeps the sample
+ * budget it was built with. */
+MVG_API int32_t mvg_set_budgets(int64_t samples, int64_t pixels, int32_t candidates);
+MVG_API int32_t mvg_get_budgets(int64_t* samples, int64_t* pixels, int32_t* candidates);
+
 /* Test hook for the bounded waits of the tensor-core kernel (calling
  * thread's finds): on = 1 makes the kernel load no weights, so the MMA
  * thread's mbarrier wait runs out after one second, the kernel sets the

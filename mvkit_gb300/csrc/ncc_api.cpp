@@ -748,6 +748,21 @@ Workspace& workspace() {
   return *t_workspace;
 }
 
+// Zeroes the query state on the device and sets its candidate budget, from
+// the pinned host copy (no readback of the state is in flight between finds).
+void init_state(Workspace& ws, cudaStream_t s, int cap) {
+  *ws.h_state = QueryState{};
+  ws.h_state->cap = cap;
+  check(cudaMemcpyAsync(ws.state.p, ws.h_state, sizeof(QueryState), cudaMemcpyHostToDevice, s), "state");
+}
+
+// Power of two >= 3 x the candidate budget (the dedup table of a find).
+int hash_slots(int cap) {
+  int n = kHashSlots;
+  while (n < 3 * cap) n *= 2;
+  return n;
+}
+
 // Per-thread stage profile: CUDA events on the find's stream around each
 // kernel group (only while enabled), launch counts and algorithmic work.
 enum Stage { kStUpload, kStPyramid, kStPrefix, kStCoarse, kStNms, kStTrack, kStDedup, kStScore, kStSort, kStSelect,
@@ -1031,7 +1046,7 @@ void fetch_stage(Workspace& ws, cudaStream_t s, const Cand* src, int slot, FindO
   t_prof.used = 0;
   check(cudaMemcpyAsync(ws.h_state, ws.state.p, sizeof(QueryState), cudaMemcpyDeviceToHost, s), "state");
   check(cudaStreamSynchronize(s), "sync");
-  const int n = slot < 0 ? ws.h_state->sorted_count : std::min(ws.h_state->count[slot], kMaxCandidates);
+  const int n = slot < 0 ? ws.h_state->sorted_count : std::min(ws.h_state->count[slot], ws.h_state->cap);
   std::vector<Cand> h(size_t(std::max(n, 0)));
   if (n > 0) check(cudaMemcpyAsync(h.data(), src, size_t(n) * sizeof(Cand), cudaMemcpyDeviceToHost, s), "stage");
   check(cudaStreamSynchronize(s), "sync");
@@ -1145,7 +1160,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   opt.angle_start = cs;
   opt.angle_extent = std::max(0., ce - cs);
   if (W <= 0 || H <= 0 || W > std::numeric_limits<int>::max() || H > std::numeric_limits<int>::max() ||
-      H > 32000000 / W)
+      H > thread_budgets().pixels / W)
     raise(kLimitExceeded, "search image exceeds pixel budget");
   const int64_t bpp = type == 1 ? 2 : 1;
   if (stride < W * bpp || stride % bpp) raise(kInvalidArgument, "invalid row stride");
@@ -1175,6 +1190,17 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
 
   Workspace& ws = workspace();
   cudaStream_t s = user_stream ? user_stream : ws.own_stream;
+  // candidate budget and the list buffers it sizes
+  const int cap = thread_budgets().candidates;
+  const int slots = hash_slots(cap);
+  for (DevBuf<Cand>* b : {&ws.cand_a, &ws.cand_b, &ws.tmp, &ws.sorted, &ws.accepted}) b->reserve(size_t(cap));
+  ws.aux.reserve(size_t(cap));
+  ws.accepted_aux.reserve(size_t(cap));
+  ws.tested.reserve(size_t(cap));
+  ws.sup.reserve(size_t(cap));
+  ws.refined.reserve(size_t(cap));
+  ws.refined_flag.reserve(size_t(cap));
+  ws.table.reserve(size_t(slots));
   // Planning reads (and may extend) the model's endpoint rasters: serialise
   // it per model and snapshot the device views used by this find.
   std::unique_lock<std::mutex> lock(m.mutex);
@@ -1441,7 +1467,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     }
     check(cudaMemcpyAsync(ws.tables.p, h, total, cudaMemcpyHostToDevice, s), "tables");
   }
-  check(cudaMemsetAsync(ws.state.p, 0, sizeof(QueryState), s), "memset");
+  init_state(ws, s, cap);
 
   // search domain on the device (reduced domains only)
   DomainView dv{};
@@ -1521,7 +1547,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     ws.coarse_rc.reserve(size_t(ncand));
     ws.coarse_dots.reserve(size_t(ncand) * kTcScoreStride);
     ws.tc_planes.reserve(size_t(P.parts) * kTcPlaneShifts * size_t(lh[top]) * size_t(pitch));
-    ws.tc_order.reserve(std::max(size_t(ncand), size_t(kMaxCandidates)));
+    ws.tc_order.reserve(std::max(size_t(ncand), size_t(cap)));
     ws.tc_tiles.reserve(1);
     TcArgs tca{};
     tca.lev = lev[top];
@@ -1630,7 +1656,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     }
     na.out = ws.cand_a.p;
     na.state = st;
-    na.max_candidates = kMaxCandidates;
+    na.max_candidates = cap;
     Span sp(kStNms, s);
     check(launch_nms(na, s), "nms");
   }
@@ -1675,9 +1701,9 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
         const TcPlan& P = *tc[t];
         const int ng = int(P.groups.size());
         const int pitch = (lev[t].w + kTcPlaneMargin + 7) & ~7;
-        ws.tc_dots.reserve(size_t(kMaxCandidates) * kTcScoreStride);
+        ws.tc_dots.reserve(size_t(cap) * kTcScoreStride);
         ws.tc_planes.reserve(size_t(P.parts) * kTcPlaneShifts * size_t(lev[t].h) * size_t(pitch));
-        ws.tc_order.reserve(kMaxCandidates);
+        ws.tc_order.reserve(size_t(cap));
         ws.tc_counts.reserve(size_t(ng));
         ws.tc_offsets.reserve(size_t(ng));
         ws.tc_cursor.reserve(size_t(ng));
@@ -1712,7 +1738,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
         {
           Span spp(kStTcPrep, s, 4);
           check(launch_tc_planes(lev[t], ws.tc_planes.p, pitch, P.parts, P.offset, s), "tc planes");
-          check(launch_tc_group(tca, ng, ws.tc_counts.p, ws.tc_offsets.p, ws.tc_cursor.p, kMaxCandidates, s),
+          check(launch_tc_group(tca, ng, ws.tc_counts.p, ws.tc_offsets.p, ws.tc_cursor.p, cap, s),
                 "tc group");
         }
         {
@@ -1724,9 +1750,9 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
         ta.tc_groups = d_tc_groups[t];
       }
       Span sp(kStTrack, s);
-      check(launch_track(ta, kMaxCandidates, s, ws.smem_optin), "track");
+      check(launch_track(ta, cap, s, ws.smem_optin), "track");
     }
-    check(cudaMemsetAsync(ws.table.p, 0xff, sizeof(int) * kHashSlots, s), "memset");
+    check(cudaMemsetAsync(ws.table.p, 0xff, sizeof(int) * size_t(slots), s), "memset");
     DedupArgs da;
     da.in = snap ? cur : ws.tmp.p;
     da.out = nxt;
@@ -1739,9 +1765,10 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     da.height = Hd;
     da.width = Wd;
     da.dom = dv;
+    da.hash_slots = slots;
     {
       Span sp(kStDedup, s, snap ? 2 : 1);
-      check(launch_dedup(da, kMaxCandidates, s), "dedup");
+      check(launch_dedup(da, cap, s), "dedup");
     }
     std::swap(cur, nxt);
     ++slot;
@@ -1781,7 +1808,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     sa.absolute = hm.params.ignore_polarity;
     {
       Span sp(kStScore, s);
-      check(launch_score(sa, kMaxCandidates, s), "score");
+      check(launch_score(sa, cap, s), "score");
     }
     SortArgs so;
     so.in = cur;
@@ -1789,7 +1816,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     so.state = st;
     so.slot = slot;
     Span sp(kStSort, s);
-    check(launch_sort(so, s), "sort");
+    check(launch_sort(so, cap, s), "sort");
   }
   if (stage == 100) {
     fetch_stage(ws, s, ws.sorted.p, -1, out);
@@ -1797,9 +1824,9 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   }
 
   // greedy selection with refinement (matcher.cpp:1063-1076)
-  check(cudaMemsetAsync(ws.refined_flag.p, 0, sizeof(int32_t) * kMaxCandidates, s), "memset");
-  check(cudaMemsetAsync(ws.tested.p, 0, sizeof(int32_t) * kMaxCandidates, s), "memset");
-  check(cudaMemsetAsync(ws.sup.p, 0, kMaxCandidates, s), "memset");
+  check(cudaMemsetAsync(ws.refined_flag.p, 0, sizeof(int32_t) * size_t(cap), s), "memset");
+  check(cudaMemsetAsync(ws.tested.p, 0, sizeof(int32_t) * size_t(cap), s), "memset");
+  check(cudaMemsetAsync(ws.sup.p, 0, size_t(cap), s), "memset");
   // speculative refinement batch: the next NumMatches unsuppressed,
   // mutually non-overlapping candidates (32 when all matches are wanted)
   const int batch_limit = int(std::min<int64_t>(64, opt.num_matches > 0 ? opt.num_matches : 32));
@@ -1862,7 +1889,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     check(cudaStreamSynchronize(s), "sync");
     if (ws.h_state->error) raise_device_error(ws.h_state->error);
     if (ws.h_state->overflow) raise(kLimitExceeded, "coarse candidate budget exceeded");
-    const int n = std::max(0, std::min(ws.h_state->sorted_count, kMaxCandidates));
+    const int n = std::max(0, std::min(ws.h_state->sorted_count, cap));
     prep->cands.resize(size_t(n));
     if (n > 0)
       check(cudaMemcpyAsync(prep->cands.data(), ws.sorted.p, size_t(n) * sizeof(Cand), cudaMemcpyDeviceToHost, s),
@@ -1905,7 +1932,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
   }
   {
     Span sp(kStSelect, s, 2);
-    check(launch_rects(ws.sorted.p, ws.aux.p, st, geom, kMaxCandidates, s), "rects");
+    check(launch_rects(ws.sorted.p, ws.aux.p, st, geom, cap, s), "rects");
     check(launch_select(se, s), "select");
   }
   for (int round = 0; round < 100000; ++round) {
@@ -2200,7 +2227,7 @@ std::vector<MultiCand> run_find_models(const std::vector<mvg_ncc_model_s*>& mode
   if (!pixels) raise(kInvalidArgument, "image pixels must not be null");
   const int64_t bpp = type == 1 ? 2 : 1;
   if (W <= 0 || H <= 0 || W > std::numeric_limits<int>::max() || H > std::numeric_limits<int>::max() ||
-      H > 32000000 / W)
+      H > thread_budgets().pixels / W)
     raise(kLimitExceeded, "search image exceeds pixel budget");
   if (stride < W * bpp || stride % bpp) raise(kInvalidArgument, "invalid row stride");
   // one upload of a host image for all models
@@ -2718,6 +2745,7 @@ int32_t mvg_find_ncc_models_batch(const void* const* images, const int32_t* pixe
     int device = 0;
     check(cudaGetDevice(&device), "batch");
     const int path = t_path;
+    const Budgets budgets = thread_budgets();
     std::vector<BatchImage> done(static_cast<size_t>(num_images));
     std::atomic<int64_t> next{0};
     const int nworkers = int(std::min<int64_t>(workers, num_images));
@@ -2743,6 +2771,7 @@ int32_t mvg_find_ncc_models_batch(const void* const* images, const int32_t* pixe
       } member{batcher};
       if (cudaSetDevice(device) != cudaSuccess) return;
       t_path = path;
+      thread_budgets() = budgets;
       t_batcher = batcher;
       for (int64_t i; (i = next.fetch_add(1)) < num_images;) {
         BatchImage& b = done[size_t(i)];
@@ -2814,7 +2843,7 @@ int32_t mvg_ncc_score_gradient(const void* pixels, int32_t pixel_type, int64_t w
     if (count < 0 || (count > 0 && (!poses || !score || !gradient)))
       raise(kInvalidArgument, "poses, score and gradient arrays required");
     if (width <= 0 || height <= 0 || width > std::numeric_limits<int>::max() ||
-        height > std::numeric_limits<int>::max() || height > 32000000 / width)
+        height > std::numeric_limits<int>::max() || height > thread_budgets().pixels / width)
       raise(kLimitExceeded, "search image exceeds pixel budget");
     const int64_t bpp = pixel_type == 1 ? 2 : 1;
     if (row_stride < width * bpp || row_stride % bpp) raise(kInvalidArgument, "invalid row stride");
@@ -2836,7 +2865,7 @@ int32_t mvg_ncc_score_gradient(const void* pixels, int32_t pixel_type, int64_t w
       check(cudaMemcpyAsync(ws.image.p, pixels, bytes, cudaMemcpyHostToDevice, s), "image upload");
       dev = ws.image.p;
     }
-    check(cudaMemsetAsync(ws.state.p, 0, sizeof(QueryState), s), "memset");
+    init_state(ws, s, kMaxCandidates);
     LevelImage lev0{};
     ws.lev_v[0].reserve(size_t(width) * size_t(height));
     lev0.v = ws.lev_v[0].p;
@@ -2873,7 +2902,7 @@ int32_t mvg_ncc_refine_similarity(const void* pixels, int32_t pixel_type, int64_
     if (count < 0 || (count > 0 && (!poses || !score))) raise(kInvalidArgument, "poses and score arrays required");
     if (iterations < 0 || iterations > 100) raise(kInvalidArgument, "iterations must be in [0, 100]");
     if (width <= 0 || height <= 0 || width > std::numeric_limits<int>::max() ||
-        height > std::numeric_limits<int>::max() || height > 32000000 / width)
+        height > std::numeric_limits<int>::max() || height > thread_budgets().pixels / width)
       raise(kLimitExceeded, "search image exceeds pixel budget");
     const int64_t bpp = pixel_type == 1 ? 2 : 1;
     if (row_stride < width * bpp || row_stride % bpp) raise(kInvalidArgument, "invalid row stride");
@@ -2895,7 +2924,7 @@ int32_t mvg_ncc_refine_similarity(const void* pixels, int32_t pixel_type, int64_
       check(cudaMemcpyAsync(ws.image.p, pixels, bytes, cudaMemcpyHostToDevice, s), "image upload");
       dev = ws.image.p;
     }
-    check(cudaMemsetAsync(ws.state.p, 0, sizeof(QueryState), s), "memset");
+    init_state(ws, s, kMaxCandidates);
     LevelImage lev0{};
     ws.lev_v[0].reserve(size_t(width) * size_t(height));
     lev0.v = ws.lev_v[0].p;
@@ -2972,7 +3001,7 @@ int32_t mvg_ncc_pyramid_level(const void* pixels, int32_t pixel_type, int64_t wi
     const size_t bytes = size_t(row_stride) * size_t(height - 1) + size_t(width * bpp);
     ws.image.reserve(bytes);
     check(cudaMemcpyAsync(ws.image.p, pixels, bytes, cudaMemcpyHostToDevice, s), "image upload");
-    check(cudaMemsetAsync(ws.state.p, 0, sizeof(QueryState), s), "memset");
+    init_state(ws, s, kMaxCandidates);
     LevelImage lev[kMaxLevels];
     int w = int(crop_right), h = int(crop_bottom);
     for (int l = 0; l <= level; ++l) {
@@ -3030,6 +3059,26 @@ int32_t mvg_profile_read(int32_t stage, const char** name, double* ms, int64_t* 
     if (work) *work = t_prof.work[stage];
     if (finds) *finds = t_prof.finds;
   });
+}
+
+int32_t mvg_set_budgets(int64_t samples, int64_t pixels, int32_t candidates) {
+  return guarded([&] {
+    if (samples < 0 || samples > int64_t(INT32_MAX) || pixels < 0 || pixels > (int64_t(1) << 30) || candidates < 0 ||
+        candidates > kMaxCandidatesExt)
+      raise(kInvalidArgument, "budgets: samples 0..2^31-1, pixels 0..2^30, candidates 0..262144 (0 = default)");
+    Budgets& b = thread_budgets();
+    b.samples = samples ? size_t(samples) : kModelSampleBudget;
+    b.pixels = pixels ? pixels : 32000000;
+    b.candidates = candidates ? candidates : kMaxCandidates;
+  });
+}
+
+int32_t mvg_get_budgets(int64_t* samples, int64_t* pixels, int32_t* candidates) {
+  const Budgets& b = thread_budgets();
+  if (samples) *samples = int64_t(b.samples);
+  if (pixels) *pixels = b.pixels;
+  if (candidates) *candidates = b.candidates;
+  return kOk;
 }
 
 int32_t mvg_set_batch_merge(int32_t cohorts) {

@@ -386,7 +386,7 @@ void build_tables_device(const HostModel& m, const std::vector<int32_t>& lin_pit
     // the reference's checks, raster by raster (model.cpp:235-238)
     for (int k = 0; k < nj; ++k) {
       if (flag[size_t(k)]) raise(kInvalidArgument, "rotation produces a degenerate template");
-      if (size_t(ns[size_t(k)]) > kModelSampleBudget - total) raise(kLimitExceeded, "model raster budget exceeded");
+      if (size_t(ns[size_t(k)]) > m.sample_budget - total) raise(kLimitExceeded, "model raster budget exceeded");
       total += size_t(ns[size_t(k)]);
     }
     raster_tables_kernel<<<nj, kBuildThreads, 0, s>>>(

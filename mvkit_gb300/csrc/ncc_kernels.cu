@@ -793,8 +793,9 @@ __global__ void dedup_kernel(DedupArgs a) {
   if (!isfinite(p.score) || p.score < a.threshold) return;
   const unsigned long long kr = __double_as_longlong(p.row), kc = __double_as_longlong(p.col),
                            ka = __double_as_longlong(p.angle);
-  unsigned slot = unsigned(mix64(kr ^ mix64(kc ^ mix64(ka)))) & (kHashSlots - 1);
-  for (int probe = 0; probe < kHashSlots; ++probe) {
+  const unsigned mask = unsigned(a.hash_slots - 1);
+  unsigned slot = unsigned(mix64(kr ^ mix64(kc ^ mix64(ka)))) & mask;
+  for (int probe = 0; probe < a.hash_slots; ++probe) {
     const int prev = atomicCAS(a.table + slot, -1, i);
     if (prev == -1) {
       const int k = atomicAdd(&a.state->count[a.out_slot], 1);
@@ -805,7 +806,7 @@ __global__ void dedup_kernel(DedupArgs a) {
     if ((unsigned long long)__double_as_longlong(q.row) == kr && (unsigned long long)__double_as_longlong(q.col) == kc &&
         (unsigned long long)__double_as_longlong(q.angle) == ka)
       return;
-    slot = (slot + 1) & (kHashSlots - 1);
+    slot = (slot + 1) & mask;
   }
 }
 
@@ -2262,8 +2263,8 @@ cudaError_t launch_pairs(const float* v, int w, int h, uint32_t* pairs, cudaStre
   return cudaGetLastError();
 }
 
-cudaError_t launch_sort(const SortArgs& a, cudaStream_t s) {
-  sort_kernel<<<(kMaxCandidates + kSortPer - 1) / kSortPer, 256, 0, s>>>(a);
+cudaError_t launch_sort(const SortArgs& a, int max_candidates, cudaStream_t s) {
+  sort_kernel<<<(max_candidates + kSortPer - 1) / kSortPer, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 

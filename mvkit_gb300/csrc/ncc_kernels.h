@@ -11,11 +11,11 @@ namespace mvg {
 struct TcGroup;  // tensor-core group (below)
 
 // Entries of a candidate list that exist: a list's counter keeps counting
-// past the kMaxCandidates-entry buffers when the coarse budget overflows
-// (the find then ends with LimitExceeded), so readers clamp it.
+// past the cap-entry buffers when the coarse budget overflows (the find then
+// ends with LimitExceeded), so readers clamp it.
 #ifdef __CUDACC__
 __device__ __forceinline__ int live_count(const QueryState* s, int slot) {
-  return min(s->count[slot], kMaxCandidates);
+  return min(s->count[slot], s->cap);
 }
 #endif
 
@@ -140,7 +140,7 @@ constexpr int kTcMaxP = 16;              // patches of one group (N = 10 P <= 16
 constexpr int kTcCands = 16;             // candidates per tile (M = 16 x 8 rows)
 constexpr int kTcScoreStride = 16 * 25;  // dots per candidate: [selected patch][placement]
 constexpr int kTcMaxGroups = 4096;       // groups of one tracking step
-constexpr int kTcMaxTiles = kMaxCandidates / kTcCands + kTcMaxGroups + 1;
+constexpr int kTcMaxTiles = kMaxCandidatesExt / kTcCands + kTcMaxGroups + 1;
 constexpr int kTcMaxStages = 16;         // weight-chunk buffers
 constexpr int kTcPlaneShifts = 8;        // column-shifted copies of a level plane
 constexpr int kTcPlaneMargin = 8;        // plane columns left of the level
@@ -239,6 +239,7 @@ struct DedupArgs {
   int snap;                 // 1: snap poses outside the domain into it first
   double height, width;     // image size for the snap (full domain)
   DomainView dom;
+  int hash_slots;           // entries of `table`: a power of two >= 3 x the candidate budget
 };
 
 struct ImageView {
@@ -351,7 +352,7 @@ cudaError_t launch_dedup(const DedupArgs& a, int max_candidates, cudaStream_t s)
 cudaError_t launch_score(const ScoreArgs& a, int max_candidates, cudaStream_t s);
 cudaError_t launch_adjoint(const AdjointArgs& a, cudaStream_t s);
 cudaError_t launch_refine4(const Refine4Args& a, cudaStream_t s);
-cudaError_t launch_sort(const SortArgs& a, cudaStream_t s);
+cudaError_t launch_sort(const SortArgs& a, int max_candidates, cudaStream_t s);
 cudaError_t launch_rects(const Cand* sorted, RectAux* aux, const QueryState* state, RectGeom g, int max_candidates,
                          cudaStream_t s);
 cudaError_t launch_select(const SelectArgs& a, cudaStream_t s);

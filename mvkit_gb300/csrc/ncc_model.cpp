@@ -12,10 +12,15 @@
 #include <limits>
 
 namespace mvg {
+Budgets& thread_budgets() {
+  thread_local Budgets b;
+  return b;
+}
+
 namespace {
 
 constexpr double kTwoPi = 6.283185307179586476925286766559;
-constexpr size_t kTemplatePixels = kModelTemplatePixels, kAngles = kModelAngles, kSampleBudget = kModelSampleBudget;
+constexpr size_t kTemplatePixels = kModelTemplatePixels, kAngles = kModelAngles;
 
 // Pending raster before normalisation: FP64 gray values at integer offsets.
 struct RawSample { int32_t row, col; double value; };
@@ -251,6 +256,7 @@ HostModel rebuild_model(ModelLevel first, const CreateParams& params, double ori
   m.level0_mean = level0.mean;
   m.level0_energy = level0.energy;
   m.rasters = false;
+  m.sample_budget = thread_budgets().samples;
   if (rasters) build_rasters(m);
   return m;
 }
@@ -265,7 +271,7 @@ void build_rasters(HostModel& m) {
     for (const double angle : m.angles) {
       Raster p = rotate_impl(L, angle, li == 0 ? &level0 : nullptr);
       if (p.w.empty()) raise(kInvalidArgument, "rotation produces a degenerate template");
-      if (p.size() > kSampleBudget - total) raise(kLimitExceeded, "model raster budget exceeded");
+      if (p.size() > m.sample_budget - total) raise(kLimitExceeded, "model raster budget exceeded");
       total += p.size();
       L.patches.push_back(std::move(p));
     }

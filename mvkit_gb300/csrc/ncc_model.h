@@ -43,6 +43,9 @@ struct ModelLevel {
   std::vector<Raster> patches;
 };
 
+// Limits of the model build (src/ncc_matching/model.cpp:14-18).
+constexpr size_t kModelTemplatePixels = 1048576, kModelAngles = 4096, kModelSampleBudget = 16000000;
+
 struct HostModel {
   CreateParams params;          // params.angle_step holds the resolved step
   size_t sample_count = 0;
@@ -54,10 +57,22 @@ struct HostModel {
   std::vector<double> angles;
   double level0_mean = 0, level0_energy = 0;
   bool rasters = true;          // levels[l].patches built (false: built on the device)
+  size_t sample_budget = kModelSampleBudget;  // raster samples allowed (the building thread's budget)
 };
 
-// Limits of the model build (src/ncc_matching/model.cpp:14-18).
-constexpr size_t kModelTemplatePixels = 1048576, kModelAngles = 4096, kModelSampleBudget = 16000000;
+
+// Budgets of this thread's model builds and finds.  By default the
+// reference's: rotated-raster samples of a model (model.cpp:15,237), pixels
+// of a search image (matcher.cpp:373-374), coarse candidates of a find
+// (model.hpp:21, matcher.cpp:591), each exceeded with LimitExceeded.  An
+// explicit extended mode (mvg_set_budgets) raises them; what fits the
+// default budgets gives the same results either way.
+struct Budgets {
+  size_t samples = kModelSampleBudget;
+  int64_t pixels = 32000000;
+  int candidates = kMaxCandidates;
+};
+Budgets& thread_budgets();
 
 // CreateNccModel on a byte (type 0) or uint16 (type 1) template.  `mask`
 // (width*height bytes, nonzero = inside) is the template domain; NULL means

@@ -8,7 +8,8 @@ namespace mvg {
 
 constexpr int kMaxLevels = 16;
 constexpr int kMaxCandidates = 10000;        // FindOptions::max_candidates (src/ncc_matching/model.hpp:21)
-constexpr int kHashSlots = 32768;            // >= 3 x kMaxCandidates, power of two
+constexpr int kMaxCandidatesExt = 1 << 18;   // largest candidate budget of an extended find
+constexpr int kHashSlots = 32768;            // >= 3 x kMaxCandidates, power of two (dedup table of a default find)
 
 // Status codes (MvStatus, include/mvkit/c/mv_status.h:12-24 in the reference).
 enum Status : int32_t {
@@ -100,7 +101,7 @@ struct QueryState {
   int32_t need;                    // 1: refinement results missing for `next`
   int32_t done;
   int32_t batch_count;             // entries in the refinement batch
-  int32_t pad_;
+  int32_t cap;                     // candidate budget of the find (list buffers hold this many)
   unsigned long long track_macs;   // algorithmic MACs of the CUDA-core tracking (25 positions x samples per patch)
   unsigned long long tc_macs;      // algorithmic MACs of the tensor-core tracking
   unsigned long long tc_issued;    // MACs issued to the tensor cores (M x N x K per MMA)

@@ -714,6 +714,39 @@ def set_correlation_path(path: str) -> None:
     _check(lib.mvg_set_correlation_path(0 if path == "tensor" else 1), "set_correlation_path")
 
 
+def set_budgets(samples: int = 0, pixels: int = 0, candidates: int = 0) -> None:
+    """Extended mode: this thread's model-raster sample, search-image pixel and
+    coarse-candidate budgets (0 = the reference's 16 000 000, 32 000 000 and
+    10 000)."""
+    lib = load()
+    lib.mvg_set_budgets.argtypes = [C.c_int64, C.c_int64, C.c_int32]
+    lib.mvg_set_budgets.restype = C.c_int32
+    _check(lib.mvg_set_budgets(int(samples), int(pixels), int(candidates)), "set_budgets")
+
+
+def get_budgets() -> dict:
+    lib = load()
+    a, b, c = C.c_int64(), C.c_int64(), C.c_int32()
+    lib.mvg_get_budgets.argtypes = [_i64p, _i64p, _i32p]
+    _check(lib.mvg_get_budgets(C.byref(a), C.byref(b), C.byref(c)), "get_budgets")
+    return {"samples": a.value, "pixels": b.value, "candidates": c.value}
+
+
+class extended_budgets:
+    """Context manager: the budgets raised inside, restored on exit."""
+
+    def __init__(self, samples: int = 0, pixels: int = 0, candidates: int = 0):
+        self.want = (samples, pixels, candidates)
+
+    def __enter__(self):
+        self.old = get_budgets()
+        set_budgets(*self.want)
+        return self
+
+    def __exit__(self, *exc):
+        set_budgets(self.old["samples"], self.old["pixels"], self.old["candidates"])
+
+
 def set_batch_merge(cohorts: int = 0) -> None:
     """Batched calls from this thread merge their finds' tensor-core launches
     within `cohorts` groups of workers; 0 (the library's default) launches

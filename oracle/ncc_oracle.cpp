@@ -24,8 +24,13 @@ namespace orc {
 namespace {
 
 constexpr double kTau = 6.283185307179586476925286766559;
-constexpr std::size_t kMaxPixels = 1048576, kMaxAngles = 4096, kMaxSamples = 16000000;
-constexpr std::size_t kMaxCandidates = 10000;
+constexpr std::size_t kMaxPixels = 1048576, kMaxAngles = 4096;
+// Budgets (model.cpp:15, matcher.cpp:373-374, model.hpp:21): the reference's
+// by default; orc_set_budgets lifts them for checking the library's extended
+// mode (process-wide, set before the calls it applies to).
+std::size_t g_max_samples = 16000000;
+long long g_max_image_pixels = 32000000;
+std::size_t g_max_candidates = 10000;
 const double kMissing = -std::numeric_limits<double>::infinity();
 
 enum Status : int {
@@ -66,7 +71,7 @@ struct Model {
 struct Pose { double row = 0, col = 0, angle = 0, score = 0; };
 struct FindOpts {
   double start = 0, extent = 0, min_score = .8, max_overlap = .5;
-  std::size_t num_matches = 1, max_candidates = kMaxCandidates;
+  std::size_t num_matches = 1, max_candidates = g_max_candidates;
   bool subpixel = true;
   int highest = 0, lowest = 1;
 };
@@ -278,7 +283,7 @@ Model rebuild(Level first, const CreateOpts& opt, double orow, double ocol) {
       const double angle = opt.start + std::min(opt.extent, i * m.opt.step);
       Patch p = rotate(L, angle, &L == &m.levels.front() ? &first_norm : nullptr);
       if (p.s.empty()) fail(kInvalidArgument, "rotation produces a degenerate template");
-      if (p.s.size() > kMaxSamples - total) fail(kLimitExceeded, "model raster budget exceeded");
+      if (p.s.size() > g_max_samples - total) fail(kLimitExceeded, "model raster budget exceeded");
       total += p.s.size();
       L.patches.push_back(std::move(p));
     }
@@ -579,7 +584,7 @@ std::unique_ptr<Query> prepare(const T* px, std::int64_t W, std::int64_t H, std:
   opt.start = cs;
   opt.extent = std::max(0., ce - cs);
   q->opt = opt;
-  if (!W || !H || W > std::numeric_limits<int>::max() || H > std::numeric_limits<int>::max() || H > 32000000 / W)
+  if (!W || !H || W > std::numeric_limits<int>::max() || H > std::numeric_limits<int>::max() || H > g_max_image_pixels / (long long)W)
     fail(kLimitExceeded, "search image exceeds pixel budget");
   q->dom = make_domain(W, H, dmask);
   const Domain& dom = q->dom;
@@ -989,6 +994,12 @@ std::vector<Pose> run_find(const Model& m, const void* img, int type, std::int64
 using namespace orc;
 
 extern "C" {
+
+void orc_set_budgets(int64_t samples, int64_t pixels, int64_t candidates) {
+  orc::g_max_samples = samples > 0 ? std::size_t(samples) : 16000000;
+  orc::g_max_image_pixels = pixels > 0 ? pixels : 32000000;
+  orc::g_max_candidates = candidates > 0 ? std::size_t(candidates) : 10000;
+}
 
 int orc_create(const void* pixels, int type, int64_t width, int64_t height, int64_t stride, const uint8_t* mask,
                int levels, double angle_start, double angle_extent, double angle_step, int ignore_polarity,

@@ -41,6 +41,11 @@ int orc_pyramid(void* model, const void* image, int type, int64_t width, int64_t
                 int64_t stride, int highest, int level, double* out, int64_t capacity,
                 double* geom, char* err, int errlen);
 
+/* Budgets of the following calls (process-wide): model raster samples,
+ * search-image pixels, coarse candidates; 0 = the reference's (16 000 000,
+ * 32 000 000, 10 000).  Lifted, they check the library's extended mode. */
+void orc_set_budgets(int64_t samples, int64_t pixels, int64_t candidates);
+
 /* Batch of independent finds over `n` images on `threads` host threads (one
  * image per thread at a time); returns the number of matches summed. */
 int64_t orc_find_many(void* model, const void* const* images, int type, int64_t width,

@@ -230,6 +230,15 @@ def oracle() -> Checker:
     return Checker(build_oracle(), "orc")
 
 
+def set_oracle_budgets(samples: int = 0, pixels: int = 0, candidates: int = 0) -> None:
+    """The oracle's raster-sample, image-pixel and candidate budgets for the
+    following calls (process-wide; 0 = the reference's)."""
+    lib = oracle().lib
+    lib.orc_set_budgets.argtypes = [C.c_int64, C.c_int64, C.c_int64]
+    lib.orc_set_budgets.restype = None
+    lib.orc_set_budgets(int(samples), int(pixels), int(candidates))
+
+
 def reference(kind: str = "scalar") -> Checker | None:
     p = REF_DIR / f"libref_{kind}.so"
     if not p.exists():

@@ -92,3 +92,43 @@ def test_rasters_equal_oracle_and_reference(host_build, name):
     with pytest.raises(mg.MvError) as e:
         ncc.ncc_model_raster(model, levels, 0)
     assert e.value.status == ncc.MV_STATUS_INVALID_ARGUMENT
+
+
+def test_extended_sample_budget(host_build):
+    """A 160^2 template over a full circle needs more than the reference's 16
+    million raster samples: refused (LimitExceeded, as by the reference) under
+    the default budget; under a raised budget every raster equals the
+    oracle's with the same budget, bit for bit.  The model keeps its budget."""
+    t = template(9, (160, 160), np.uint8, 255)
+    with pytest.raises(mg.MvError) as e:
+        mg.create_ncc_model(t, 4, -math.pi, 2 * math.pi, "auto", "use_polarity")
+    assert e.value.status == -103 and "raster budget" in e.value.message
+    orc = oracle_lib.oracle()
+    with pytest.raises(oracle_lib.CheckerError) as oe:
+        orc.create(t, levels=4, angle_start=-math.pi, angle_extent=2 * math.pi)
+    assert oe.value.status == -103
+    with mg.extended_budgets(samples=100_000_000):
+        model = mg.create_ncc_model(t, 4, -math.pi, 2 * math.pi, "auto", "use_polarity")
+    assert mg.get_budgets()["samples"] == 16_000_000
+    oracle_lib.set_oracle_budgets(samples=100_000_000)
+    try:
+        om = orc.create(t, levels=4, angle_start=-math.pi, angle_extent=2 * math.pi)
+    finally:
+        oracle_lib.set_oracle_budgets()
+    info = om.info()
+    total = 0
+    for lv in range(4):
+        for k in range(info["patches"]):
+            a = ncc.ncc_model_raster(model, lv, k)
+            same(a, om.patch(lv, k), f"extended level {lv} raster {k}")
+            total += len(a["rows"])
+    assert total > 16_000_000
+
+
+def test_budget_arguments():
+    with pytest.raises(mg.MvError) as e:
+        mg.set_budgets(candidates=1 << 20)
+    assert e.value.status == -1
+    with mg.extended_budgets(samples=5, pixels=7, candidates=11):
+        assert mg.get_budgets() == {"samples": 5, "pixels": 7, "candidates": 11}
+    assert mg.get_budgets() == {"samples": 16_000_000, "pixels": 32_000_000, "candidates": 10_000}
