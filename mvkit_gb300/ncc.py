@@ -617,13 +617,16 @@ def find_ncc_model_stage(image, model: NccModel, angle_start, angle_extent, min_
     ctl = _find_controls(op, angle_start, angle_extent, min_score, num_matches, max_overlap, subpixel, num_levels)
     a, typ = _image(image, op, "Image")
     cap = 20000
-    out = np.zeros((cap, 4))
-    cnt = C.c_int64()
     dom = _domain(domain, a.shape, op)
-    _check(load().mvg_find_ncc_model_stage(a.ctypes.data, typ, a.shape[1], a.shape[0], a.strides[0], 0,
-                                           None if dom is None else dom.ctypes.data, model.handle, *ctl, int(stage),
-                                           out.ctypes.data_as(_dp), cap, C.byref(cnt)), op)
-    return out[: min(cnt.value, cap)].copy()
+    while True:
+        out = np.zeros((cap, 4))
+        cnt = C.c_int64()
+        _check(load().mvg_find_ncc_model_stage(a.ctypes.data, typ, a.shape[1], a.shape[0], a.strides[0], 0,
+                                               None if dom is None else dom.ctypes.data, model.handle, *ctl,
+                                               int(stage), out.ctypes.data_as(_dp), cap, C.byref(cnt)), op)
+        if cnt.value <= cap:
+            return out[: cnt.value].copy()
+        cap = int(cnt.value)
 
 
 def pyramid_level(image, model: NccModel, highest_level: int, level: int):

@@ -1,0 +1,100 @@
+"""Extended mode on the GPU: searches the reference refuses under its budgets
+(mvg_set_budgets) give the matches of the FP64 oracle with the same budgets
+lifted (count, order, |drow|, |dcol| <= 0.05 px, |dangle| <= 0.05 deg,
+|dscore| <= 1e-4), and the default budgets still give the reference's
+statuses.
+
+- more than 10 000 coarse candidates (a 48^2 template over a full circle
+  with automatic levels: the reference's LimitExceeded case `budget_360`);
+- a search image of more than 32 million pixels (4096 x 8192);
+- a model of more than 16 million raster samples (160^2 over a full circle)."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle_lib
+from golden.cases import CASES, make_inputs
+from test_gpu_parity import GOLDEN, assert_same_matches
+
+pytestmark = pytest.mark.gpu
+EXT = dict(samples=100_000_000, pixels=1 << 30, candidates=200_000)
+
+
+@pytest.fixture(scope="module")
+def mg():
+    import mvkit_gb300
+    from mvkit_gb300 import build
+    build.build()
+    mvkit_gb300.load()
+    return mvkit_gb300
+
+
+@pytest.fixture
+def orc_ext():
+    orc = oracle_lib.oracle()
+    oracle_lib.set_oracle_budgets(**EXT)
+    yield orc
+    oracle_lib.set_oracle_budgets()
+
+
+def test_candidate_budget(mg, orc_ext):
+    case = CASES["budget_360"]
+    wl, _ = make_inputs(case)
+    c, f = case["create"], case["find"]
+    ctl = (f["angle_start"], f["angle_extent"], f["min_score"], f["num_matches"], f["max_overlap"], "true",
+           [f["highest"], f["lowest"]])
+    model = mg.create_ncc_model(wl.template, "auto", c["angle_start"], c["angle_extent"], "auto", "use_polarity")
+    with pytest.raises(mg.MvError) as e:
+        mg.find_ncc_model(wl.image, model, *ctl)
+    assert e.value.status == GOLDEN["budget_360"]["status"] == -103
+    om = orc_ext.create(wl.template, levels=0, angle_start=c["angle_start"], angle_extent=c["angle_extent"])
+    want = orc_ext.find(om, wl.image, f["angle_start"], f["angle_extent"], f["min_score"], f["num_matches"],
+                        f["max_overlap"], True, f["highest"], f["lowest"])
+    coarse = orc_ext.find(om, wl.image, f["angle_start"], f["angle_extent"], f["min_score"], f["num_matches"],
+                          f["max_overlap"], True, f["highest"], f["lowest"], stage=0)
+    assert len(coarse) > 10_000 and len(want) == 3
+    with mg.extended_budgets(**EXT):
+        got = mg.find_ncc_model(wl.image, model, *ctl)
+        gc = mg.find_ncc_model_stage(wl.image, model, *ctl, stage=0)
+    assert len(gc) == len(coarse)
+    assert_same_matches(got, want, "budget_360 extended")
+
+
+def test_pixel_budget(mg, orc_ext):
+    from mvkit_gb300 import workloads as W
+    base = W.make_workload(61, 1024, 2048, 64, 2)
+    image = np.tile(base.image, (4, 4))  # 4096 x 8192: 33.5 M pixels
+    assert image.size > 32_000_000
+    model = mg.create_ncc_model(base.template, 4, 0.0, 0.0, "auto", "use_polarity")
+    ctl = (0.0, 0.0, 0.7, 6, 0.5, "true", 4)
+    with pytest.raises(mg.MvError) as e:
+        mg.find_ncc_model(image, model, *ctl)
+    assert e.value.status == -103 and "pixel budget" in e.value.message
+    om = orc_ext.create(base.template, levels=4, angle_start=0.0, angle_extent=0.0)
+    want = orc_ext.find(om, image, 0.0, 0.0, 0.7, 6, 0.5, True, 4, 1)
+    assert len(want) == 6
+    with mg.extended_budgets(**EXT):
+        got = mg.find_ncc_model(image, model, *ctl)
+    assert_same_matches(got, want, "4096 x 8192")
+
+
+@pytest.mark.parametrize("path", ["tensor", "plain"])
+def test_sample_budget(mg, orc_ext, path):
+    from mvkit_gb300 import workloads as W
+    wl = W.make_workload(62, 1024, 1024, 160, 3, angle_range=(-math.pi, math.pi))
+    with pytest.raises(mg.MvError) as e:
+        mg.create_ncc_model(wl.template, 4, -math.pi, 2 * math.pi, "auto", "use_polarity")
+    assert e.value.status == -103
+    with mg.extended_budgets(**EXT):
+        model = mg.create_ncc_model(wl.template, 4, -math.pi, 2 * math.pi, "auto", "use_polarity")
+    om = orc_ext.create(wl.template, levels=4, angle_start=-math.pi, angle_extent=2 * math.pi)
+    want = orc_ext.find(om, wl.image, -math.pi, 2 * math.pi, 0.7, 3, 0.5, True, 4, 1)
+    assert len(want) == 3
+    mg.set_correlation_path(path)
+    try:
+        with mg.extended_budgets(**EXT):
+            got = mg.find_ncc_model(wl.image, model, -math.pi, 2 * math.pi, 0.7, 3, 0.5, "true", 4)
+    finally:
+        mg.set_correlation_path("tensor")
+    assert_same_matches(got, want, f"160^2 full circle ({path})")
