@@ -104,7 +104,9 @@ MVG_API int32_t mvg_set_model_build(int32_t where);
  * full circle, images such as 8192 x 8192, and searches with more coarse
  * candidates run where the reference refuses them; searches within the
  * default budgets give the same results either way.  Limits: samples <=
- * 2^31 - 1, pixels <= 2^30, candidates <= 262144.  A model keeps the sample
+ * 2^31 - 1, pixels <= 2^30, candidates <= 2^21.  Device memory of a find grows
+ * with its candidate budget (about 1.7 KB per candidate on the tensor-core
+ * path).  A model keeps the sample
  * budget it was built with. */
 MVG_API int32_t mvg_set_budgets(int64_t samples, int64_t pixels, int32_t candidates);
 MVG_API int32_t mvg_get_budgets(int64_t* samples, int64_t* pixels, int32_t* candidates);

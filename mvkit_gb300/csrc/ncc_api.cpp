@@ -3065,7 +3065,7 @@ int32_t mvg_set_budgets(int64_t samples, int64_t pixels, int32_t candidates) {
   return guarded([&] {
     if (samples < 0 || samples > int64_t(INT32_MAX) || pixels < 0 || pixels > (int64_t(1) << 30) || candidates < 0 ||
         candidates > kMaxCandidatesExt)
-      raise(kInvalidArgument, "budgets: samples 0..2^31-1, pixels 0..2^30, candidates 0..262144 (0 = default)");
+      raise(kInvalidArgument, "budgets: samples 0..2^31-1, pixels 0..2^30, candidates 0..2097152 (0 = default)");
     Budgets& b = thread_budgets();
     b.samples = samples ? size_t(samples) : kModelSampleBudget;
     b.pixels = pixels ? pixels : 32000000;

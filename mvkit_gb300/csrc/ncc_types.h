@@ -8,7 +8,7 @@ namespace mvg {
 
 constexpr int kMaxLevels = 16;
 constexpr int kMaxCandidates = 10000;        // FindOptions::max_candidates (src/ncc_matching/model.hpp:21)
-constexpr int kMaxCandidatesExt = 1 << 18;   // largest candidate budget of an extended find
+constexpr int kMaxCandidatesExt = 1 << 21;   // largest candidate budget of an extended find
 constexpr int kHashSlots = 32768;            // >= 3 x kMaxCandidates, power of two (dedup table of a default find)
 
 // Status codes (MvStatus, include/mvkit/c/mv_status.h:12-24 in the reference).

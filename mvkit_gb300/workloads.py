@@ -295,18 +295,28 @@ def config_workload(name: str, seed: int) -> Workload:
     return make_workload(seed, **CONFIGS[name]["gen"])
 
 
+def _multi_args(a):
+    return make_multi_workload(*a[0], **a[1])
+
+
 def make_batch_workloads(seed: int, n_images: int, sizes: tuple, tsizes: tuple, max_pastes: int,
                          angle_range: tuple = (-math.pi, math.pi), contrast: float = 0.1, noise_sigma: int = 5,
-                         maxval: int = 255) -> list:
+                         maxval: int = 255, processes: int = 1) -> list:
     """A batch of scenes of uneven size sharing one template set (one model
     per template searches every scene): scene i has a size drawn from
     `sizes` ((height, width) pairs) and each template pasted 1..max_pastes
-    times, with contrast U[1-c, 1+c] and noise `noise_sigma`."""
+    times, with contrast U[1-c, 1+c] and noise `noise_sigma`.  processes > 1
+    generates the scenes in that many spawned processes (same scenes)."""
     rng = np.random.default_rng([seed, 7])
-    batch = []
+    jobs = []
     for i in range(n_images):
         h, w = sizes[int(rng.integers(0, len(sizes)))]
         n = tuple(int(rng.integers(1, max_pastes + 1)) for _ in tsizes)
-        batch.append(make_multi_workload(seed * 1000 + i + 1, h, w, tsizes, n, angle_range, noise_sigma,
-                                         maxval=maxval, contrast=contrast, template_seed=seed))
-    return batch
+        jobs.append(((seed * 1000 + i + 1, h, w, tsizes, n, angle_range, noise_sigma),
+                     dict(maxval=maxval, contrast=contrast, template_seed=seed)))
+    if processes <= 1:
+        return [_multi_args(j) for j in jobs]
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    with ProcessPoolExecutor(processes, mp_context=mp.get_context("spawn")) as ex:
+        return list(ex.map(_multi_args, jobs))

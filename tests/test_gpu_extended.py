@@ -98,3 +98,48 @@ def test_sample_budget(mg, orc_ext, path):
     finally:
         mg.set_correlation_path("tensor")
     assert_same_matches(got, want, f"160^2 full circle ({path})")
+
+
+def test_large_uint16_configuration_scaled(mg, orc_ext):
+    """The large uint16 configuration (12-bit data, noise sigma 20, a template
+    over a full circle, MinScore 0.5, MaxOverlap 0.3) scaled to a 1024^2 image
+    and a 128^2 template: its coarse scan yields more than the reference's
+    10 000 candidates (LimitExceeded by default); extended, the matches are
+    the budget-lifted oracle's."""
+    from mvkit_gb300 import workloads as W
+    wl = W.make_workload(71, 1024, 1024, 128, 3, angle_range=(-math.pi, math.pi), maxval=4095, noise_sigma=20)
+    assert wl.image.dtype == np.uint16
+    model = mg.create_ncc_model(wl.template, 4, -math.pi, 2 * math.pi, "auto", "use_polarity")
+    ctl = (-math.pi, 2 * math.pi, 0.5, 3, 0.3, "true", 4)
+    with pytest.raises(mg.MvError) as e:
+        mg.find_ncc_model(wl.image, model, *ctl)
+    assert e.value.status == -103
+    om = orc_ext.create(wl.template, levels=4, angle_start=-math.pi, angle_extent=2 * math.pi)
+    want = orc_ext.find(om, wl.image, -math.pi, 2 * math.pi, 0.5, 3, 0.3, True, 4, 1)
+    assert len(want) == 3
+    with mg.extended_budgets(**EXT):
+        got = mg.find_ncc_model(wl.image, model, *ctl)
+    assert_same_matches(got, want, "u16 full circle extended")
+
+
+def test_batched_configuration_scaled(mg, orc_ext):
+    """The batched configuration's controls (a template over a full circle,
+    automatic levels, MinScore 0.6, all matches, contrast +-10 %, noise sigma
+    5) on a batch of scenes of uneven size, in extended mode through the
+    batched operator: each scene's matches are the budget-lifted oracle's."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from mvkit_gb300 import workloads as W
+    batch = W.make_batch_workloads(13, 4, ((768, 1024), (640, 800), (512, 512)), (64,), 3)
+    t = batch[0].templates[0]
+    model = mg.create_ncc_model(t, "auto", -math.pi, 2 * math.pi, "auto", "use_polarity")
+    ctl = (-math.pi, 2 * math.pi, 0.6, 0, 0.5, "true", 0)
+    with mg.extended_budgets(**EXT):
+        got = mg.find_ncc_models_batch([b.image for b in batch], [model], *ctl, workers=4)
+    om = orc_ext.create(t, levels=0, angle_start=-math.pi, angle_extent=2 * math.pi)
+    with ThreadPoolExecutor(4) as ex:
+        want = list(ex.map(lambda b: orc_ext.find(om, b.image, -math.pi, 2 * math.pi, 0.6, 0, 0.5, True, 0, 1),
+                           batch))
+    for i, (g, w) in enumerate(zip(got, want)):
+        assert len(w) >= len(batch[i].poses[0])
+        assert_same_matches(g[:4], w, f"batch scene {i}")

@@ -127,7 +127,7 @@ def test_extended_sample_budget(host_build):
 
 def test_budget_arguments():
     with pytest.raises(mg.MvError) as e:
-        mg.set_budgets(candidates=1 << 20)
+        mg.set_budgets(candidates=1 << 22)
     assert e.value.status == -1
     with mg.extended_budgets(samples=5, pixels=7, candidates=11):
         assert mg.get_budgets() == {"samples": 5, "pixels": 7, "candidates": 11}
