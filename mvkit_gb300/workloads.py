@@ -223,12 +223,13 @@ class MultiWorkload:
 def make_multi_workload(seed: int, height: int, width: int, tsizes: tuple, n_poses: tuple,
                         angle_range: tuple = (0.0, 0.0), noise_sigma: int = 3, shapes: int = 40,
                         maxval: int = 255, contrast: float = 0.0,
-                        template_seed: int | None = None) -> MultiWorkload:
+                        template_seed: int | None = None, fit: bool = False) -> MultiWorkload:
     """One scene holding several different templates (FindNccModels): template
     k (side tsizes[k], cropped from its own source scene) is pasted n_poses[k]
     times; no two pastes overlap.  contrast > 0 scales each paste by
     U[1-c, 1+c]; template_seed (default: seed) makes the templates, so scenes
-    of one batch can share them."""
+    of one batch can share them.  fit: a template gets fewer pastes (at least
+    none) when no free place is found in 10000 tries, instead of an error."""
     dtype = np.uint8 if maxval <= 255 else np.uint16
     tseed = seed if template_seed is None else template_seed
     templates = []
@@ -251,6 +252,8 @@ def make_multi_workload(seed: int, height: int, width: int, tsizes: tuple, n_pos
         while len(poses[k]) < n_poses[k]:
             tries += 1
             if tries > 10000:
+                if fit:
+                    break
                 raise ValueError("cannot place the requested poses without overlap")
             row = margin + float(rng.integers(0, 1 << 20)) / (1 << 20) * (height - 1 - 2 * margin)
             col = margin + float(rng.integers(0, 1 << 20)) / (1 << 20) * (width - 1 - 2 * margin)
@@ -301,19 +304,21 @@ def _multi_args(a):
 
 def make_batch_workloads(seed: int, n_images: int, sizes: tuple, tsizes: tuple, max_pastes: int,
                          angle_range: tuple = (-math.pi, math.pi), contrast: float = 0.1, noise_sigma: int = 5,
-                         maxval: int = 255, processes: int = 1) -> list:
+                         maxval: int = 255, processes: int = 1, fit: bool = False) -> list:
     """A batch of scenes of uneven size sharing one template set (one model
     per template searches every scene): scene i has a size drawn from
     `sizes` ((height, width) pairs) and each template pasted 1..max_pastes
     times, with contrast U[1-c, 1+c] and noise `noise_sigma`.  processes > 1
-    generates the scenes in that many spawned processes (same scenes)."""
+    generates the scenes in that many spawned processes (same scenes); fit:
+    a scene too small for its pastes gets as many as fit (its poses list
+    them)."""
     rng = np.random.default_rng([seed, 7])
     jobs = []
     for i in range(n_images):
         h, w = sizes[int(rng.integers(0, len(sizes)))]
         n = tuple(int(rng.integers(1, max_pastes + 1)) for _ in tsizes)
         jobs.append(((seed * 1000 + i + 1, h, w, tsizes, n, angle_range, noise_sigma),
-                     dict(maxval=maxval, contrast=contrast, template_seed=seed)))
+                     dict(maxval=maxval, contrast=contrast, template_seed=seed, fit=fit)))
     if processes <= 1:
         return [_multi_args(j) for j in jobs]
     import multiprocessing as mp
