@@ -276,14 +276,25 @@ CONFIG_WORKLOADS = {
     # {32..256}^2 each pasted 1-10 times over a full circle (as many as fit
     # without overlap on the smaller scenes), contrast +-10 %, noise sigma 5;
     # automatic levels, MinScore 0.6, NumMatches 10 per template (at most 10
-    # pastes; one value per model: a single value would be a quota over all
-    # models), MaxOverlap 0.5 over all models
+    # pastes), MaxOverlap 0.5.  A step searches the batch once per template
+    # (one single-model batched call each, selection on the device): a
+    # FindNccModels with per-model quotas selects on the host and refines
+    # candidate after candidate until every quota is met
     "batch_64_t32_256_360": dict(
         kind="batch", gen=dict(seed=3, n_images=64, sizes=((512, 512), (1024, 1280), (2048, 2448), (3000, 4096)),
                                tsizes=(32, 48, 64, 96, 128, 160, 192, 256), max_pastes=10,
                                angle_range=(-math.pi, math.pi), contrast=0.1, noise_sigma=5, fit=True),
-        levels="auto", find=(FULL_CIRCLE[0], FULL_CIRCLE[1], 0.6, [10] * 8, 0.5, "true", 0),
+        levels="auto", find=(FULL_CIRCLE[0], FULL_CIRCLE[1], 0.6, 10, 0.5, "true", 0), per_model=True,
         budgets=dict(samples=600_000_000, pixels=1 << 30, candidates=1 << 21), workers=8),
+    # 5120x5120 uint8, 4 templates {128, 160, 192, 256}^2 pasted at 256 poses
+    # (subpixel row/column, angle U[0, 360 deg), scale U[0.95, 1.05]): a
+    # full-circle FindNccModels (rigid, the reference's refinement) and the
+    # adjoint-driven Gauss-Newton on (row, column, angle, scale) from its
+    # poses; the quadratic peak fit of the discrete poses beside them
+    "similarity_5120_t128_256_256x": dict(
+        kind="similarity", gen=dict(seed=7, height=5120, width=5120, tsizes=(128, 160, 192, 256), n_poses=256),
+        levels=4, find=(FULL_CIRCLE[0], FULL_CIRCLE[1], 0.4, [64] * 4, 0.5, "true", 4),
+        budgets=dict(samples=600_000_000, pixels=1 << 30, candidates=1 << 21), workers=1),
     # 8192x8192 uint16 (12-bit, noise sigma 20), one 512^2 template pasted 20
     # times over a full circle; NumLevels 6, MinScore 0.5, NumMatches 20,
     # MaxOverlap 0.3
@@ -308,6 +319,9 @@ def run_config(args) -> None:
     from mvkit_gb300 import workloads as W
 
     cfg = CONFIG_WORKLOADS[args.workload]
+    if cfg["kind"] == "similarity":
+        run_similarity(args, cfg)
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -347,7 +361,22 @@ def run_config(args) -> None:
     st = torch.cuda.Stream()
 
     def step(imgs):
-        return mg.find_ncc_models_batch(imgs, models, *cfg["find"], workers=workers, raise_errors=False)
+        if not cfg.get("per_model"):
+            return mg.find_ncc_models_batch(imgs, models, *cfg["find"], workers=workers, raise_errors=False)
+        # one batched call per model; image i's matches of every model, model
+        # index k (a failed image keeps its first error)
+        per = [mg.find_ncc_models_batch(imgs, [m], *cfg["find"], workers=workers, raise_errors=False)
+               for m in models]
+        out = []
+        for i in range(len(imgs)):
+            errs = [p_[i] for p_ in per if isinstance(p_[i], mg.MvError)]
+            if errs:
+                out.append(errs[0])
+                continue
+            parts = [p_[i] for p_ in per]
+            out.append(tuple(np.concatenate([q[j] for q in parts]) for j in range(4)) +
+                       (np.concatenate([np.full(len(q[0]), k, np.int64) for k, q in enumerate(parts)]),))
+        return out
 
     def timed(imgs, events: bool):
         total, out = 0.0, None
@@ -476,6 +505,171 @@ def run_config(args) -> None:
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def matcher_pose(r, c, a):
+    """The matcher's pixel-centre pose of the operator's edge-centred one."""
+    ca, sa = np.cos(a), np.sin(a)
+    return r - .5 * (1 - ca + sa), c - .5 * (1 - ca - sa)
+
+
+def similarity_errors(poses, model_of, truth) -> dict:
+    """Pose errors against the pasted similarity poses (nearest pose of the
+    paste's model within 3 px): median and max per degree of freedom, and the
+    share within 0.05 px (row and column) and 0.05 deg."""
+    err, missing = [], 0
+    for t in truth:
+        sel = np.nonzero(model_of == t.model)[0]
+        d = np.hypot(poses[sel, 0] - t.row, poses[sel, 1] - t.column) if len(sel) else np.zeros(0)
+        if not len(sel) or d.min() > 3:
+            missing += 1
+            continue
+        p = poses[sel[int(np.argmin(d))]]
+        err.append((abs(p[0] - t.row), abs(p[1] - t.column), abs(math.degrees(math.remainder(p[2] - t.angle,
+                                                                                                 2 * math.pi))),
+                    abs(p[3] - t.scale)))
+    e = np.array(err) if err else np.zeros((0, 4))
+    names = ("row_px", "col_px", "angle_deg", "scale")
+    return {"found": len(err), "missing": missing,
+            "median": dict(zip(names, np.median(e, axis=0).tolist())) if len(e) else None,
+            "max": dict(zip(names, e.max(axis=0).tolist())) if len(e) else None,
+            "within_0.05px_0.05deg": float(np.mean((e[:, 0] <= .05) & (e[:, 1] <= .05) & (e[:, 2] <= .05)))
+            if len(e) else None}
+
+
+def run_similarity(args, cfg) -> None:
+    """The differentiable-refinement configuration: a step is the full-circle
+    FindNccModels of the scene (extended mode) plus the adjoint Gauss-Newton
+    refinement of every match; pose errors of the rigid, quadratic-fit and
+    adjoint forms against the pasted poses."""
+    import torch
+    import mvkit_gb300 as mg
+    from mvkit_gb300 import build
+    from mvkit_gb300 import workloads as W
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    t0 = time.perf_counter()
+    wl = W.make_similarity_workload(**cfg["gen"])
+    t_gen = time.perf_counter() - t0
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    build.build()
+    mg.load()
+    mg.set_budgets(**cfg["budgets"])
+    t0 = time.perf_counter()
+    models = [mg.create_ncc_model(t, cfg["levels"], FULL_CIRCLE[0], FULL_CIRCLE[1], "auto", "use_polarity")
+              for t in wl.templates]
+    t_models = time.perf_counter() - t0
+    dev = mg.DeviceImage(wl.image)
+    pb = mg.PinnedBuffer(wl.image.shape, np.uint8)
+    pb.array[...] = wl.image
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    f = cfg["find"]
+    st = torch.cuda.Stream()
+
+    def step(img, subpixel="true"):
+        r, c, a, sc, m = mg.find_ncc_models(img, models, f[0], f[1], f[2], f[3], f[4], subpixel, f[6])
+        mr, mc = matcher_pose(r, c, a)
+        poses = np.stack([mr, mc, a, np.ones_like(a)], axis=1)
+        refined = poses.copy()
+        for k, model in enumerate(models):
+            if (m == k).any():
+                refined[m == k], _ = mg.ncc_refine_similarity(img, model, poses[m == k], iterations=40)
+        return poses, refined, m
+
+    def timed(img, events):
+        total, out = 0.0, None
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            w0 = time.perf_counter()
+            e0.record(st)
+            out = step(img)
+            e1.record(st)
+            torch.cuda.synchronize()
+            total += e0.elapsed_time(e1) if events else (time.perf_counter() - w0) * 1e3
+        return total, out
+
+    for _ in range(args.warmup):
+        step(dev)
+    step(pb.array)
+    with ClockSampler(local) as clocks:
+        dev_ms, (rigid, adjoint, m) = timed(dev, True)
+    host_ms, (rigid_h, adjoint_h, _) = timed(pb.array, False)
+    # the quadratic peak fit of the discrete (SubPixel "false") poses
+    r, c, a, _, md = mg.find_ncc_models(dev, models, f[0], f[1], f[2], f[3], f[4], "false", f[6])
+    mr, mc = matcher_pose(r, c, a)
+    discrete = np.stack([mr, mc, a, np.ones_like(a)], axis=1)
+    quad = discrete.copy()
+    for k, model in enumerate(models):
+        if (md == k).any():
+            quad[md == k], _ = mg.ncc_quadratic_peak_fit(dev, model, discrete[md == k],
+                                                         (1.0, 1.0, mg.get_ncc_model_params(model)[3], 0.02))
+    # stage profile of the finds (one per model) on this thread
+    mg.profile_reset()
+    mg.profile_enable(True)
+    for model in models:
+        mg.find_ncc_model(dev, model, f[0], f[1], f[2], f[3][0], f[4], "true", f[6])
+    mg.profile_enable(False)
+    prof = mg.profile_read()
+    if rank != 0:
+        return
+    pk = peaks()
+    tc = prof.get("track_tc", {"ms": 0.0, "work": 0.0, "launches": 0})
+    ach = 2.0 * tc["work"] / (tc["ms"] / 1e3) / 1e12 if tc["ms"] else None
+    value = replica_value(args.steps, world, dev_ms)
+    line = {
+        "metric": METRIC, "value": value, "unit": "images/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": args.workload, "image": f"{wl.image.shape[1]}x{wl.image.shape[0]} u8",
+                   "templates": [t.shape[0] for t in wl.templates], "poses": len(wl.poses),
+                   "controls": list(f), "num_levels": cfg["levels"], "budgets": cfg["budgets"],
+                   "mode": "extended (the reference's budgets lifted)",
+                   "step": "FindNccModels (rigid Gauss-Newton) + adjoint Gauss-Newton on (row, column, angle, "
+                           "scale) of every match, 40 iterations at most",
+                   "l2": "flushed (256 MiB write) between steps", "generation_s": round(t_gen, 1),
+                   "model_build_s": round(t_models, 2)},
+        "e2e": {"value": replica_value(args.steps, world, host_ms), "unit": "images/s",
+                "h2d_bytes_per_step": int(2 * wl.image.nbytes),
+                "d2h_bytes_per_step": int(len(rigid) * 8 * 9),
+                "api": "find_ncc_models and ncc_refine_similarity on the page-locked host image (each call "
+                       "uploads it); wall clock per step"},
+        "roofline": {"bound": "tensor", "achieved": ach, "peak": pk["tflops_sustained"], "unit": "TFLOP/s",
+                     "frac": ach / pk["tflops_sustained"] if ach else None, "traffic": None,
+                     "kernel": "tc_track_kernel", "ms_per_launch": tc["ms"] / max(1, tc["launches"]),
+                     "note": "profiled pass: one find per model on one stream"},
+        "gpu_launches": int(sum(v["launches"] for v in prof.values() if isinstance(v, dict)) * args.steps),
+        "clocks": clocks.summary(),
+        "pose_error": {"rigid_gauss_newton": similarity_errors(rigid, m, wl.poses),
+                       "quadratic_peak_fit": similarity_errors(quad, md, wl.poses),
+                       "adjoint_gauss_newton": similarity_errors(adjoint, m, wl.poses),
+                       "e2e_equals_value_pass": bool(np.array_equal(adjoint_h, adjoint))},
+    }
+    if not args.no_cpu_baseline:
+        import oracle_lib
+        b = cfg["budgets"]
+        oracle_lib.set_oracle_budgets(b["samples"], b["pixels"], b["candidates"])
+        orc = oracle_lib.oracle()
+        crop = np.ascontiguousarray(wl.image[:1280, :1280])
+        om = orc.create(wl.templates[0], levels=cfg["levels"], angle_start=FULL_CIRCLE[0],
+                        angle_extent=FULL_CIRCLE[1])
+        t0 = time.perf_counter()
+        n = len(orc.find(om, crop, f[0], f[1], f[2], f[3][0], f[4], True, f[6], 1))
+        dt = time.perf_counter() - t0
+        oracle_lib.set_oracle_budgets()
+        share = crop.size / wl.image.size / len(models)  # of one step's work, by pixels and models
+        line["cpu_baseline"] = {"value": share / dt, "unit": "images/s", "cores": 1, "kind": "port",
+                                "sample": f"the FP64 oracle's rigid find of the {wl.templates[0].shape[0]}^2 model "
+                                          f"on a 1280x1280 crop of the scene ({n} matches, {dt:.1f} s), scaled to "
+                                          f"a whole image and {len(models)} models by pixels x models",
+                                "seconds": dt}
+    print(json.dumps(line), flush=True)
 
 
 def config_cpu_baseline(cfg, scenes_, templates) -> dict:

@@ -584,6 +584,37 @@ def ncc_score_gradient(image, model: NccModel, poses, stream=None):
     return score, grad
 
 
+def ncc_quadratic_peak_fit(image, model: NccModel, poses, steps, stream=None):
+    """Quadratic peak fitting of similarity poses (row, column, angle, scale),
+    the plain form of sub-sample pose estimation kept beside the Gauss-Newton
+    refinements: per degree of freedom a parabola through the NCC at the pose
+    and at pose -/+ step (the scores of ncc_score_gradient, on the GPU); the
+    vertex offset, clipped to one step, moves that degree of freedom.  The
+    four fits are separable (each from the unmoved pose).  steps: (row,
+    column, angle, scale) sampling steps, e.g. (1, 1, the model's angle step,
+    0.02).  Returns (fitted poses (n, 4), score at them (n,))."""
+    p = np.array(np.asarray(poses, dtype=np.float64).reshape(-1, 4), copy=True)
+    n = p.shape[0]
+    if n == 0:
+        return p, np.zeros(0)
+    steps = np.asarray(steps, dtype=np.float64).reshape(4)
+    probe = np.repeat(p[:, None, :], 9, axis=1)  # centre, then -/+ per DOF
+    for d in range(4):
+        probe[:, 1 + 2 * d, d] -= steps[d]
+        probe[:, 2 + 2 * d, d] += steps[d]
+    sc, _ = ncc_score_gradient(image, model, probe.reshape(-1, 4), stream=stream)
+    sc = sc.reshape(n, 9)
+    s0 = sc[:, 0]
+    for d in range(4):
+        sm, sp = sc[:, 1 + 2 * d], sc[:, 2 + 2 * d]
+        den = sm - 2 * s0 + sp
+        ok = np.isfinite(sm) & np.isfinite(sp) & np.isfinite(s0) & (den < 0)
+        off = np.where(ok, 0.5 * (sm - sp) / np.where(ok, den, -1.0), 0.0)
+        p[:, d] += np.clip(off, -1.0, 1.0) * steps[d]
+    score, _ = ncc_score_gradient(image, model, p, stream=stream)
+    return p, score
+
+
 def ncc_refine_similarity(image, model: NccModel, poses, iterations: int = 20, stream=None):
     """Gauss-Newton refinement of similarity poses (row, column, angle,
     scale) on the NCC of ncc_score_gradient.  Returns (refined poses (n, 4),

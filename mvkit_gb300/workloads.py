@@ -273,6 +273,130 @@ def make_multi_workload(seed: int, height: int, width: int, tsizes: tuple, n_pos
     return MultiWorkload(image=image, templates=[t.astype(dtype) for t in templates], poses=poses, maxval=maxval)
 
 
+@dataclass
+class SimilarityPose:
+    row: float
+    column: float
+    angle: float
+    scale: float
+    model: int
+
+
+@dataclass
+class SimilarityWorkload:
+    image: np.ndarray
+    templates: list              # square uint8 templates, one per model
+    poses: list                  # SimilarityPose (template centre, angle, scale, template index)
+
+
+def paste_similarity(img: np.ndarray, patch: np.ndarray, row: float, col: float, angle: float, scale: float) -> None:
+    """Bilinear FP64 paste of a square patch at a similarity pose, in place:
+    the patch offset (dr, dc) from its centre lands at row + s (cos dr -
+    sin dc), col + s (sin dr + cos dc) (the matcher's pose convention with a
+    scale factor)."""
+    t = patch.shape[0]
+    o = (t - 1) / 2.0
+    ca, sa = math.cos(angle), math.sin(angle)
+    reach = int(math.ceil(scale * t * 0.75)) + 2
+    r0, c0 = max(0, int(row) - reach), max(0, int(col) - reach)
+    r1, c1 = min(img.shape[0], int(row) + reach + 1), min(img.shape[1], int(col) + reach + 1)
+    if r0 >= r1 or c0 >= c1:
+        return
+    dy = np.arange(r0, r1, dtype=np.float64)[:, None] - row
+    dx = np.arange(c0, c1, dtype=np.float64)[None, :] - col
+    tr = (ca * dy + sa * dx) / scale + o
+    tc = (-sa * dy + ca * dx) / scale + o
+    inside = (tr >= 0) & (tc >= 0) & (tr <= t - 1) & (tc <= t - 1)
+    ir = np.clip(np.floor(tr).astype(np.int64), 0, t - 1)
+    ic = np.clip(np.floor(tc).astype(np.int64), 0, t - 1)
+    ir1, ic1 = np.minimum(ir + 1, t - 1), np.minimum(ic + 1, t - 1)
+    fr, fc = tr - np.floor(tr), tc - np.floor(tc)
+    f = patch.astype(np.float64)
+    v = (1 - fr) * ((1 - fc) * f[ir, ic] + fc * f[ir, ic1]) + fr * ((1 - fc) * f[ir1, ic] + fc * f[ir1, ic1])
+    sub = img[r0:r1, c0:c1]
+    sub[inside] = np.floor(v[inside] + 0.5)
+
+
+def _square(row: float, col: float, angle: float, half: float):
+    """Corners (row, col) of a square of half side `half` rotated by `angle`
+    about (row, col), in the matcher's pose convention."""
+    ca, sa = math.cos(angle), math.sin(angle)
+    return [(row + ca * dr - sa * dc, col + sa * dr + ca * dc) for dr, dc in
+            ((-half, -half), (-half, half), (half, half), (half, -half))]
+
+
+def _squares_apart(a, b, gap: float) -> bool:
+    """True when two convex quadrilaterals are at least `gap` apart along
+    some edge normal (separating axis test)."""
+    for poly in (a, b):
+        for i in range(4):
+            (y0, x0), (y1, x1) = poly[i], poly[(i + 1) % 4]
+            ny, nx = x1 - x0, -(y1 - y0)
+            norm = math.hypot(ny, nx)
+            ny, nx = ny / norm, nx / norm
+            pa = [ny * y + nx * x for y, x in a]
+            pb = [ny * y + nx * x for y, x in b]
+            if max(pa) + gap <= min(pb) or max(pb) + gap <= min(pa):
+                return True
+    return False
+
+
+def make_similarity_workload(seed: int, height: int, width: int, tsizes: tuple, n_poses: int,
+                             scale_range: tuple = (0.95, 1.05), noise_sigma: int = 3) -> SimilarityWorkload:
+    """One uint8 scene holding `n_poses` pastes of the templates (template
+    n mod len(tsizes) for paste n) at similarity poses: subpixel row and
+    column, angle U[0, 2 pi), scale U[scale_range]; the rotated template
+    squares do not overlap (2 px apart).  Each paste first lays the texture
+    around its template (a patch 1.5 x the template, cropped from the same
+    source scene around the same centre), as an object in a real scene has;
+    then every template square is pasted over it, so no surround covers
+    another paste's template."""
+    rng = np.random.default_rng([seed, 11])
+    templates, patches = [], []
+    for k, ts in enumerate(tsizes):
+        src = scene(seed * 7919 + 31 * k + 7, 2 * ts + 16, 2 * ts + 16, shapes=10)
+        ps = ts + 2 * (ts // 4)
+        y0 = (src.shape[0] - ps) // 2
+        patch = src[y0:y0 + ps, y0:y0 + ps]
+        m = ts // 4
+        patches.append(patch)
+        templates.append(np.clip(patch[m:m + ts, m:m + ts], 0, 255).astype(np.uint8))
+    img = scene(seed, height, width).astype(np.float64)
+    # larger templates are placed first (the packing is dense)
+    order = sorted(range(n_poses), key=lambda n: -tsizes[n % len(tsizes)])
+    placed = {}
+    squares = []  # (row, col, reach, corners)
+    for n in order:
+        k = n % len(tsizes)
+        tries = 0
+        while True:
+            tries += 1
+            if tries > 100000:
+                raise ValueError("cannot place the requested poses without overlap")
+            s = scale_range[0] + float(rng.integers(0, 1 << 20)) / (1 << 20) * (scale_range[1] - scale_range[0])
+            half = s * tsizes[k] / 2
+            margin = half * 1.5 * math.sqrt(2) + 4
+            row = margin + float(rng.integers(0, 1 << 20)) / (1 << 20) * (height - 1 - 2 * margin)
+            col = margin + float(rng.integers(0, 1 << 20)) / (1 << 20) * (width - 1 - 2 * margin)
+            ang = float(rng.integers(0, 1 << 20)) / (1 << 20) * 2 * math.pi - math.pi
+            sq = _square(row, col, ang, half)
+            reach = half * math.sqrt(2)
+            if all(math.hypot(row - r, col - c) > reach + q + 2 or _squares_apart(sq, corners, 2.0)
+                   for r, c, q, corners in squares):
+                squares.append((row, col, reach, sq))
+                placed[n] = SimilarityPose(row, col, ang, s, k)
+                break
+    poses = [placed[n] for n in range(n_poses)]
+    for p in poses:
+        paste_similarity(img, patches[p.model], p.row, p.column, p.angle, p.scale)
+    for p in poses:
+        paste_similarity(img, templates[p.model], p.row, p.column, p.angle, p.scale)
+    if noise_sigma:
+        img = img + _gauss_int(rng, img.shape, noise_sigma)
+    image = np.clip(img, 0, 255).astype(np.uint8)
+    return SimilarityWorkload(image=image, templates=templates, poses=poses)
+
+
 # Named workloads.  "find_640x480_t64" is the CPU-runnable case; "find_2048_t128_5x"
 # is the single-GPU throughput case.
 CONFIGS = {
