@@ -1935,18 +1935,28 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     check(launch_rects(ws.sorted.p, ws.aux.p, st, geom, cap, s), "rects");
     check(launch_select(se, s), "select");
   }
+  // A round that accepts nothing (the candidates fail refinement or overlap)
+  // makes the next speculative batch the widest (64): fewer host round trips
+  // while a quota is far from met.  The matches do not depend on the batch:
+  // each candidate's refinement is its own, and the selection takes them in
+  // rank order.
+  int prepared = batch_limit;  // batch bound of the last select launched
+  int accepted = 0;
   for (int round = 0; round < 100000; ++round) {
     {
       Span sp(kStRefine, s);
-      check(launch_refine(ra, batch_limit, s), "refine");
+      check(launch_refine(ra, prepared, s), "refine");
     }
     {
       Span sp(kStSelect, s);
       check(launch_select(se, s), "select");
     }
+    prepared = se.batch_limit;
     check(cudaMemcpyAsync(ws.h_state, st, sizeof(QueryState), cudaMemcpyDeviceToHost, s), "state");
     check(cudaStreamSynchronize(s), "find");
     if (ws.h_state->done || !ws.h_state->need) break;
+    se.batch_limit = ws.h_state->accepted > accepted ? batch_limit : 64;
+    accepted = ws.h_state->accepted;
   }
   const QueryState hs = *ws.h_state;
   t_prof.collect();
