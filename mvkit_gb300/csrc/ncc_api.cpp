@@ -351,16 +351,18 @@ double half_value(uint16_t b) {
   return double(h);
 }
 
-// fp16 planes of level t: the level minus `offset` is an exact fp16 integer
-// (parts 1), or 64 x an exact high part plus a low part in [0, 64) (parts
-// 2); 0 when neither holds (the CUDA-core path scores that level).
+// fp16 planes of level t: the level minus `offset` as base-64 digits, each
+// an exact fp16 integer: the first signed (|d| <= 2048), the others in
+// [0, 64) (parts 1: the value itself; 2: 64 h + l; up to 4 for uint16
+// level sums); 0 when even four parts do not hold it (the CUDA-core path
+// scores that level).
 int tc_parts(int type, size_t t, float* offset) {
   const double maxv = (type == 1 ? 65535.0 : 255.0) * std::ldexp(1., int(2 * t));
   const double off = std::floor((maxv + 1) * .5);
   *offset = float(off);
   const double range = std::max(off, maxv - off);
-  if (range <= 2048.0) return 1;
-  if (range <= 2048.0 * 64.0) return 2;
+  for (int parts = 1; parts <= kTcMaxParts; ++parts)
+    if (range <= 2048.0 * std::ldexp(1.0, 6 * (parts - 1))) return parts;
   return 0;
 }
 
@@ -566,7 +568,7 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
     }
     // weight scale: a power of two keeping the weights (x 64 for a split
     // level) and the centring row sums (x 64 likewise) within fp16 range
-    const double m64 = parts == 2 ? 64.0 : 1.0;
+    const double m64 = std::ldexp(1.0, 6 * (parts - 1));  // multiplier of the first part
     const double limit = std::min(maxw > 0 ? 16384.0 / (maxw * m64) : 1e30, maxrow > 0 ? 16384.0 / (maxrow * m64) : 1e30);
     const double sigma = limit < 1e30 ? std::ldexp(1., int(std::floor(std::log2(limit)))) : 1.0;
     const int rg = pr.rg, chunks = (pr.kr + rg - 1) / rg;
@@ -609,7 +611,7 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
         for (int dc = 0; dc < 5; ++dc) {
           const int x = col - pr.cmin + dc;
           for (int part = 0; part < parts; ++part) {
-            const double mult = (parts == 2 && part == 0) ? 64.0 : 1.0;
+            const double mult = std::ldexp(1.0, 6 * (parts - 1 - part));
             const int k = part * pr.kw + x;
             for (int half = 0; half < 2; ++half)
               host[at(y, q, dc, half, k)] = half_bits((half ? lv : hv) * mult);
@@ -625,17 +627,13 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
           const uint16_t f1 = half_bits(r);
           const uint16_t f2 = half_bits(r - half_value(f1));
           ecorr += half_value(f1) + half_value(f2);
-          for (int dc = 0; dc < 5; ++dc) {
-            if (parts == 2) {
-              host[at(y, q, dc, half, kc0)] = half_bits(64.0 * half_value(f1));
-              host[at(y, q, dc, half, kc0 + 1)] = half_bits(64.0 * half_value(f2));
-              host[at(y, q, dc, half, kc0 + 2)] = f1;
-              host[at(y, q, dc, half, kc0 + 3)] = f2;
-            } else {
-              host[at(y, q, dc, half, kc0)] = f1;
-              host[at(y, q, dc, half, kc0 + 1)] = f2;
+          // part q of the centre meets 64^(parts - 1 - q) x the row sum
+          for (int dc = 0; dc < 5; ++dc)
+            for (int part = 0; part < parts; ++part) {
+              const double mult = std::ldexp(1.0, 6 * (parts - 1 - part));
+              host[at(y, q, dc, half, kc0 + 2 * part)] = half_bits(mult * half_value(f1));
+              host[at(y, q, dc, half, kc0 + 2 * part + 1)] = half_bits(mult * half_value(f2));
             }
-          }
         }
       g.ecorr[q] = float(ecorr / sigma);
       g.k_of[q] = pr.ks[size_t(q)];
@@ -753,6 +751,8 @@ Workspace& workspace() {
 void init_state(Workspace& ws, cudaStream_t s, int cap) {
   *ws.h_state = QueryState{};
   ws.h_state->cap = cap;
+  ws.h_state->pix_min = std::numeric_limits<int32_t>::max();
+  ws.h_state->pix_max = std::numeric_limits<int32_t>::min();
   check(cudaMemcpyAsync(ws.state.p, ws.h_state, sizeof(QueryState), cudaMemcpyHostToDevice, s), "state");
 }
 
@@ -1513,6 +1513,9 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
                           pairs0 ? ws.pairs.p : nullptr),
           "pyramid0");
     for (size_t l = 1; l < level_count; ++l) check(launch_pyramid(lev[l - 1], lev[l], err_flag, s), "pyramid");
+    // uint16: the tensor-core planes are centred on the data's own range
+    // (a 12-bit image sits far below the type's mid-range)
+    if (type == 1) check(launch_level_range(lev[0], st, s), "level range");
   }
   const size_t first_target = std::max(finest, size_t(opt.subpixel ? 1 : 0));
   for (size_t l = 0; l < level_count; ++l) {
@@ -1569,6 +1572,8 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     tca.sets = P.sets;
     tca.npad = P.npad;
     tca.plane_offset = P.offset;
+    tca.dyn_offset = type == 1;
+    tca.level_mult = float(std::ldexp(1., int(2 * top)));
     tca.planes = ws.tc_planes.p;
     tca.plane_pitch = pitch;
     tca.rc = ws.coarse_rc.p;
@@ -1576,7 +1581,9 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     tca.withhold_weights = t_withhold_weights;
     {
       Span spp(kStTcPrep, s, 2);
-      check(launch_tc_planes(lev[top], ws.tc_planes.p, pitch, P.parts, P.offset, s), "tc planes");
+      check(launch_tc_planes(lev[top], ws.tc_planes.p, pitch, P.parts, P.offset, s, type == 1 ? st : nullptr,
+                             tca.level_mult),
+            "tc planes");
       check(launch_coarse_lattice(ws.coarse_cand.p, ws.coarse_rc.p, coarse_nsrc, lat_r, lat_c, d_co_gsrc,
                                   ws.tc_order.p, ws.tc_tiles.p, st, slot_c, s),
             "coarse lattice");
@@ -1730,6 +1737,8 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
         tca.sets = P.sets;
         tca.npad = P.npad;
         tca.plane_offset = P.offset;
+        tca.dyn_offset = type == 1;
+        tca.level_mult = float(std::ldexp(1., int(2 * t)));
         tca.planes = ws.tc_planes.p;
         tca.plane_pitch = pitch;
         tca.rc = nullptr;
@@ -1737,7 +1746,9 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
         tca.withhold_weights = t_withhold_weights;
         {
           Span spp(kStTcPrep, s, 4);
-          check(launch_tc_planes(lev[t], ws.tc_planes.p, pitch, P.parts, P.offset, s), "tc planes");
+          check(launch_tc_planes(lev[t], ws.tc_planes.p, pitch, P.parts, P.offset, s, type == 1 ? st : nullptr,
+                                 tca.level_mult),
+                "tc planes");
           check(launch_tc_group(tca, ng, ws.tc_counts.p, ws.tc_offsets.p, ws.tc_cursor.p, cap, s),
                 "tc group");
         }

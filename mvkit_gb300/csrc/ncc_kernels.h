@@ -143,6 +143,7 @@ constexpr int kTcMaxGroups = 4096;       // groups of one tracking step
 constexpr int kTcMaxTiles = kMaxCandidatesExt / kTcCands + kTcMaxGroups + 1;
 constexpr int kTcMaxStages = 16;         // weight-chunk buffers
 constexpr int kTcPlaneShifts = 8;        // column-shifted copies of a level plane
+constexpr int kTcMaxParts = 4;           // fp16 parts of a level value (base-64 digits)
 constexpr int kTcPlaneMargin = 8;        // plane columns left of the level
 constexpr int kTcBlocksPerSm = 1;        // resident tensor-core blocks per SM (512 / this TMEM columns each)
 
@@ -150,7 +151,7 @@ struct TcGroup {
   const uint8_t* b;                      // ceil(kr / rg) chunks: N x K fp16 weights, canonical K-major
   long long macs;                        // algorithmic MACs per candidate (25 x samples of all patches)
   int kr, kw;                            // grid rows; window columns per part (multiple of 16)
-  int parts;                             // planes per value: 1, or 2 (64 x high part, low part)
+  int parts;                             // planes per value (1..4): base-64 digits, the first signed
   int rmin, cmin;                        // grid origin relative to the placement centre
   int p, rg, n;                          // patches; grid rows per chunk (N columns side by side);
                                          // MMA N (10 p rg rounded up to 16)
@@ -186,7 +187,10 @@ struct TcArgs {
   int stages;                            // weight-chunk buffers in use
   int stage_bytes, abuf_bytes;           // bytes per weight buffer / per window buffer
   int sets, npad;                        // accumulator sets (grid row y -> set y mod sets), columns per set
-  float plane_offset;                    // level value subtracted in the planes
+  float plane_offset;                    // level value subtracted in the planes (dyn_offset 0)
+  int dyn_offset;                        // 1: the offset is the mid-range of the level's values,
+                                         // level_mult x (pix_min + pix_max) / 2 from the state
+  float level_mult;                      // 4^level (pixels summed into a level value)
   const uint16_t* planes;                // fp16 planes (launch_tc_planes)
   int plane_pitch;                       // elements per plane row
   const int2* rc;                        // candidate lattice positions given directly (nullable)
@@ -210,7 +214,19 @@ struct TcLaunch {
 // copies (plane d holds level column x - kTcPlaneMargin + d at x), `pitch`
 // elements per row (a multiple of 8, at least the level width + 8).
 cudaError_t launch_tc_planes(const LevelImage& lev, uint16_t* planes, int pitch, int parts, float offset,
-                             cudaStream_t s);
+                             cudaStream_t s, const QueryState* state = nullptr, float level_mult = 1.f);
+// Range of the level-0 crop into state->pix_min / pix_max (uint16 finds).
+cudaError_t launch_level_range(const LevelImage& lev0, QueryState* state, cudaStream_t s);
+#ifdef __CUDACC__
+// Offset of the fp16 planes of a level: fixed, or (state given) the
+// mid-range of the level's values, floor(mult (min + max) / 2) of the level-0
+// range; exact in float (below 2^24).
+__device__ __forceinline__ float tc_plane_offset(float fixed, const QueryState* state, float mult) {
+  if (!state) return fixed;
+  const long long s = (long long)(state->pix_min + state->pix_max) * (long long)mult;
+  return float(s >> 1);
+}
+#endif
 size_t tc_kernel_static_smem();
 // Groups the step's candidates into tiles (counts, tile list, order).
 cudaError_t launch_tc_group(const TcArgs& a, int ngroups, int32_t* counts, int32_t* offsets, int32_t* cursor,

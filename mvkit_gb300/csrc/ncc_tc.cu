@@ -257,7 +257,7 @@ __device__ void tc_window_role(const TcArgs& a, TcShared& sh, uint8_t* abase, in
   const size_t plane = size_t(H) * size_t(pitch);
   const int lane = pt & 31, wp = pt >> 5;
   const int rblocks = rows / 8;
-  const size_t part_stride = size_t(kTcPlaneShifts) * plane;  // high plane -> low plane
+  const size_t part_stride = size_t(kTcPlaneShifts) * plane;  // one part's planes -> the next part's
   for (int sl = 0; sl < sp.nslabs; ++sl) {
     const int buf = sa & 1;
     if (sa >= 2 && !bar_wait(&sh.slab_done[buf], uint32_t(((sa >> 1) - 1) & 1))) {
@@ -277,10 +277,10 @@ __device__ void tc_window_role(const TcArgs& a, TcShared& sh, uint8_t* abase, in
         const int row = row0 + rb * 8;
         const bool rok = row >= 0 && row < H;
         for (int sg = lane >> 3; sg < sp.nplane; sg += 4) {
-          const int q = sg >= sp.segs ? 1 : 0;
+          const int q = sg / sp.segs;  // part of the level value
           const int x = x0 + 8 * (sg - q * sp.segs);
           const bool valid = rok && x >= 0 && x + 8 <= pitch;
-          const uint16_t* src = pbase + (q ? part_stride : 0) + (valid ? size_t(row) * pitch + x : 0);
+          const uint16_t* src = pbase + size_t(q) * part_stride + (valid ? size_t(row) * pitch + x : 0);
           cp_async16(dg + size_t(sg) * sp.lbo + size_t(rb) * 128, src, valid);
         }
       }
@@ -412,7 +412,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         sh.R[t] = R;
         sh.C[t] = C;
         const int cr = min(max(R, 0), a.lev.h - 1), cc = min(max(C, 0), a.lev.w - 1);
-        sh.centre[t] = a.lev.v[size_t(cr) * a.lev.w + cc] - a.plane_offset;
+        sh.centre[t] = a.lev.v[size_t(cr) * a.lev.w + cc] -
+                       tc_plane_offset(a.plane_offset, a.dyn_offset ? a.state : nullptr, a.level_mult);
         const int x0 = C - 2 + a.groups[gi].cmin;
         sh.x0a[t] = x0 & ~7;  // floor to a multiple of 8 (16-byte TMA start)
         sh.delta[t] = x0 - (x0 & ~7);
@@ -420,23 +421,30 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     __syncthreads();
     {
-      // centring columns of every staged row of both window buffers: (-c, -c)
-      // for one plane, (-c_high, -c_high, -c_low, -c_low) for a split value,
-      // c = 64 c_high + c_low
+      // centring columns of every staged row of both window buffers: the
+      // centre c split like the planes, c = sum_q c_q 64^(parts - 1 - q), as
+      // the pairs (-c_q, -c_q), q = 0 .. parts - 1, then zeros
       const TcGroup& G = sh.grp;
       const TcShape sp(G);
       const int rows = G.rows_slab;
       for (int it = t; it < 2 * kTcCands * rows; it += kTcThreads) {
         const int buf = it / (kTcCands * rows), g = (it / rows) % kTcCands, r = it % rows;
         const float c = g < sh.cnt ? sh.centre[g] : 0.f;
-        const float ch = G.parts == 2 ? floorf(c * (1.f / 64.f)) : c;
-        const float cl = G.parts == 2 ? c - 64.f * ch : 0.f;
-        const __half2 h = __floats2half2_rn(-ch, -ch), l = __floats2half2_rn(-cl, -cl);
+        uint32_t w[kTcMaxParts] = {};
+        float rem = c, unit = 1.f;
+        for (int q = 1; q < G.parts; ++q) unit *= 64.f;
+        for (int q = 0; q < G.parts; ++q) {
+          const float dq = q + 1 < G.parts ? floorf(rem / unit) : rem;
+          const __half2 h = __floats2half2_rn(-dq, -dq);
+          w[q] = *reinterpret_cast<const uint32_t*>(&h);
+          rem -= dq * unit;
+          unit *= (1.f / 64.f);
+        }
         uint4 v;
-        v.x = *reinterpret_cast<const uint32_t*>(&h);
-        v.y = *reinterpret_cast<const uint32_t*>(&l);
-        v.z = 0;
-        v.w = 0;
+        v.x = w[0];
+        v.y = w[1];
+        v.z = w[2];
+        v.w = w[3];
         uint8_t* row = abase + size_t(buf) * a.abuf_bytes + size_t(g) * sp.sbo + size_t(sp.nplane) * sp.lbo +
                        size_t(r) * 16;
         *reinterpret_cast<uint4*>(row) = v;
@@ -505,6 +513,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     // one output per thread, consecutive threads on consecutive dots of a
     // candidate ([selected patch][row placement][column placement])
     const int per = 25 * G.p;
+    const float poff = tc_plane_offset(a.plane_offset, a.dyn_offset ? a.state : nullptr, a.level_mult);
     for (int it = t; it < sh.cnt * per; it += kTcThreads) {
       const int g = it / per, e = it - g * per;
       const int q = e / 25, pos = e - q * 25, dr = pos / 5, dc = pos - dr * 5;
@@ -519,7 +528,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       // sum w S = sum w (S' - c) + c ecorr + offset weff (S' = S - offset);
       // the consumers subtract S0 weff (first sample S0) themselves
       a.dots[size_t(sh.ci[g]) * kTcScoreStride + size_t(G.k_of[q]) * 25 + pos] =
-          sum * G.inv_scale + (sh.centre[g] * G.ecorr[q] + a.plane_offset * G.weff[q]);
+          sum * G.inv_scale + (sh.centre[g] * G.ecorr[q] + poff * G.weff[q]);
     }
     if (t == 0) {
       atomicAdd(&a.state_rw->tc_macs, (unsigned long long)G.macs * (unsigned long long)sh.cnt);
@@ -537,7 +546,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
 // fp16 planes: thread = 8 consecutive columns of one (shift, row); plane d
 // holds level column x - kTcPlaneMargin + d at column x
-__global__ void tc_planes_kernel(LevelImage lev, __half* planes, int pitch, int parts, float offset) {
+__global__ void tc_planes_kernel(LevelImage lev, __half* planes, int pitch, int parts, float fixed_offset,
+                                 const QueryState* state, float level_mult) {
+  const float offset = tc_plane_offset(fixed_offset, state, level_mult);
   const int groups = pitch / 8;
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long total = (long long)kTcPlaneShifts * lev.h * groups;
@@ -545,25 +556,28 @@ __global__ void tc_planes_kernel(LevelImage lev, __half* planes, int pitch, int 
   const int gx = int(idx % groups);
   const int y = int((idx / groups) % lev.h);
   const int d = int(idx / ((long long)groups * lev.h));
-  __align__(16) __half hv[8];
-  __align__(16) __half lv[8];
+  __align__(16) __half pv[kTcMaxParts][8];
 #pragma unroll
   for (int e = 0; e < 8; ++e) {
     const int x = gx * 8 + e + d - kTcPlaneMargin;
     const float v = x >= 0 && x < lev.w ? lev.v[size_t(y) * lev.w + x] - offset : 0.f;
-    if (parts == 2) {
-      const float h = floorf(v * (1.f / 64.f));
-      hv[e] = __float2half_rn(h);
-      lv[e] = __float2half_rn(v - 64.f * h);
-    } else {
-      hv[e] = __float2half_rn(v);
+    // v = sum_q digit_q 64^(parts - 1 - q): the first digit signed, the
+    // others in [0, 64); every step is exact in float (|v| < 2^24)
+    float r = v;
+    float unit = 1.f;
+    for (int q = 1; q < parts; ++q) unit *= 64.f;
+    for (int q = 0; q < parts; ++q) {
+      const float dq = q + 1 < parts ? floorf(r / unit) : r;
+      pv[q][e] = __float2half_rn(dq);
+      r -= dq * unit;
+      unit *= (1.f / 64.f);
     }
   }
   const size_t plane = size_t(lev.h) * pitch;
   const size_t at = (size_t(d) * lev.h + y) * pitch + size_t(gx) * 8;
-  *reinterpret_cast<uint4*>(planes + at) = *reinterpret_cast<const uint4*>(hv);
-  if (parts == 2)
-    *reinterpret_cast<uint4*>(planes + size_t(kTcPlaneShifts) * plane + at) = *reinterpret_cast<const uint4*>(lv);
+  for (int q = 0; q < parts; ++q)
+    *reinterpret_cast<uint4*>(planes + size_t(q) * kTcPlaneShifts * plane + at) =
+        *reinterpret_cast<const uint4*>(pv[q]);
 }
 
 // Grouping of the step's candidates: counts per group, tile list, order.
@@ -632,10 +646,37 @@ __global__ void tc_scatter_kernel(const Cand* in, const QueryState* state, int s
 size_t tc_kernel_static_smem() { return sizeof(TcShared); }
 
 cudaError_t launch_tc_planes(const LevelImage& lev, uint16_t* planes, int pitch, int parts, float offset,
-                             cudaStream_t s) {
+                             cudaStream_t s, const QueryState* state, float level_mult) {
   const long long total = (long long)kTcPlaneShifts * lev.h * (pitch / 8);
   const unsigned blocks = unsigned((total + 255) / 256);
-  tc_planes_kernel<<<blocks, 256, 0, s>>>(lev, reinterpret_cast<__half*>(planes), pitch, parts, offset);
+  tc_planes_kernel<<<blocks, 256, 0, s>>>(lev, reinterpret_cast<__half*>(planes), pitch, parts, offset, state,
+                                          level_mult);
+  return cudaGetLastError();
+}
+
+namespace {
+// min / max of a level (exact integers held as float), grid-stride
+__global__ void level_range_kernel(LevelImage lev, QueryState* state) {
+  const size_t n = size_t(lev.w) * size_t(lev.h);
+  float mn = INFINITY, mx = -INFINITY;
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
+    const float v = lev.v[i];
+    mn = fminf(mn, v);
+    mx = fmaxf(mx, v);
+  }
+  for (int o = 16; o; o >>= 1) {
+    mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  if ((threadIdx.x & 31) == 0 && mn <= mx) {
+    atomicMin(&state->pix_min, int(mn));
+    atomicMax(&state->pix_max, int(mx));
+  }
+}
+}  // namespace
+
+cudaError_t launch_level_range(const LevelImage& lev0, QueryState* state, cudaStream_t s) {
+  level_range_kernel<<<608, 256, 0, s>>>(lev0, state);
   return cudaGetLastError();
 }
 

@@ -102,6 +102,7 @@ struct QueryState {
   int32_t done;
   int32_t batch_count;             // entries in the refinement batch
   int32_t cap;                     // candidate budget of the find (list buffers hold this many)
+  int32_t pix_min, pix_max;        // range of the level-0 crop (uint16 finds: tensor-core plane offsets)
   unsigned long long track_macs;   // algorithmic MACs of the CUDA-core tracking (25 positions x samples per patch)
   unsigned long long tc_macs;      // algorithmic MACs of the tensor-core tracking
   unsigned long long tc_issued;    // MACs issued to the tensor cores (M x N x K per MMA)

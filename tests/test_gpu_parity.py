@@ -331,6 +331,35 @@ def test_tensor_core_tracking_runs(mg):
     assert launches["tensor"] > 0 and launches["plain"] == 0, launches
 
 
+@pytest.mark.parametrize("maxval", [4095, 65535])
+def test_uint16_levels_on_tensor_cores(mg, orc, maxval):
+    """uint16 level sums need three or four fp16 parts above level 1: the
+    coarse scan (level 3) and both tracking steps (levels 2 and 1) run on the
+    tensor cores (three track_tc launches per find), and the candidates after
+    every stage and the final matches equal the oracle's."""
+    from mvkit_gb300 import workloads as W
+    wl = W.make_workload(81, 600, 800, 64, 3, angle_range=(-math.radians(20), math.radians(20)), maxval=maxval,
+                         noise_sigma=20)
+    a0, ext = -math.radians(20), math.radians(40)
+    model = mg.create_ncc_model(wl.template, 4, a0, ext, "auto", "use_polarity")
+    om = orc.create(wl.template, levels=4, angle_start=a0, angle_extent=ext)
+    ctl = (a0, ext, 0.7, 3, 0.5, "true", 4)
+    mg.set_correlation_path("tensor")
+    mg.profile_enable(True)
+    mg.profile_reset()
+    got = mg.find_ncc_model(wl.image, model, *ctl)
+    prof = mg.profile_read()
+    mg.profile_enable(False)
+    assert prof["track_tc"]["launches"] == 3 and prof["track_tc"]["work"] > 0, prof["track_tc"]
+    want = orc.find(om, wl.image, a0, ext, 0.7, 3, 0.5, True, 4, 1)
+    assert len(want) == 3
+    assert_same_matches(got, want, f"uint16 max {maxval}")
+    for stage in (0, 1, 2):
+        w = orc.find(om, wl.image, a0, ext, 0.7, 3, 0.5, True, 4, 1, stage=stage)
+        g = mg.find_ncc_model_stage(wl.image, model, *ctl, stage=stage)
+        assert len(pose_set(g) ^ pose_set(w)) <= 2, f"stage {stage}"
+
+
 def test_device_resident_input_and_repeat_calls(mg):
     case = CASES["rot3_all"]
     wl, mask = make_inputs(case)
