@@ -320,26 +320,30 @@ __device__ void tc_weight_role(const TcArgs& a, TcShared& sh, uint8_t* wbase, Ri
 // weights, warps 2-5 stage windows, and all six warps run the set-up and the
 // epilogue.  Shared memory: weight ring (stages x stage_bytes) | two window
 // buffers, the same for every job of the launch.
+// Multi: a table of jobs in device memory, the current one copied to shared
+// memory per tile; otherwise the one job of the launch parameters (read
+// through the constant bank).
+template <bool Multi>
 __global__ void __launch_bounds__(kTcThreads, 1)
     tc_track_kernel(const __grid_constant__ TcLaunch L) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ TcShared sh;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  const TcArgs* jobs = L.jobs ? L.jobs : &L.single;
+  const TcArgs* jobs = Multi ? L.jobs : &L.single;
   // first launch tile of each job (the jobs' tile lists were planned on the device)
   if (t == 0) {
     int n = 0;
-    for (int j = 0; j < L.njobs; ++j) {
+    for (int j = 0; j < (Multi ? L.njobs : 1); ++j) {
       sh.job_base[j] = n;
       n += jobs[j].tiles->count;
     }
-    sh.job_base[L.njobs] = n;
+    sh.job_base[Multi ? L.njobs : 1] = n;
     sh.job_of = -1;
   }
   __syncthreads();
-  const int ntiles = sh.job_base[L.njobs];
+  const int ntiles = sh.job_base[Multi ? L.njobs : 1];
   if (int(blockIdx.x) >= ntiles) return;
-  const TcArgs& a = sh.job;
+  const TcArgs& a = Multi ? sh.job : L.single;
   // launch shape: equal for every job
   const int stages = jobs[0].stages, stage_bytes = jobs[0].stage_bytes;
   uint8_t* smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
@@ -374,14 +378,16 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   for (int gtile = blockIdx.x; gtile < ntiles; gtile = sh.next_tile) {
     // the tile's job into shared memory (when it changes)
     int jb = 0;
-    while (gtile >= sh.job_base[jb + 1]) ++jb;
-    if (jb != sh.job_of) {
-      __syncthreads();
-      const uint32_t* src = reinterpret_cast<const uint32_t*>(jobs + jb);
-      uint32_t* dst = reinterpret_cast<uint32_t*>(&sh.job);
-      for (int w = t; w < int(sizeof(TcArgs) / 4); w += kTcThreads) dst[w] = src[w];
-      __syncthreads();
-      if (t == 0) sh.job_of = jb;
+    if (Multi) {
+      while (gtile >= sh.job_base[jb + 1]) ++jb;
+      if (jb != sh.job_of) {
+        __syncthreads();
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(jobs + jb);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(&sh.job);
+        for (int w = t; w < int(sizeof(TcArgs) / 4); w += kTcThreads) dst[w] = src[w];
+        __syncthreads();
+        if (t == 0) sh.job_of = jb;
+      }
     }
     const int tile = gtile - sh.job_base[jb];
     // tile set-up: the group into shared memory, one candidate per thread
@@ -430,15 +436,17 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       for (int it = t; it < 2 * kTcCands * rows; it += kTcThreads) {
         const int buf = it / (kTcCands * rows), g = (it / rows) % kTcCands, r = it % rows;
         const float c = g < sh.cnt ? sh.centre[g] : 0.f;
-        uint32_t w[kTcMaxParts] = {};
-        float rem = c, unit = 1.f;
-        for (int q = 1; q < G.parts; ++q) unit *= 64.f;
-        for (int q = 0; q < G.parts; ++q) {
-          const float dq = q + 1 < G.parts ? floorf(rem / unit) : rem;
+        uint32_t w[kTcMaxParts];
+        float rem = c;
+#pragma unroll
+        for (int q = 0; q < kTcMaxParts; ++q) {
+          // digit q of parts: weight 64^(parts - 1 - q); none past the last
+          const int sh6 = 6 * (G.parts - 1 - q);
+          const float unit = sh6 >= 0 ? float(1 << max(sh6, 0)) : 0.f;
+          const float dq = q >= G.parts ? 0.f : q + 1 < G.parts ? floorf(rem * (1.f / unit)) : rem;
           const __half2 h = __floats2half2_rn(-dq, -dq);
-          w[q] = *reinterpret_cast<const uint32_t*>(&h);
+          w[q] = q < G.parts ? *reinterpret_cast<const uint32_t*>(&h) : 0u;
           rem -= dq * unit;
-          unit *= (1.f / 64.f);
         }
         uint4 v;
         v.x = w[0];
@@ -546,7 +554,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
 // fp16 planes: thread = 8 consecutive columns of one (shift, row); plane d
 // holds level column x - kTcPlaneMargin + d at column x
-__global__ void tc_planes_kernel(LevelImage lev, __half* planes, int pitch, int parts, float fixed_offset,
+template <int Parts>
+__global__ void tc_planes_kernel(LevelImage lev, __half* planes, int pitch, float fixed_offset,
                                  const QueryState* state, float level_mult) {
   const float offset = tc_plane_offset(fixed_offset, state, level_mult);
   const int groups = pitch / 8;
@@ -556,26 +565,26 @@ __global__ void tc_planes_kernel(LevelImage lev, __half* planes, int pitch, int 
   const int gx = int(idx % groups);
   const int y = int((idx / groups) % lev.h);
   const int d = int(idx / ((long long)groups * lev.h));
-  __align__(16) __half pv[kTcMaxParts][8];
+  __align__(16) __half pv[Parts][8];
 #pragma unroll
   for (int e = 0; e < 8; ++e) {
     const int x = gx * 8 + e + d - kTcPlaneMargin;
     const float v = x >= 0 && x < lev.w ? lev.v[size_t(y) * lev.w + x] - offset : 0.f;
-    // v = sum_q digit_q 64^(parts - 1 - q): the first digit signed, the
+    // v = sum_q digit_q 64^(Parts - 1 - q): the first digit signed, the
     // others in [0, 64); every step is exact in float (|v| < 2^24)
     float r = v;
-    float unit = 1.f;
-    for (int q = 1; q < parts; ++q) unit *= 64.f;
-    for (int q = 0; q < parts; ++q) {
-      const float dq = q + 1 < parts ? floorf(r / unit) : r;
+#pragma unroll
+    for (int q = 0; q < Parts; ++q) {
+      const float unit = float(1 << (6 * (Parts - 1 - q)));
+      const float dq = q + 1 < Parts ? floorf(r * (1.f / unit)) : r;
       pv[q][e] = __float2half_rn(dq);
       r -= dq * unit;
-      unit *= (1.f / 64.f);
     }
   }
   const size_t plane = size_t(lev.h) * pitch;
   const size_t at = (size_t(d) * lev.h + y) * pitch + size_t(gx) * 8;
-  for (int q = 0; q < parts; ++q)
+#pragma unroll
+  for (int q = 0; q < Parts; ++q)
     *reinterpret_cast<uint4*>(planes + size_t(q) * kTcPlaneShifts * plane + at) =
         *reinterpret_cast<const uint4*>(pv[q]);
 }
@@ -649,8 +658,14 @@ cudaError_t launch_tc_planes(const LevelImage& lev, uint16_t* planes, int pitch,
                              cudaStream_t s, const QueryState* state, float level_mult) {
   const long long total = (long long)kTcPlaneShifts * lev.h * (pitch / 8);
   const unsigned blocks = unsigned((total + 255) / 256);
-  tc_planes_kernel<<<blocks, 256, 0, s>>>(lev, reinterpret_cast<__half*>(planes), pitch, parts, offset, state,
-                                          level_mult);
+  __half* p = reinterpret_cast<__half*>(planes);
+  switch (parts) {
+    case 1: tc_planes_kernel<1><<<blocks, 256, 0, s>>>(lev, p, pitch, offset, state, level_mult); break;
+    case 2: tc_planes_kernel<2><<<blocks, 256, 0, s>>>(lev, p, pitch, offset, state, level_mult); break;
+    case 3: tc_planes_kernel<3><<<blocks, 256, 0, s>>>(lev, p, pitch, offset, state, level_mult); break;
+    case 4: tc_planes_kernel<4><<<blocks, 256, 0, s>>>(lev, p, pitch, offset, state, level_mult); break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 
@@ -692,9 +707,14 @@ cudaError_t launch_tc_group(const TcArgs& a, int ngroups, int32_t* counts, int32
 
 cudaError_t launch_tc_track(const TcLaunch& l, size_t smem, int grid, cudaStream_t s) {
   if (l.njobs < 1 || l.njobs > kTcMaxJobs) return cudaErrorInvalidValue;
-  if (cudaError_t e = reserve_dynamic_smem(reinterpret_cast<const void*>(tc_track_kernel), smem)) return e;
+  const void* fn = l.jobs ? reinterpret_cast<const void*>(tc_track_kernel<true>)
+                           : reinterpret_cast<const void*>(tc_track_kernel<false>);
+  if (cudaError_t e = reserve_dynamic_smem(fn, smem)) return e;
   if (cudaError_t e = cudaMemsetAsync(l.next, 0, sizeof(int), s)) return e;
-  tc_track_kernel<<<grid, kTcThreads, smem, s>>>(l);
+  if (l.jobs)
+    tc_track_kernel<true><<<grid, kTcThreads, smem, s>>>(l);
+  else
+    tc_track_kernel<false><<<grid, kTcThreads, smem, s>>>(l);
   return cudaGetLastError();
 }
 
