@@ -206,7 +206,8 @@ constexpr int kTcMaxJobs = 64;
 struct TcLaunch {
   const TcArgs* jobs;  // nullptr: the one job `single`
   int njobs;
-  int* next;           // tiles handed out after the first gridDim.x; zeroed by launch_tc_track
+  int* next;           // tiles handed out after the first gridDim.x; zero at launch (a job table's:
+                       // zeroed by launch_tc_track; a single job's: its tile list's, reset by the planner)
   TcArgs single;
 };
 

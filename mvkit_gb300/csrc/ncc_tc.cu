@@ -154,6 +154,7 @@ struct __align__(16) TcShared {
   int sm, sa;        // window slabs consumed (MMA thread) / staged (window producer)
   int ci[kTcCands], R[kTcCands], C[kTcCands], x0a[kTcCands], delta[kTcCands];
   float centre[kTcCands];  // window centre value minus the plane offset (exact integer)
+  uint4 cwords[kTcCands];  // its centring words: (-c_q, -c_q) half2 per digit q, then zeros
 };
 
 // Shape of one tile's operands.
@@ -420,6 +421,21 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const int cr = min(max(R, 0), a.lev.h - 1), cc = min(max(C, 0), a.lev.w - 1);
         sh.centre[t] = a.lev.v[size_t(cr) * a.lev.w + cc] -
                        tc_plane_offset(a.plane_offset, a.dyn_offset ? a.state : nullptr, a.level_mult);
+        // the centre split like the planes, c = sum_q c_q 64^(parts - 1 - q),
+        // as the pairs (-c_q, -c_q), q = 0 .. parts - 1, then zeros
+        const int parts = a.groups[gi].parts;
+        uint32_t wd[kTcMaxParts];
+        float rem = sh.centre[t];
+#pragma unroll
+        for (int q = 0; q < kTcMaxParts; ++q) {
+          const int sh6 = 6 * (parts - 1 - q);
+          const float unit = sh6 >= 0 ? float(1 << max(sh6, 0)) : 0.f;
+          const float dq = q >= parts ? 0.f : q + 1 < parts ? floorf(rem * (1.f / unit)) : rem;
+          const __half2 h = __floats2half2_rn(-dq, -dq);
+          wd[q] = q < parts ? *reinterpret_cast<const uint32_t*>(&h) : 0u;
+          rem -= dq * unit;
+        }
+        sh.cwords[t] = make_uint4(wd[0], wd[1], wd[2], wd[3]);
         const int x0 = C - 2 + a.groups[gi].cmin;
         sh.x0a[t] = x0 & ~7;  // floor to a multiple of 8 (16-byte TMA start)
         sh.delta[t] = x0 - (x0 & ~7);
@@ -428,31 +444,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     __syncthreads();
     {
       // centring columns of every staged row of both window buffers: the
-      // centre c split like the planes, c = sum_q c_q 64^(parts - 1 - q), as
-      // the pairs (-c_q, -c_q), q = 0 .. parts - 1, then zeros
+      // candidate's centring words (set-up above)
       const TcGroup& G = sh.grp;
       const TcShape sp(G);
       const int rows = G.rows_slab;
       for (int it = t; it < 2 * kTcCands * rows; it += kTcThreads) {
         const int buf = it / (kTcCands * rows), g = (it / rows) % kTcCands, r = it % rows;
-        const float c = g < sh.cnt ? sh.centre[g] : 0.f;
-        uint32_t w[kTcMaxParts];
-        float rem = c;
-#pragma unroll
-        for (int q = 0; q < kTcMaxParts; ++q) {
-          // digit q of parts: weight 64^(parts - 1 - q); none past the last
-          const int sh6 = 6 * (G.parts - 1 - q);
-          const float unit = sh6 >= 0 ? float(1 << max(sh6, 0)) : 0.f;
-          const float dq = q >= G.parts ? 0.f : q + 1 < G.parts ? floorf(rem * (1.f / unit)) : rem;
-          const __half2 h = __floats2half2_rn(-dq, -dq);
-          w[q] = q < G.parts ? *reinterpret_cast<const uint32_t*>(&h) : 0u;
-          rem -= dq * unit;
-        }
-        uint4 v;
-        v.x = w[0];
-        v.y = w[1];
-        v.z = w[2];
-        v.w = w[3];
+        const uint4 v = g < sh.cnt ? sh.cwords[g] : make_uint4(0, 0, 0, 0);
         uint8_t* row = abase + size_t(buf) * a.abuf_bytes + size_t(g) * sp.sbo + size_t(sp.nplane) * sp.lbo +
                        size_t(r) * 16;
         *reinterpret_cast<uint4*>(row) = v;
@@ -710,7 +708,9 @@ cudaError_t launch_tc_track(const TcLaunch& l, size_t smem, int grid, cudaStream
   const void* fn = l.jobs ? reinterpret_cast<const void*>(tc_track_kernel<true>)
                            : reinterpret_cast<const void*>(tc_track_kernel<false>);
   if (cudaError_t e = reserve_dynamic_smem(fn, smem)) return e;
-  if (cudaError_t e = cudaMemsetAsync(l.next, 0, sizeof(int), s)) return e;
+  // a single job's counter (its tile list's) is reset by the tile planner
+  if (l.jobs)
+    if (cudaError_t e = cudaMemsetAsync(l.next, 0, sizeof(int), s)) return e;
   if (l.jobs)
     tc_track_kernel<true><<<grid, kTcThreads, smem, s>>>(l);
   else
