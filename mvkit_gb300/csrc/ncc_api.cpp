@@ -433,14 +433,16 @@ bool lattice_exact32(double v) {
 // Builds the tensor-core groups of the tracking step into level T (query
 // plan `lp`, `nsrc` patches on the source level).  A group is the rotated
 // patches (origin on the lattice) of one source patch's selected list; the
-// sources with identical lists share it.  Weights: for grid row y, an N x K
-// fp16 matrix in the canonical K-major no-swizzle layout (8 x 8 core
-// matrices of 128 bytes, K-adjacent cores 128 bytes apart, N-adjacent cores
-// K/8 x 128 bytes apart); column (p, dc, half) holds the high or low fp16
-// half of sigma w_p(y, x - dc), row x + part kw the same for each plane part
-// (x 64 for the high part of a split level).  The last 16 rows hold the
-// column's row sum for grid row y as two fp16 terms (x 64 for the high part),
-// which the centring columns of the window multiply.
+// sources with identical lists share it.  Weights: per chunk of rg grid
+// rows, an N x K fp16 matrix in the canonical K-major no-swizzle layout
+// (8 x 8 core matrices of 128 bytes, K-adjacent cores 128 bytes apart,
+// N-adjacent cores K/8 x 128 bytes apart); column (((p 5 + dc) rg + y mod
+// rg) 2 + half) holds the high or low fp16 half of sigma w_p(y, x - dc), row
+// x + part kw the same for each plane part (x 64 per digit above the last).
+// The slots of one output sit side by side, so 32 accumulator columns hold
+// 16 / rg whole outputs (rg is 1, 2 or 4).  The last 16 rows hold the
+// column's row sum for grid row y as two fp16 terms (x 64 likewise), which
+// the centring columns of the window multiply.
 std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, const LevelPlan& lp, int parts,
                                             float offset, size_t budget) {
   auto plan = std::make_shared<TcPlan>();
@@ -479,11 +481,12 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
     }
     pr.kr = pr.rmax - pr.rmin + 1;
     pr.kw = (pr.cmax - pr.cmin + 1 + 4 + 15) / 16 * 16;
-    // grid rows per chunk: as many as keep N <= 256 (and <= 4, so that
-    // placement row + chunk row stays within the 8 rows of a candidate)
+    // grid rows per chunk: a power of two (whole outputs per 32 accumulator
+    // columns), as many as keep N <= 256, and <= 4 (placement row + chunk
+    // row stays within the 8 rows of a candidate)
     const int P = int(pr.descs.size());
     pr.rg = 4;
-    while (pr.rg > 1 && (10 * P * pr.rg + 15) / 16 * 16 > 256) --pr.rg;
+    while (pr.rg > 1 && (10 * P * pr.rg + 15) / 16 * 16 > 256) pr.rg >>= 1;
     pr.n = (10 * P * pr.rg + 15) / 16 * 16;
     by_key[key] = int(protos.size());
     plan->group_of_src[src] = int(protos.size());
@@ -586,9 +589,9 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
     g.inv_scale = float(1.0 / sigma);
     g.macs = 0;
     // element of grid row y, column (patch q, placement dc, half), K index k:
-    // chunk y / rg, N column ((y mod rg) P + q) 5 + dc) 2 + half
+    // chunk y / rg, N column ((q 5 + dc) rg + y mod rg) 2 + half
     auto at = [&](size_t y, int q, int dc, int half, int k) {
-      const int n = ((int(y % size_t(rg)) * P + q) * 5 + dc) * 2 + half;
+      const int n = ((q * 5 + dc) * rg + int(y % size_t(rg))) * 2 + half;
       return (y / size_t(rg)) * chunk_elems + size_t(n / 8) * size_t(K / 8) * 64 + size_t(k / 8) * 64 +
              size_t(n % 8) * 8 + size_t(k % 8);
     };
@@ -649,7 +652,6 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
     check(cudaMemcpy(buf->p, host.data(), host.size() * 2, cudaMemcpyHostToDevice), "tc weights");
     g.b = buf->p;
     plan->weights.push_back(std::move(buf));
-    plan->smem = std::max(plan->smem, size_t(128) * size_t(N + 1) * 4 + 1024);  // accumulator staging
     plan->groups.push_back(g);
   }
   return plan;

@@ -7,7 +7,7 @@
 // candidates of a group and one MMA computes, for a chunk of rg grid rows
 // y .. y + rg - 1 of the patches' union grid (k < rg),
 //
-//   D[(candidate g, row m)][(k, patch p, column placement dc, half)]
+//   D[(candidate g, row m)][(patch p, column placement dc, k, half)]
 //     += sum_x window_g(y + m, x) * w_{p,half}(y + k, x - dc)
 //
 // Window row y + m is placement m at grid row y and placement m - k at grid
@@ -28,10 +28,11 @@
 // planes start 8 columns left of the level.  Weights (fp16 high and low
 // halves of the scaled weights) stream through a ring of shared-memory
 // buffers with bulk copies (TMA engine).  The block is warp-specialised:
-// four window-producer warps (two slab buffers), a weight-producer thread
-// and an MMA-issue thread; accumulation is FP32 in tensor memory.  The
-// epilogue writes sum w (S - S0) per placement; track_kernel adds the exact
-// integer window moments and applies the reference's selection rule.
+// four set-up and window-producer warps (two slab buffers), a
+// weight-producer thread, an MMA-issue thread and four epilogue warps, with
+// two tiles in flight; accumulation is FP32 in tensor memory.  The epilogue
+// writes sum w (S - S0) per placement; track_kernel adds the exact integer
+// window moments and applies the reference's selection rule.
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -42,8 +43,9 @@
 namespace mvg {
 namespace {
 
-constexpr int kTcThreads = 192;     // warp 0 MMA, warp 1 weights, warps 2-5 windows
+constexpr int kTcThreads = 320;  // warp 0 MMA, warp 1 weights, warps 2-5 set-up and windows, warps 6-9 epilogue
 constexpr int kTcWindowThreads = 128;
+constexpr int kTcEpilogueThreads = 128;
 constexpr int kTcRows = 128;                  // MMA M
 constexpr uint32_t kTmemCols = 512 / kTcBlocksPerSm;  // accumulator sets x columns per set
 constexpr unsigned long long kWaitNs = 1000000000ull;  // an mbarrier wait gives up after one second
@@ -91,8 +93,9 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 
 // Waits for the phase with the given parity; false once kWaitNs passed
-// without it (the caller records the failure and leaves).
-__device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity) {
+// without it, or (given `fail`) once another role of the block has failed
+// (the caller records the failure and leaves).
+__device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity, const int* fail = nullptr) {
   unsigned long long start = 0;
   for (;;) {
     uint32_t done;
@@ -102,6 +105,7 @@ __device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity) {
         : "r"(smem_u32(bar)), "r"(parity)
         : "memory");
     if (done) return true;
+    if (fail && *reinterpret_cast<const volatile int*>(fail)) return false;
     const unsigned long long now = global_ns();
     if (!start)
       start = now;
@@ -140,21 +144,30 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 
+// One tile in flight: its set-up, written by the window warps and shared
+// with the other roles (info_full hands it over; info_empty, arrived by the
+// MMA thread, the weight producer and the epilogue, hands the slot back).
+struct __align__(16) TcSlot {
+  TcArgs job;    // the tile's job (job tables only)
+  TcGroup grp;
+  int gtile;     // launch tile; -1: the block has no more tiles
+  int cnt;       // candidates of the tile
+  int ci[kTcCands], R[kTcCands], x0a[kTcCands], delta[kTcCands];
+  float centre[kTcCands];  // window centre value minus the plane offset (exact integer)
+  uint4 cwords[kTcCands];  // its centring words: (-c_q, -c_q) half2 per digit q, then zeros
+};
+
 struct __align__(16) TcShared {
   uint64_t a_full[2], slab_done[2], drain;
   uint64_t b_full[kTcMaxStages], b_empty[kTcMaxStages];
-  TcArgs job;              // the current tile's job
+  uint64_t info_full[2], info_empty[2];  // tile slots
+  uint64_t acc_full, acc_empty;          // the tile's accumulators in tensor memory
+  TcSlot slot[2];
   int job_base[kTcMaxJobs + 1];  // first launch tile of each job
-  int job_of;              // index of `job` (-1: none loaded)
-  TcGroup grp;
   uint32_t tmem;
-  int fail, cnt;
-  int next_tile;     // the block's next tile (dynamic scheduling)
-  long long cm, cb;  // weight chunks consumed (MMA thread) / loaded (weight producer)
-  int sm, sa;        // window slabs consumed (MMA thread) / staged (window producer)
-  int ci[kTcCands], R[kTcCands], C[kTcCands], x0a[kTcCands], delta[kTcCands];
-  float centre[kTcCands];  // window centre value minus the plane offset (exact integer)
-  uint4 cwords[kTcCands];  // its centring words: (-c_q, -c_q) half2 per digit q, then zeros
+  int fail;
+  int claim;         // the window warps' next tile (broadcast)
+  long long cm, cb;  // weight chunks consumed (MMA thread) / loaded (weight producer), at exit
 };
 
 // Shape of one tile's operands.
@@ -176,14 +189,26 @@ struct TcShape {
   }
 };
 
-__device__ __forceinline__ void tc_fail(const TcArgs& a, TcShared& sh) {
-  atomicExch(&sh.fail, 1);
-  atomicExch(a.error, int32_t(kInternal));
+// A role gave up (a wait ran out, or another role failed): the others leave
+// at their next wait; the launch's jobs get the error flag at the end.
+__device__ __forceinline__ void tc_fail(TcShared& sh) { atomicExch(&sh.fail, 1); }
+
+// Named barriers of one role's warps (warp-divergent forms).  The AND form
+// gives every thread the same verdict, so a group leaves its loop together.
+__device__ __forceinline__ void named_sync(int id, int threads) {
+  asm volatile("barrier.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+}
+__device__ __forceinline__ bool named_and(int id, int threads, bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred pi, po;\n setp.ne.u32 pi, %1, 0;\n barrier.red.and.pred po, %2, %3, pi;\n"
+      " selp.u32 %0, 1, 0, po;\n}\n"
+      : "=r"(r)
+      : "r"(uint32_t(v)), "r"(id), "r"(threads)
+      : "memory");
+  return r != 0;
 }
 
-// MMA issue (one thread): per slab, wait for the windows, then per grid row
-// wait for its weights, issue K/16 MMAs into accumulator set y mod sets and
-// release the weight buffer; release the window buffer after the slab.
 // Position in the weight ring: buffer index and phase parity of chunk count,
 // advanced incrementally (no division on the issue path).
 struct RingPos {
@@ -199,18 +224,19 @@ struct RingPos {
   }
 };
 
-__device__ void tc_mma_role(const TcArgs& a, TcShared& sh, uint8_t* wbase, uint8_t* abase, uint32_t tmem,
-                            RingPos& cm, int& sm) {
-  const TcGroup& G = sh.grp;
+// MMA issue (one thread), one tile: per slab, wait for the windows, then per
+// grid row wait for its weights, issue K/16 MMAs into accumulator set
+// y mod sets and release the weight buffer; release the window buffer after
+// the slab, and the accumulators to the epilogue after the tile.
+__device__ bool tc_mma_tile(const TcArgs& a, const TcSlot& ts, TcShared& sh, uint8_t* wbase, uint8_t* abase,
+                            uint32_t tmem, RingPos& cm, int& sm) {
+  const TcGroup& G = ts.grp;
   const TcShape sp(G);
   const int S = a.stages;
   const uint32_t idesc = (1u << 4) | (uint32_t(G.n >> 3) << 17) | (uint32_t(kTcRows >> 4) << 24);
   for (int sl = 0; sl < sp.nslabs; ++sl) {
     const int buf = sm & 1;
-    if (!bar_wait(&sh.a_full[buf], uint32_t((sm >> 1) & 1))) {
-      tc_fail(a, sh);
-      return;
-    }
+    if (!bar_wait(&sh.a_full[buf], uint32_t((sm >> 1) & 1), &sh.fail)) return false;
     // descriptors advance by plain adds of the 16-byte address units: one row
     // per grid row, two segments (2 lbo) per K step; weights 256 bytes per K step
     const uint64_t a_desc0 = smem_desc(smem_u32(abase + size_t(buf) * a.abuf_bytes), sp.lbo, sp.sbo);
@@ -222,10 +248,7 @@ __device__ void tc_mma_role(const TcArgs& a, TcShared& sh, uint8_t* wbase, uint8
     uint32_t d = tmem + uint32_t((chunk % a.sets) * a.npad);
     const uint32_t d_end = tmem + uint32_t(a.sets * a.npad);
     for (int y = y0; y < y1; y += G.rg, ++chunk) {
-      if (!bar_wait(&sh.b_full[cm.stage], cm.phase)) {
-        tc_fail(a, sh);
-        return;
-      }
+      if (!bar_wait(&sh.b_full[cm.stage], cm.phase, &sh.fail)) return false;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       uint64_t ad = a_desc0 + uint64_t(y - y0), bd = b_desc0 + uint64_t(cm.stage) * b_stage;
       mma_f16(d, ad, bd, idesc, chunk >= a.sets ? 1u : 0u);
@@ -243,36 +266,39 @@ __device__ void tc_mma_role(const TcArgs& a, TcShared& sh, uint8_t* wbase, uint8
     mma_commit(&sh.slab_done[buf]);
     ++sm;
   }
+  mma_commit(&sh.acc_full);
+  return true;
 }
 
-// Window producers (four warps): per slab, once the MMAs of the slab that
-// last used the buffer are done, 16-byte cp.async copies from the planes
-// (zero outside them); a warp's copies are 8 rows x 4 segments, so its global
-// reads are 64-byte row pieces and its shared writes 128-byte row runs.
-// Each thread waits for its own copies, orders them for the tensor cores
-// (proxy fence) and arrives on the buffer's barrier (128 arrivals).
-__device__ void tc_window_role(const TcArgs& a, TcShared& sh, uint8_t* abase, int& sa, int pt) {
-  const TcGroup& G = sh.grp;
+// Window producers (four warps), one tile: per slab, once the MMAs of the
+// slab that last used the buffer are done, 16-byte cp.async copies from the
+// planes (zero outside them) and the centring columns of the tile's
+// candidates; a warp's copies are 8 rows x 4 segments, so its global reads
+// are 64-byte row pieces and its shared writes 128-byte row runs.  Each
+// thread waits for its own copies, orders its writes for the tensor cores
+// (proxy fence) and arrives on the buffer's barrier (128 arrivals).  Rows of
+// candidates beyond the tile's count are left as they are: their
+// accumulator rows are never read.
+__device__ bool tc_window_tile(const TcArgs& a, const TcSlot& ts, TcShared& sh, uint8_t* abase, int& sa, int pt) {
+  const TcGroup& G = ts.grp;
   const TcShape sp(G);
-  const int cnt = sh.cnt, rows = G.rows_slab, H = a.lev.h, pitch = a.plane_pitch;
+  const int cnt = ts.cnt, rows = G.rows_slab, H = a.lev.h, pitch = a.plane_pitch;
   const size_t plane = size_t(H) * size_t(pitch);
   const int lane = pt & 31, wp = pt >> 5;
   const int rblocks = rows / 8;
   const size_t part_stride = size_t(kTcPlaneShifts) * plane;  // one part's planes -> the next part's
+  const int g_first = pt / rows, r_first = pt - g_first * rows;  // first centring row of this thread
   for (int sl = 0; sl < sp.nslabs; ++sl) {
     const int buf = sa & 1;
-    if (sa >= 2 && !bar_wait(&sh.slab_done[buf], uint32_t(((sa >> 1) - 1) & 1))) {
-      tc_fail(a, sh);
-      return;
-    }
+    if (sa >= 2 && !bar_wait(&sh.slab_done[buf], uint32_t(((sa >> 1) - 1) & 1), &sh.fail)) return false;
     uint8_t* dst0 = abase + size_t(buf) * a.abuf_bytes;
     const int y0 = sl * sp.Y;
     // warp wp stages candidates wp, wp + 4, ...; lane = (row in an 8-row block,
     // segment in a 4-segment block)
     for (int g = wp; g < cnt; g += kTcWindowThreads / 32) {
-      const int row0 = sh.R[g] - 2 + G.rmin + y0 + (lane & 7);
-      const int x0 = sh.x0a[g] + kTcPlaneMargin;
-      const uint16_t* pbase = a.planes + size_t(sh.delta[g]) * plane;
+      const int row0 = ts.R[g] - 2 + G.rmin + y0 + (lane & 7);
+      const int x0 = ts.x0a[g] + kTcPlaneMargin;
+      const uint16_t* pbase = a.planes + size_t(ts.delta[g]) * plane;
       uint8_t* dg = dst0 + size_t(g) * sp.sbo + size_t(lane & 7) * 16;
       for (int rb = 0; rb < rblocks; ++rb) {
         const int row = row0 + rb * 8;
@@ -286,44 +312,181 @@ __device__ void tc_window_role(const TcArgs& a, TcShared& sh, uint8_t* abase, in
         }
       }
     }
+    // centring columns: (candidate g, row r) for g < cnt, 128 rows apart
+    for (int g = g_first, r = r_first; g < cnt;) {
+      uint8_t* row = dst0 + size_t(g) * sp.sbo + size_t(sp.nplane) * sp.lbo + size_t(r) * 16;
+      *reinterpret_cast<uint4*>(row) = ts.cwords[g];
+      *reinterpret_cast<uint4*>(row + sp.lbo) = make_uint4(0, 0, 0, 0);
+      r += kTcWindowThreads;
+      while (r >= rows) {
+        r -= rows;
+        ++g;
+      }
+    }
     asm volatile("cp.async.commit_group;\n cp.async.wait_group 0;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     bar_arrive(&sh.a_full[buf]);
     ++sa;
   }
+  return true;
 }
 
-// Weight producer (one thread): the tile's grid-row chunks through the ring,
-// as far ahead as the ring allows.
-__device__ void tc_weight_role(const TcArgs& a, TcShared& sh, uint8_t* wbase, RingPos& cb) {
-  if (a.withhold_weights) return;  // test hook: the MMA thread's weight wait runs out
-  const TcGroup& G = sh.grp;
-  const TcShape sp(G);
+// Weight producer (one thread), one tile: its grid-row chunks through the
+// ring, as far ahead as the ring allows (into the next tile while the MMAs
+// of this one run).
+__device__ bool tc_weight_tile(const TcArgs& a, const TcSlot& ts, TcShared& sh, uint8_t* wbase, RingPos& cb) {
+  if (a.withhold_weights) return true;  // test hook: the MMA thread's weight wait runs out
+  const TcShape sp(ts.grp);
   const int S = a.stages;
-  const uint8_t* src = G.b;
+  const uint8_t* src = ts.grp.b;
   for (int i = 0; i < sp.chunks; ++i) {
     // the buffer's previous chunk (count - S) has been consumed
-    if (cb.count >= S && !bar_wait(&sh.b_empty[cb.stage], cb.phase ^ 1u)) {
-      tc_fail(a, sh);
-      return;
-    }
+    if (cb.count >= S && !bar_wait(&sh.b_empty[cb.stage], cb.phase ^ 1u, &sh.fail)) return false;
     expect_tx(&sh.b_full[cb.stage], sp.bchunk);
     bulk_load(wbase + size_t(cb.stage) * a.stage_bytes, src, sp.bchunk, &sh.b_full[cb.stage]);
     src += sp.bchunk;
     cb.advance(S);
   }
+  return true;
 }
 
-// Persistent and warp-specialised: the launch's tiles are those of its jobs
-// in job order; block b takes tile b first, then the next unclaimed tile
-// from a global counter (tiles differ in cost, so a static stride leaves
-// blocks idle at the end); per tile warp 0 issues the MMAs, warp 1 streams
-// weights, warps 2-5 stage windows, and all six warps run the set-up and the
-// epilogue.  Shared memory: weight ring (stages x stage_bytes) | two window
-// buffers, the same for every job of the launch.
-// Multi: a table of jobs in device memory, the current one copied to shared
-// memory per tile; otherwise the one job of the launch parameters (read
-// through the constant bank).
+// Tile set-up (the window warps): the tile's job (job tables), group and
+// candidates into the slot, one candidate per thread.
+template <bool Multi>
+__device__ void tc_setup(const TcArgs* jobs, const TcShared& sh, TcSlot& ts, int gtile, int ntiles, int pt) {
+  if (gtile >= ntiles) {
+    if (pt == 0) ts.gtile = -1;
+    return;
+  }
+  int jb = 0;
+  if (Multi)
+    while (gtile >= sh.job_base[jb + 1]) ++jb;
+  const TcArgs& a = jobs[jb];
+  const int tile = gtile - sh.job_base[jb];
+  if (Multi) {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(&a);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&ts.job);
+    for (int w = pt; w < int(sizeof(TcArgs) / 4); w += kTcWindowThreads) dst[w] = src[w];
+  }
+  const int gi = a.tiles->group[tile];
+  const TcGroup& gsrc = a.groups[gi];
+  {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(&gsrc);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&ts.grp);
+    for (int w = pt; w < int(sizeof(TcGroup) / 4); w += kTcWindowThreads) dst[w] = src[w];
+  }
+  const int first = a.tiles->first[tile];
+  const int cnt = min(kTcCands, a.tiles->last[tile] - first);
+  if (pt == 0) {
+    ts.gtile = gtile;
+    ts.cnt = cnt;
+  }
+  if (pt < cnt) {
+    const int ci = a.order[first + pt];
+    const Cand cd = a.in[ci];
+    int R, C;
+    if (a.rc) {
+      R = a.rc[ci].x;
+      C = a.rc[ci].y;
+    } else if (a.exact32) {
+      const float s = float(1.0 / a.step);
+      R = int(roundf(__fmul_rn(__fsub_rn(__fsub_rn(float(cd.row), float(a.crop_row)), float(a.offset)), s)));
+      C = int(roundf(__fmul_rn(__fsub_rn(__fsub_rn(float(cd.col), float(a.crop_col)), float(a.offset)), s)));
+    } else {
+      R = int(round(dsub(dsub(cd.row, a.crop_row), a.offset) / a.step));
+      C = int(round(dsub(dsub(cd.col, a.crop_col), a.offset) / a.step));
+    }
+    ts.ci[pt] = ci;
+    ts.R[pt] = R;
+    const int cr = min(max(R, 0), a.lev.h - 1), cc = min(max(C, 0), a.lev.w - 1);
+    const float centre = a.lev.v[size_t(cr) * a.lev.w + cc] -
+                         tc_plane_offset(a.plane_offset, a.dyn_offset ? a.state : nullptr, a.level_mult);
+    ts.centre[pt] = centre;
+    // the centre split like the planes, c = sum_q c_q 64^(parts - 1 - q),
+    // as the pairs (-c_q, -c_q), q = 0 .. parts - 1, then zeros
+    const int parts = gsrc.parts;
+    uint32_t wd[kTcMaxParts];
+    float rem = centre;
+#pragma unroll
+    for (int q = 0; q < kTcMaxParts; ++q) {
+      const int sh6 = 6 * (parts - 1 - q);
+      const float unit = sh6 >= 0 ? float(1 << max(sh6, 0)) : 0.f;
+      const float dq = q >= parts ? 0.f : q + 1 < parts ? floorf(rem * (1.f / unit)) : rem;
+      const __half2 h = __floats2half2_rn(-dq, -dq);
+      wd[q] = q < parts ? *reinterpret_cast<const uint32_t*>(&h) : 0u;
+      rem -= dq * unit;
+    }
+    ts.cwords[pt] = make_uint4(wd[0], wd[1], wd[2], wd[3]);
+    const int x0 = C - 2 + gsrc.cmin;
+    ts.x0a[pt] = x0 & ~7;  // floor to a multiple of 8 (16-byte copy start)
+    ts.delta[pt] = x0 - (x0 & ~7);
+  }
+}
+
+// Epilogue (four warps), one tile: warp w reads tensor-memory lanes
+// 32 (w mod 4) .. + 31, accumulator row m = 8 g + r of candidate g.  The
+// columns of output u = (patch q, column placement dc) are the rg grid-row
+// slots k and two weight halves side by side, (u rg + k) 2 + half, so 32
+// columns hold 16 / rg whole outputs.  Per 32 columns the accumulator sets
+// are summed (set order), slot k comes from row m + k (a shuffle within the
+// candidate's 8 rows), and the dot of placement (dr = r, dc) is
+// sum_k (D[m + k][.., half 0] + D[m + k][.., half 1]) in k order.
+template <int RG>
+__device__ void tc_epilogue(const TcArgs& a, const TcSlot& ts, uint32_t trow, int quarter, int lane) {
+  const TcGroup& G = ts.grp;
+  constexpr int kPer = 16 / RG;  // outputs per 32 accumulator columns
+  const int nout = G.p * 5;
+  const int nsets = min(a.sets, (G.kr + RG - 1) / RG);
+  const int g = quarter * 4 + (lane >> 3), dr = lane & 7;
+  const bool live = g < ts.cnt && dr < 5;
+  const float poff = tc_plane_offset(a.plane_offset, a.dyn_offset ? a.state : nullptr, a.level_mult);
+  const float cen = live ? ts.centre[g] : 0.f;
+  float* out = a.dots + (live ? size_t(ts.ci[g]) * kTcScoreStride + size_t(dr) * 5 : 0);
+  for (int u0 = 0; u0 < nout; u0 += kPer) {
+    const uint32_t c0 = uint32_t(u0 * RG * 2);  // a multiple of 32
+    float x[32];
+    tmem_ld32(trow + c0, x);
+    for (int set = 1; set < nsets; ++set) {
+      float v[32];
+      tmem_ld32(trow + uint32_t(set * a.npad) + c0, v);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) x[j] += v[j];
+    }
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+      float sum = 0.f;
+#pragma unroll
+      for (int k = 0; k < RG; ++k) {
+        const float v0 = __shfl_down_sync(0xffffffffu, x[(j * RG + k) * 2], k);
+        const float v1 = __shfl_down_sync(0xffffffffu, x[(j * RG + k) * 2 + 1], k);
+        sum += v0 + v1;
+      }
+      const int u = u0 + j;
+      if (live && u < nout) {
+        const int q = u / 5, dc = u - q * 5;
+        // sum w S = sum w (S' - c) + c ecorr + offset weff (S' = S - offset);
+        // the consumers subtract S0 weff (first sample S0) themselves
+        out[G.k_of[q] * 25 + dc] = sum * G.inv_scale + (cen * G.ecorr[q] + poff * G.weff[q]);
+      }
+    }
+  }
+}
+
+// Persistent and warp-specialised, tiles pipelined: the launch's tiles are
+// those of its jobs in job order; block b takes tile b first, then the next
+// unclaimed tile from a global counter (tiles differ in cost, so a static
+// stride leaves blocks idle at the end).  Warp 0 issues the MMAs, warp 1
+// streams weights, warps 2-5 set up tiles and stage windows, warps 6-9 run
+// the epilogue.  Two tile slots let the set-up, windows and weights of the
+// next tile go ahead while the MMAs of this one run; the MMAs of the next
+// tile start once the epilogue has read the accumulators.  Shared memory:
+// weight ring (stages x stage_bytes) | two window buffers, the same for
+// every job of the launch.  Every wait is bounded; a role that gives up
+// makes the others leave, the block drains its copies and MMAs and flags
+// every job of the launch.
+// Multi: a table of jobs in device memory, a tile's job copied into its
+// slot; otherwise the one job of the launch parameters (read through the
+// constant bank).
 template <bool Multi>
 __global__ void __launch_bounds__(kTcThreads, 1)
     tc_track_kernel(const __grid_constant__ TcLaunch L) {
@@ -331,20 +494,19 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __shared__ TcShared sh;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const TcArgs* jobs = Multi ? L.jobs : &L.single;
+  const int njobs = Multi ? L.njobs : 1;
   // first launch tile of each job (the jobs' tile lists were planned on the device)
   if (t == 0) {
     int n = 0;
-    for (int j = 0; j < (Multi ? L.njobs : 1); ++j) {
+    for (int j = 0; j < njobs; ++j) {
       sh.job_base[j] = n;
       n += jobs[j].tiles->count;
     }
-    sh.job_base[Multi ? L.njobs : 1] = n;
-    sh.job_of = -1;
+    sh.job_base[njobs] = n;
   }
   __syncthreads();
-  const int ntiles = sh.job_base[Multi ? L.njobs : 1];
+  const int ntiles = sh.job_base[njobs];
   if (int(blockIdx.x) >= ntiles) return;
-  const TcArgs& a = Multi ? sh.job : L.single;
   // launch shape: equal for every job
   const int stages = jobs[0].stages, stage_bytes = jobs[0].stage_bytes;
   uint8_t* smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
@@ -360,10 +522,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       bar_init(&sh.b_full[s]);
       bar_init(&sh.b_empty[s]);
     }
+    for (int b = 0; b < 2; ++b) {
+      bar_init(&sh.info_full[b]);
+      bar_init(&sh.info_empty[b], 3);  // MMA thread, weight producer, epilogue
+    }
+    bar_init(&sh.acc_full);
+    bar_init(&sh.acc_empty);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     sh.fail = 0;
     sh.cm = sh.cb = 0;
-    sh.sm = sh.sa = 0;
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh.tmem)),
@@ -374,177 +541,124 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = sh.tmem;
-  RingPos cm, cb;            // role-local ring positions (MMA thread, weight producer)
-  int sm = 0, sa = 0;        // role-local counters (MMA thread, window producer)
-  for (int gtile = blockIdx.x; gtile < ntiles; gtile = sh.next_tile) {
-    // the tile's job into shared memory (when it changes)
-    int jb = 0;
-    if (Multi) {
-      while (gtile >= sh.job_base[jb + 1]) ++jb;
-      if (jb != sh.job_of) {
-        __syncthreads();
-        const uint32_t* src = reinterpret_cast<const uint32_t*>(jobs + jb);
-        uint32_t* dst = reinterpret_cast<uint32_t*>(&sh.job);
-        for (int w = t; w < int(sizeof(TcArgs) / 4); w += kTcThreads) dst[w] = src[w];
-        __syncthreads();
-        if (t == 0) sh.job_of = jb;
-      }
-    }
-    const int tile = gtile - sh.job_base[jb];
-    // tile set-up: the group into shared memory, one candidate per thread
-    {
-      const int gi = a.tiles->group[tile];
-      const uint32_t* src = reinterpret_cast<const uint32_t*>(a.groups + gi);
-      uint32_t* dst = reinterpret_cast<uint32_t*>(&sh.grp);
-      for (int w = t; w < int(sizeof(TcGroup) / 4); w += kTcThreads) dst[w] = src[w];
-      const int first = a.tiles->first[tile];
-      const int cnt = min(kTcCands, a.tiles->last[tile] - first);
-      if (t == 0) sh.cnt = cnt;
-      if (t < cnt) {
-        const int ci = a.order[first + t];
-        const Cand cd = a.in[ci];
-        int R, C;
-        if (a.rc) {
-          R = a.rc[ci].x;
-          C = a.rc[ci].y;
-        } else if (a.exact32) {
-          const float s = float(1.0 / a.step);
-          R = int(roundf(__fmul_rn(__fsub_rn(__fsub_rn(float(cd.row), float(a.crop_row)), float(a.offset)), s)));
-          C = int(roundf(__fmul_rn(__fsub_rn(__fsub_rn(float(cd.col), float(a.crop_col)), float(a.offset)), s)));
-        } else {
-          R = int(round(dsub(dsub(cd.row, a.crop_row), a.offset) / a.step));
-          C = int(round(dsub(dsub(cd.col, a.crop_col), a.offset) / a.step));
+  if (warp == 0) {
+    if (lane == 0) {
+      RingPos cm;
+      int sm = 0;
+      for (int s = 0;; ++s) {
+        const int b = s & 1;
+        if (!bar_wait(&sh.info_full[b], uint32_t((s >> 1) & 1), &sh.fail)) {
+          tc_fail(sh);
+          break;
         }
-        sh.ci[t] = ci;
-        sh.R[t] = R;
-        sh.C[t] = C;
-        const int cr = min(max(R, 0), a.lev.h - 1), cc = min(max(C, 0), a.lev.w - 1);
-        sh.centre[t] = a.lev.v[size_t(cr) * a.lev.w + cc] -
-                       tc_plane_offset(a.plane_offset, a.dyn_offset ? a.state : nullptr, a.level_mult);
-        // the centre split like the planes, c = sum_q c_q 64^(parts - 1 - q),
-        // as the pairs (-c_q, -c_q), q = 0 .. parts - 1, then zeros
-        const int parts = a.groups[gi].parts;
-        uint32_t wd[kTcMaxParts];
-        float rem = sh.centre[t];
-#pragma unroll
-        for (int q = 0; q < kTcMaxParts; ++q) {
-          const int sh6 = 6 * (parts - 1 - q);
-          const float unit = sh6 >= 0 ? float(1 << max(sh6, 0)) : 0.f;
-          const float dq = q >= parts ? 0.f : q + 1 < parts ? floorf(rem * (1.f / unit)) : rem;
-          const __half2 h = __floats2half2_rn(-dq, -dq);
-          wd[q] = q < parts ? *reinterpret_cast<const uint32_t*>(&h) : 0u;
-          rem -= dq * unit;
+        const TcSlot& ts = sh.slot[b];
+        if (ts.gtile < 0) break;
+        // the previous tile's accumulators have been read
+        if (s > 0 && !bar_wait(&sh.acc_empty, uint32_t((s - 1) & 1), &sh.fail)) {
+          tc_fail(sh);
+          break;
         }
-        sh.cwords[t] = make_uint4(wd[0], wd[1], wd[2], wd[3]);
-        const int x0 = C - 2 + a.groups[gi].cmin;
-        sh.x0a[t] = x0 & ~7;  // floor to a multiple of 8 (16-byte TMA start)
-        sh.delta[t] = x0 - (x0 & ~7);
-      }
-    }
-    __syncthreads();
-    {
-      // centring columns of every staged row of both window buffers: the
-      // candidate's centring words (set-up above)
-      const TcGroup& G = sh.grp;
-      const TcShape sp(G);
-      const int rows = G.rows_slab;
-      for (int it = t; it < 2 * kTcCands * rows; it += kTcThreads) {
-        const int buf = it / (kTcCands * rows), g = (it / rows) % kTcCands, r = it % rows;
-        const uint4 v = g < sh.cnt ? sh.cwords[g] : make_uint4(0, 0, 0, 0);
-        uint8_t* row = abase + size_t(buf) * a.abuf_bytes + size_t(g) * sp.sbo + size_t(sp.nplane) * sp.lbo +
-                       size_t(r) * 16;
-        *reinterpret_cast<uint4*>(row) = v;
-        *reinterpret_cast<uint4*>(row + sp.lbo) = make_uint4(0, 0, 0, 0);
-      }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    }
-    __syncthreads();
-    if (warp == 0) {
-      if (lane == 0) {
-        tc_mma_role(a, sh, wbase, abase, tmem, cm, sm);
-        sh.cm = cm.count;
-        sh.sm = sm;
-      }
-      __syncwarp();
-    } else if (warp == 1) {
-      if (lane == 0) {
-        tc_weight_role(a, sh, wbase, cb);
-        sh.cb = cb.count;
-      }
-      __syncwarp();
-    } else {
-      tc_window_role(a, sh, abase, sa, t - 64);
-      if (t == 64) sh.sa = sa;
-    }
-    __syncthreads();
-    if (!sh.fail) {
-      // all MMAs of the tile are complete once the last slab's commit arrived
-      const int last = sh.sm - 1;
-      if (!bar_wait(&sh.slab_done[last & 1], uint32_t((last >> 1) & 1))) tc_fail(a, sh);
-    }
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    __syncthreads();
-    if (sh.fail) {
-      // drain in-flight copies and MMAs (bounded) before leaving
-      if (t == 0) {
-        for (long long c = sh.cm; c < sh.cb; ++c)
-          bar_wait(&sh.b_full[int(c % a.stages)], uint32_t((c / a.stages) & 1));
-        mma_commit(&sh.drain);
-        bar_wait(&sh.drain, 0);
-      }
-      __syncthreads();
-      break;
-    }
-    const TcGroup& G = sh.grp;
-    // accumulators -> shared memory (row t; the operand buffers are free now)
-    float* D = reinterpret_cast<float*>(smem);
-    const int ld = G.n + 1;
-    const int nsets = min(a.sets, (G.kr + G.rg - 1) / G.rg);
-    if (warp < 4)  // warp w reads tensor-memory lanes 32w..32w+31
-      for (int c0 = 0; c0 < G.n; c0 += 32) {
-        float acc[32];
-        tmem_ld32(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0), acc);
-        for (int set = 1; set < nsets; ++set) {
-          float v[32];
-          tmem_ld32(tmem + (uint32_t(warp * 32) << 16) + uint32_t(set * a.npad + c0), v);
-#pragma unroll
-          for (int j = 0; j < 32; ++j) acc[j] += v[j];
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (!tc_mma_tile(Multi ? ts.job : L.single, ts, sh, wbase, abase, tmem, cm, sm)) {
+          tc_fail(sh);
+          break;
         }
-#pragma unroll
-        for (int j = 0; j < 32; ++j)
-          if (c0 + j < G.n) D[t * ld + c0 + j] = acc[j];
+        bar_arrive(&sh.info_empty[b]);
       }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    // one output per thread, consecutive threads on consecutive dots of a
-    // candidate ([selected patch][row placement][column placement])
-    const int per = 25 * G.p;
-    const float poff = tc_plane_offset(a.plane_offset, a.dyn_offset ? a.state : nullptr, a.level_mult);
-    for (int it = t; it < sh.cnt * per; it += kTcThreads) {
-      const int g = it / per, e = it - g * per;
-      const int q = e / 25, pos = e - q * 25, dr = pos / 5, dc = pos - dr * 5;
-      const int m = g * 8 + dr;  // accumulator row of grid-row slot 0
-      // sum w (S' - c) over the chunk's grid-row slots: slot k holds this
-      // placement's grid rows y + k in accumulator row m + k
-      float sum = 0.f;
-      for (int k = 0; k < G.rg; ++k) {
-        const int n0 = ((k * G.p + q) * 5 + dc) * 2;
-        sum += D[(m + k) * ld + n0] + D[(m + k) * ld + n0 + 1];
-      }
-      // sum w S = sum w (S' - c) + c ecorr + offset weff (S' = S - offset);
-      // the consumers subtract S0 weff (first sample S0) themselves
-      a.dots[size_t(sh.ci[g]) * kTcScoreStride + size_t(G.k_of[q]) * 25 + pos] =
-          sum * G.inv_scale + (sh.centre[g] * G.ecorr[q] + poff * G.weff[q]);
+      sh.cm = cm.count;
     }
+    __syncwarp();
+  } else if (warp == 1) {
+    if (lane == 0) {
+      RingPos cb;
+      for (int s = 0;; ++s) {
+        const int b = s & 1;
+        if (!bar_wait(&sh.info_full[b], uint32_t((s >> 1) & 1), &sh.fail)) {
+          tc_fail(sh);
+          break;
+        }
+        const TcSlot& ts = sh.slot[b];
+        if (ts.gtile < 0) break;
+        if (!tc_weight_tile(Multi ? ts.job : L.single, ts, sh, wbase, cb)) {
+          tc_fail(sh);
+          break;
+        }
+        bar_arrive(&sh.info_empty[b]);
+      }
+      sh.cb = cb.count;
+    }
+    __syncwarp();
+  } else if (warp < 6) {
+    // window warps (named barrier 1): claim, set up, stage
+    const int pt = t - 64;
+    int sa = 0;
+    bool ok = true;
+    for (int s = 0;; ++s) {
+      const int b = s & 1;
+      // the slot's previous tile (s - 2) is done
+      if (ok && s >= 2) ok = bar_wait(&sh.info_empty[b], uint32_t(((s >> 1) - 1) & 1), &sh.fail);
+      if (ok && pt == 0) sh.claim = s == 0 ? int(blockIdx.x) : int(gridDim.x) + atomicAdd(L.next, 1);
+      if (!named_and(1, kTcWindowThreads, ok)) {
+        tc_fail(sh);
+        break;
+      }
+      const int gtile = sh.claim;
+      tc_setup<Multi>(jobs, sh, sh.slot[b], gtile, ntiles, pt);
+      named_sync(1, kTcWindowThreads);
+      if (pt == 0) bar_arrive(&sh.info_full[b]);
+      if (gtile >= ntiles) break;
+      const TcSlot& ts = sh.slot[b];
+      ok = tc_window_tile(Multi ? ts.job : L.single, ts, sh, abase, sa, pt);
+    }
+  } else {
+    // epilogue warps (named barrier 2)
+    const int quarter = warp & 3, et = t - 192;
+    const uint32_t trow = tmem + (uint32_t(quarter * 32) << 16);
+    for (int s = 0;; ++s) {
+      const int b = s & 1;
+      bool ok = bar_wait(&sh.info_full[b], uint32_t((s >> 1) & 1), &sh.fail);
+      if (!named_and(2, kTcEpilogueThreads, ok)) {
+        tc_fail(sh);
+        break;
+      }
+      const TcSlot& ts = sh.slot[b];
+      if (ts.gtile < 0) break;
+      ok = bar_wait(&sh.acc_full, uint32_t(s & 1), &sh.fail);
+      if (!named_and(2, kTcEpilogueThreads, ok)) {
+        tc_fail(sh);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const TcArgs& a = Multi ? ts.job : L.single;
+      if (ts.grp.rg == 4)
+        tc_epilogue<4>(a, ts, trow, quarter, lane);
+      else if (ts.grp.rg == 2)
+        tc_epilogue<2>(a, ts, trow, quarter, lane);
+      else
+        tc_epilogue<1>(a, ts, trow, quarter, lane);
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      named_sync(2, kTcEpilogueThreads);
+      if (et == 0) {
+        bar_arrive(&sh.acc_empty);
+        const TcGroup& G = ts.grp;
+        atomicAdd(&a.state_rw->tc_macs, (unsigned long long)G.macs * (unsigned long long)ts.cnt);
+        atomicAdd(&a.state_rw->tc_issued,
+                  (unsigned long long)kTcRows * G.n * (G.parts * G.kw + 16) * ((G.kr + G.rg - 1) / G.rg));
+        bar_arrive(&sh.info_empty[b]);
+      }
+    }
+  }
+  __syncthreads();
+  if (sh.fail) {
+    // drain in-flight weight copies and MMAs (bounded) before leaving, and
+    // flag every job: tiles of any of them may be incomplete
     if (t == 0) {
-      atomicAdd(&a.state_rw->tc_macs, (unsigned long long)G.macs * (unsigned long long)sh.cnt);
-      atomicAdd(&a.state_rw->tc_issued,
-                (unsigned long long)kTcRows * G.n * (G.parts * G.kw + 16) * ((G.kr + G.rg - 1) / G.rg));
+      for (long long c = sh.cm; c < sh.cb; ++c)
+        bar_wait(&sh.b_full[int(c % stages)], uint32_t((c / stages) & 1));
+      mma_commit(&sh.drain);
+      bar_wait(&sh.drain, 0);
+      for (int j = 0; j < njobs; ++j) atomicExch(jobs[j].error, int32_t(kInternal));
     }
-    // generic accesses of the buffers before the next tile's async writes
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    if (t == 0) sh.next_tile = int(gridDim.x) + atomicAdd(L.next, 1);
-    __syncthreads();
   }
   __syncthreads();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
