@@ -719,6 +719,8 @@ def main():
     ap.add_argument("--no-compare", action="store_true", help="skip timing the other correlation path")
     ap.add_argument("--cohorts", type=int, default=0,
                     help="groups of finds in flight whose tensor-core launches are merged (0: per find)")
+    ap.add_argument("--tc-lookahead", type=int, default=None,
+                    help="grid rows of tensor-core weights in flight (launch shape; default: the library's)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, *CONFIG_WORKLOADS],
                     help="the headline workload or a configuration workload (extended mode)")
@@ -767,10 +769,15 @@ def main():
 
     path = [args.path]
 
+    def thread_settings():
+        mg.set_correlation_path(path[0])
+        if args.tc_lookahead is not None:
+            mg.ncc.set_tc_weight_lookahead(args.tc_lookahead)
+
     def worker(j, images, location_host: bool, ends, profile: bool):
         # each host thread owns one stream and the library's per-thread workspace
         torch.cuda.set_device(local)
-        mg.set_correlation_path(path[0])
+        thread_settings()
         st = streams[j]
         if profile:
             mg.profile_reset()
@@ -829,7 +836,7 @@ def main():
         # the batched operator: finds on the library's host threads (one
         # stream each, the calling thread's correlation path), tensor-core
         # launches merged across the finds in flight; results read back
-        mg.set_correlation_path(path[0])
+        thread_settings()
         mg.set_batch_merge(args.cohorts if merge is None else merge)
         return mg.find_ncc_models_batch(images, [model], *ctl, workers=threads)
 
@@ -900,7 +907,7 @@ def main():
     # the same finds one at a time (untimed): per-kernel event times without
     # other streams' kernels interleaved
     def isolated():
-        mg.set_correlation_path(args.path)
+        thread_settings()
         mg.profile_reset()
         mg.profile_enable(True)
         st = streams[0]
@@ -982,7 +989,9 @@ def main():
         "config": {"workload": WORKLOAD, "image": "2048x2048 u8", "template": "128x128", "poses": 5,
                    "angle_range_deg": [-30, 30], "num_levels": 4, "min_score": 0.7, "num_matches": 5,
                    "max_overlap": 0.5, "scenes_per_step": args.batch, "l2": "flushed (256 MiB write) between steps",
-                   "finds_in_flight": threads, "merge_cohorts": args.cohorts, "parallelism": f"replicas x{world}",
+                   "finds_in_flight": threads, "merge_cohorts": args.cohorts,
+                   **({"tc_weight_lookahead": args.tc_lookahead} if args.tc_lookahead is not None else {}),
+                   "parallelism": f"replicas x{world}",
                    "path": ("tensor-core (tcgen05) tracking correlation" if args.path == "tensor"
                             else "plain FP32 CUDA-core correlation")},
         "e2e": {"value": e2e, "unit": "images/s",

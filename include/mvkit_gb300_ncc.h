@@ -297,6 +297,13 @@ MVG_API const char* mvg_last_error(void);
  * return the same matches within the parity tolerances. */
 MVG_API int32_t mvg_set_correlation_path(int32_t path);
 
+/* Grid rows of tensor-core weights the calling thread's finds keep in flight
+ * ahead of the MMAs (1..64; the weight ring gets at least two chunks of
+ * grid rows, the window buffers the rest of shared memory).  A launch-shape
+ * setting only: results do not depend on it.  Batch workers take the
+ * calling thread's value. */
+MVG_API int32_t mvg_set_tc_weight_lookahead(int32_t rows);
+
 /* Per-thread stage profile of finds on this thread: CUDA events recorded on
  * the find's stream around each kernel group while enabled.  Stages 0..12:
  * upload, pyramid, prefix, coarse, nms, track, dedup, score, sort, select,

@@ -335,6 +335,8 @@ size_t tc_launch_smem(const TcPlan& P, size_t optin) {
 // Correlation path of this thread's finds: tensor cores where applicable
 // (0) or FP32 CUDA cores only (1).
 thread_local int t_path = 0;
+// grid rows of tensor-core weights in flight ahead of the MMAs (launch shape only)
+thread_local int t_tc_lookahead = 8;
 // Batched calls from this thread: cohorts of workers whose finds' tensor-core
 // launches are merged (0, default: every find launches its own).
 thread_local int t_merge_tc = 0;
@@ -444,7 +446,7 @@ bool lattice_exact32(double v) {
 // column's row sum for grid row y as two fp16 terms (x 64 likewise), which
 // the centring columns of the window multiply.
 std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, const LevelPlan& lp, int parts,
-                                            float offset, size_t budget) {
+                                            float offset, size_t budget, int lookahead) {
   auto plan = std::make_shared<TcPlan>();
   plan->parts = parts;
   plan->offset = offset;
@@ -530,8 +532,9 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
   plan->npad = (max_n + 31) / 32 * 32;
   plan->sets = std::max(1, std::min(4, 512 / kTcBlocksPerSm / plan->npad));
   // shared memory: weight ring | two window buffers (rows_slab rows each).
-  // The ring holds about eight grid rows of weights ahead of the MMAs (the L2
-  // latency); the window buffers take the rest, at least 16 rows each.
+  // The ring holds `lookahead` grid rows of weights (at least two chunks)
+  // ahead of the MMAs, for the L2 latency; the window buffers take the rest,
+  // at least 16 rows each.  Neither changes a result.
   int max_nseg = 0;
   for (const Proto& pr : protos) max_nseg = std::max(max_nseg, parts * pr.kw / 8 + 2);
   const size_t per_row = size_t(kTcCands) * size_t(max_nseg) * 16;
@@ -540,10 +543,12 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
     plan->group_of_src.assign(nsrc, -1);
     return plan;
   }
-  const int stages = int(std::min<size_t>({size_t(kTcMaxStages), size_t(std::max(2, (8 + min_rg - 1) / min_rg)),
+  const int stages = int(std::min<size_t>({size_t(kTcMaxStages), size_t(std::max(2, (lookahead + min_rg - 1) / min_rg)),
                                            (budget - min_windows) / max_chunk}));
   const size_t ring = size_t(stages) * max_chunk + 1024;
-  const int rows = std::min(std::min(256, (max_kr + 7 + 7) / 8 * 8), int((budget - ring) / 2 / per_row) / 8 * 8);
+  // a slab holds whole chunks of grid rows plus the 7 placement rows; more
+  // rows than the tallest group's grid plus that need are never used
+  const int rows = std::min(std::min(256, max_kr + 3 + 7), int((budget - ring) / 2 / per_row));
   if (rows < 16) {
     // a slab must hold at least one chunk of grid rows plus the 7 placement
     // rows of the window; otherwise the step stays on the CUDA cores
@@ -1313,14 +1318,15 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
       if (!parts) continue;
       DevLevel& T = *m.levels[t];
       const size_t nsrc = m.levels[t + 1]->desc.size();
-      std::vector<int32_t> key{int32_t(parts), int32_t(nsrc)};
+      std::vector<int32_t> key{int32_t(parts), int32_t(nsrc), t_tc_lookahead};
       key.insert(key.end(), plan[t].plist.begin(), plan[t].plist.end());
       key.insert(key.end(), plan[t].sel_off.begin(), plan[t].sel_off.end());
       key.insert(key.end(), plan[t].sel_idx.begin(), plan[t].sel_idx.end());
       auto it = T.tc_plans.find(key);
       if (it == T.tc_plans.end()) {
         if (T.tc_plans.size() >= 32) T.tc_plans.clear();  // finds in flight keep their plans alive
-        it = T.tc_plans.emplace(std::move(key), build_tc_plan(T, nsrc, plan[t], parts, offset, budget)).first;
+        it = T.tc_plans.emplace(std::move(key), build_tc_plan(T, nsrc, plan[t], parts, offset, budget, t_tc_lookahead))
+                 .first;
       }
       if (!it->second->groups.empty()) tc[t] = it->second;
     }
@@ -1355,7 +1361,7 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
       vp.plist = plan[top].plist;
       vp.sel_off = vsel_off;
       vp.sel_idx = vsel_idx;
-      std::vector<int32_t> key{-1, int32_t(parts), int32_t(nsrc)};
+      std::vector<int32_t> key{-1, int32_t(parts), int32_t(nsrc), t_tc_lookahead};
       key.insert(key.end(), vp.plist.begin(), vp.plist.end());
       key.insert(key.end(), vsel_off.begin(), vsel_off.end());
       key.insert(key.end(), vsel_idx.begin(), vsel_idx.end());
@@ -1363,7 +1369,8 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
       auto it = T.tc_plans.find(key);
       if (it == T.tc_plans.end()) {
         if (T.tc_plans.size() >= 32) T.tc_plans.clear();
-        it = T.tc_plans.emplace(std::move(key), build_tc_plan(T, nsrc, vp, parts, offset, budget)).first;
+        it = T.tc_plans.emplace(std::move(key), build_tc_plan(T, nsrc, vp, parts, offset, budget, t_tc_lookahead))
+                 .first;
       }
       // every virtual source must have its group: the lattice covers them all
       bool all = !it->second->groups.empty();
@@ -2767,7 +2774,7 @@ int32_t mvg_find_ncc_models_batch(const void* const* images, const int32_t* pixe
                                             n_num_levels);
     int device = 0;
     check(cudaGetDevice(&device), "batch");
-    const int path = t_path;
+    const int path = t_path, lookahead = t_tc_lookahead;
     const Budgets budgets = thread_budgets();
     std::vector<BatchImage> done(static_cast<size_t>(num_images));
     std::atomic<int64_t> next{0};
@@ -2794,6 +2801,7 @@ int32_t mvg_find_ncc_models_batch(const void* const* images, const int32_t* pixe
       } member{batcher};
       if (cudaSetDevice(device) != cudaSuccess) return;
       t_path = path;
+      t_tc_lookahead = lookahead;
       thread_budgets() = budgets;
       t_batcher = batcher;
       for (int64_t i; (i = next.fetch_add(1)) < num_images;) {
@@ -3061,6 +3069,13 @@ int32_t mvg_set_correlation_path(int32_t path) {
   return guarded([&] {
     if (path != 0 && path != 1) raise(kInvalidArgument, "path must be 0 (tensor cores) or 1 (CUDA cores)");
     t_path = path;
+  });
+}
+
+int32_t mvg_set_tc_weight_lookahead(int32_t rows) {
+  return guarded([&] {
+    if (rows < 1 || rows > 64) raise(kInvalidArgument, "weight lookahead must be 1..64 grid rows");
+    t_tc_lookahead = rows;
   });
 }
 

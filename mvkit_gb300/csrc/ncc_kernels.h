@@ -155,7 +155,7 @@ struct TcGroup {
   int rmin, cmin;                        // grid origin relative to the placement centre
   int p, rg, n;                          // patches; grid rows per chunk (N columns side by side);
                                          // MMA N (10 p rg rounded up to 16)
-  int rows_slab;                         // window rows per staged slab (multiple of 8, >= 16)
+  int rows_slab;                         // window rows per staged slab (>= 16)
   float inv_scale;                       // 1 / weight scale
   int k_of[kTcMaxP];                     // index in the candidate's selected list
   int r0[kTcMaxP], c0[kTcMaxP];          // first sample offset of each patch
@@ -213,7 +213,8 @@ struct TcLaunch {
 
 // fp16 planes of a level for the tensor-core tracking: parts x 8 shifted
 // copies (plane d holds level column x - kTcPlaneMargin + d at x), `pitch`
-// elements per row (a multiple of 8, at least the level width + 8).
+// columns (a multiple of 8, at least the level width + 8), column-blocked:
+// (row y, column x) at ((x / 8) h + y) 8 + x mod 8.
 cudaError_t launch_tc_planes(const LevelImage& lev, uint16_t* planes, int pitch, int parts, float offset,
                              cudaStream_t s, const QueryState* state = nullptr, float level_mult = 1.f);
 // Range of the level-0 crop into state->pix_min / pix_max (uint16 finds).

@@ -20,12 +20,14 @@
 // path's window centring).  Chunks accumulate round-robin into up to four
 // accumulator sets in tensor memory, summed in FP32 by the epilogue.
 // Windows come straight from fp16 copies of the level ("planes", exact
-// integers: the level minus a constant, split into a high and a low plane
-// when a level's values exceed fp16's integer range), 16 bytes per cp.async,
-// into the canonical no-swizzle K-major layout whose row pitch is 16 bytes,
-// so grid row y is the same tiles started y rows later.  Eight
-// column-shifted copies of each plane keep every copy on a 16-byte boundary;
-// planes start 8 columns left of the level.  Weights (fp16 high and low
+// integers: the level minus an offset, as one to four base-64 digit planes
+// when a level's values exceed fp16's integer range), one bulk copy (TMA
+// engine) per candidate and 8-column segment, into the canonical
+// no-swizzle K-major layout whose row pitch is 16 bytes, so grid row y is
+// the same tiles started y rows later.  The planes are column-blocked (the
+// rows of an 8-column block contiguous), eight column-shifted copies keep
+// every segment on a 16-byte boundary, and planes start 8 columns left of
+// the level.  Weights (fp16 high and low
 // halves of the scaled weights) stream through a ring of shared-memory
 // buffers with bulk copies (TMA engine).  The block is warp-specialised:
 // four set-up and window-producer warps (two slab buffers), a
@@ -85,6 +87,11 @@ __device__ __forceinline__ void expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
 
+// raises the current phase's expected transaction bytes without arriving
+__device__ __forceinline__ void expect_tx_only(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
 // bounded wait for the completion of the phase with parity `parity`
 __device__ __forceinline__ unsigned long long global_ns() {
   unsigned long long t;
@@ -118,12 +125,6 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                    smem_u32(dst)),
                "l"(src), "r"(bytes), "r"(smem_u32(bar))
-               : "memory");
-}
-
-// 16 bytes global -> shared, zero-filled when `valid` is false
-__device__ __forceinline__ void cp_async16(void* dst, const void* src, bool valid) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(valid ? 16 : 0)
                : "memory");
 }
 
@@ -271,59 +272,74 @@ __device__ bool tc_mma_tile(const TcArgs& a, const TcSlot& ts, TcShared& sh, uin
 }
 
 // Window producers (four warps), one tile: per slab, once the MMAs of the
-// slab that last used the buffer are done, 16-byte cp.async copies from the
-// planes (zero outside them) and the centring columns of the tile's
-// candidates; a warp's copies are 8 rows x 4 segments, so its global reads
-// are 64-byte row pieces and its shared writes 128-byte row runs.  Each
-// thread waits for its own copies, orders its writes for the tensor cores
-// (proxy fence) and arrives on the buffer's barrier (128 arrivals).  Rows of
-// candidates beyond the tile's count are left as they are: their
+// slab that last used the buffer are done, one bulk copy (TMA engine) per
+// (candidate, plane segment) of the slab's rows that lie inside the level:
+// the planes are column-blocked, so a segment's rows are contiguous in
+// global memory and land as one run of 16-byte rows, the canonical
+// no-swizzle layout.  Rows outside the level and segments outside the plane
+// are zeroed by plain stores, as are the centring columns of the tile's
+// candidates.  Each thread announces its copies' bytes on the buffer's
+// barrier, orders its own stores for the tensor cores (proxy fence) and
+// arrives (128 arrivals); the phase completes when every byte has landed.
+// Rows of candidates beyond the tile's count are left as they are: their
 // accumulator rows are never read.
 __device__ bool tc_window_tile(const TcArgs& a, const TcSlot& ts, TcShared& sh, uint8_t* abase, int& sa, int pt) {
   const TcGroup& G = ts.grp;
   const TcShape sp(G);
-  const int cnt = ts.cnt, rows = G.rows_slab, H = a.lev.h, pitch = a.plane_pitch;
-  const size_t plane = size_t(H) * size_t(pitch);
-  const int lane = pt & 31, wp = pt >> 5;
-  const int rblocks = rows / 8;
+  const int cnt = ts.cnt, rows = G.rows_slab, H = a.lev.h, groups = a.plane_pitch / 8;
+  const size_t plane = size_t(H) * size_t(a.plane_pitch);     // elements of one shifted plane
   const size_t part_stride = size_t(kTcPlaneShifts) * plane;  // one part's planes -> the next part's
+  const int ncopies = cnt * sp.nplane;
   const int g_first = pt / rows, r_first = pt - g_first * rows;  // first centring row of this thread
+  const uint4 zero = make_uint4(0, 0, 0, 0);
   for (int sl = 0; sl < sp.nslabs; ++sl) {
     const int buf = sa & 1;
     if (sa >= 2 && !bar_wait(&sh.slab_done[buf], uint32_t(((sa >> 1) - 1) & 1), &sh.fail)) return false;
     uint8_t* dst0 = abase + size_t(buf) * a.abuf_bytes;
     const int y0 = sl * sp.Y;
-    // warp wp stages candidates wp, wp + 4, ...; lane = (row in an 8-row block,
-    // segment in a 4-segment block)
-    for (int g = wp; g < cnt; g += kTcWindowThreads / 32) {
-      const int row0 = ts.R[g] - 2 + G.rmin + y0 + (lane & 7);
-      const int x0 = ts.x0a[g] + kTcPlaneMargin;
-      const uint16_t* pbase = a.planes + size_t(ts.delta[g]) * plane;
-      uint8_t* dg = dst0 + size_t(g) * sp.sbo + size_t(lane & 7) * 16;
-      for (int rb = 0; rb < rblocks; ++rb) {
-        const int row = row0 + rb * 8;
-        const bool rok = row >= 0 && row < H;
-        for (int sg = lane >> 3; sg < sp.nplane; sg += 4) {
-          const int q = sg / sp.segs;  // part of the level value
-          const int x = x0 + 8 * (sg - q * sp.segs);
-          const bool valid = rok && x >= 0 && x + 8 <= pitch;
-          const uint16_t* src = pbase + size_t(q) * part_stride + (valid ? size_t(row) * pitch + x : 0);
-          cp_async16(dg + size_t(sg) * sp.lbo + size_t(rb) * 128, src, valid);
-        }
+    // copy i = (candidate g, segment sg): rows [lo, hi) of the slab lie in the level
+    auto piece = [&](int i, int& g, int& sg, int& xb, int& lo, int& hi) {
+      g = i / sp.nplane;
+      sg = i - g * sp.nplane;
+      const int q = sg / sp.segs;  // part of the level value
+      xb = (ts.x0a[g] + kTcPlaneMargin) / 8 + (sg - q * sp.segs);
+      const int row0 = ts.R[g] - 2 + G.rmin + y0;
+      lo = min(rows, max(0, -row0));
+      hi = max(lo, min(rows, H - row0));
+      if (xb < 0 || xb >= groups) hi = lo;  // outside the plane: all zero
+      return q;
+    };
+    uint32_t bytes = 0;
+    for (int i = pt; i < ncopies; i += kTcWindowThreads) {
+      int g, sg, xb, lo, hi;
+      piece(i, g, sg, xb, lo, hi);
+      bytes += uint32_t(hi - lo) * 16u;
+    }
+    if (bytes) expect_tx_only(&sh.a_full[buf], bytes);
+    for (int i = pt; i < ncopies; i += kTcWindowThreads) {
+      int g, sg, xb, lo, hi;
+      const int q = piece(i, g, sg, xb, lo, hi);
+      uint8_t* dst = dst0 + size_t(g) * sp.sbo + size_t(sg) * sp.lbo;
+      if (hi > lo) {
+        const int row0 = ts.R[g] - 2 + G.rmin + y0;
+        const uint16_t* src = a.planes + size_t(q) * part_stride + size_t(ts.delta[g]) * plane +
+                              (size_t(xb) * size_t(H) + size_t(row0 + lo)) * 8;
+        bulk_load(dst + size_t(lo) * 16, src, uint32_t(hi - lo) * 16u, &sh.a_full[buf]);
       }
+      for (int r = 0; r < lo; ++r) *reinterpret_cast<uint4*>(dst + size_t(r) * 16) = zero;
+      for (int r = max(hi, lo); r < rows; ++r) *reinterpret_cast<uint4*>(dst + size_t(r) * 16) = zero;
     }
     // centring columns: (candidate g, row r) for g < cnt, 128 rows apart
     for (int g = g_first, r = r_first; g < cnt;) {
       uint8_t* row = dst0 + size_t(g) * sp.sbo + size_t(sp.nplane) * sp.lbo + size_t(r) * 16;
       *reinterpret_cast<uint4*>(row) = ts.cwords[g];
-      *reinterpret_cast<uint4*>(row + sp.lbo) = make_uint4(0, 0, 0, 0);
+      *reinterpret_cast<uint4*>(row + sp.lbo) = zero;
       r += kTcWindowThreads;
       while (r >= rows) {
         r -= rows;
         ++g;
       }
     }
-    asm volatile("cp.async.commit_group;\n cp.async.wait_group 0;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     bar_arrive(&sh.a_full[buf]);
     ++sa;
@@ -664,41 +680,52 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
 }
 
-// fp16 planes: thread = 8 consecutive columns of one (shift, row); plane d
-// holds level column x - kTcPlaneMargin + d at column x
+// fp16 planes: thread = one row and one 8-column block, all 8 shifted
+// planes (plane d holds level column x - kTcPlaneMargin + d at column x, so
+// the block's planes need level columns 8 gx - 8 .. 8 gx + 6, read once),
+// column-blocked: element (row y, column x) at ((x / 8) h + y) 8 + x mod 8,
+// so the rows of an 8-column block are one contiguous run of 16-byte rows;
+// consecutive threads take consecutive rows (coalesced stores)
 template <int Parts>
 __global__ void tc_planes_kernel(LevelImage lev, __half* planes, int pitch, float fixed_offset,
                                  const QueryState* state, float level_mult) {
   const float offset = tc_plane_offset(fixed_offset, state, level_mult);
   const int groups = pitch / 8;
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long total = (long long)kTcPlaneShifts * lev.h * groups;
-  if (idx >= total) return;
-  const int gx = int(idx % groups);
-  const int y = int((idx / groups) % lev.h);
-  const int d = int(idx / ((long long)groups * lev.h));
-  __align__(16) __half pv[Parts][8];
+  if (idx >= (long long)lev.h * groups) return;
+  const int y = int(idx % lev.h);
+  const int gx = int(idx / lev.h);
+  const int x0 = gx * 8 - kTcPlaneMargin;
+  const float* row = lev.v + size_t(y) * lev.w;
+  float v[15];
 #pragma unroll
-  for (int e = 0; e < 8; ++e) {
-    const int x = gx * 8 + e + d - kTcPlaneMargin;
-    const float v = x >= 0 && x < lev.w ? lev.v[size_t(y) * lev.w + x] - offset : 0.f;
-    // v = sum_q digit_q 64^(Parts - 1 - q): the first digit signed, the
-    // others in [0, 64); every step is exact in float (|v| < 2^24)
-    float r = v;
-#pragma unroll
-    for (int q = 0; q < Parts; ++q) {
-      const float unit = float(1 << (6 * (Parts - 1 - q)));
-      const float dq = q + 1 < Parts ? floorf(r * (1.f / unit)) : r;
-      pv[q][e] = __float2half_rn(dq);
-      r -= dq * unit;
-    }
+  for (int j = 0; j < 15; ++j) {
+    const int x = x0 + j;
+    v[j] = x >= 0 && x < lev.w ? row[x] - offset : 0.f;
   }
   const size_t plane = size_t(lev.h) * pitch;
-  const size_t at = (size_t(d) * lev.h + y) * pitch + size_t(gx) * 8;
+  const size_t at = (size_t(gx) * lev.h + y) * 8;
 #pragma unroll
-  for (int q = 0; q < Parts; ++q)
-    *reinterpret_cast<uint4*>(planes + size_t(q) * kTcPlaneShifts * plane + at) =
-        *reinterpret_cast<const uint4*>(pv[q]);
+  for (int d = 0; d < kTcPlaneShifts; ++d) {
+    __align__(16) __half pv[Parts][8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      // v = sum_q digit_q 64^(Parts - 1 - q): the first digit signed, the
+      // others in [0, 64); every step is exact in float (|v| < 2^24)
+      float r = v[e + d];
+#pragma unroll
+      for (int q = 0; q < Parts; ++q) {
+        const float unit = float(1 << (6 * (Parts - 1 - q)));
+        const float dq = q + 1 < Parts ? floorf(r * (1.f / unit)) : r;
+        pv[q][e] = __float2half_rn(dq);
+        r -= dq * unit;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < Parts; ++q)
+      *reinterpret_cast<uint4*>(planes + (size_t(q) * kTcPlaneShifts + d) * plane + at) =
+          *reinterpret_cast<const uint4*>(pv[q]);
+  }
 }
 
 // Grouping of the step's candidates: counts per group, tile list, order.
@@ -768,7 +795,7 @@ size_t tc_kernel_static_smem() { return sizeof(TcShared); }
 
 cudaError_t launch_tc_planes(const LevelImage& lev, uint16_t* planes, int pitch, int parts, float offset,
                              cudaStream_t s, const QueryState* state, float level_mult) {
-  const long long total = (long long)kTcPlaneShifts * lev.h * (pitch / 8);
+  const long long total = (long long)lev.h * (pitch / 8);
   const unsigned blocks = unsigned((total + 255) / 256);
   __half* p = reinterpret_cast<__half*>(planes);
   switch (parts) {

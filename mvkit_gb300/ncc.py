@@ -748,6 +748,15 @@ def set_correlation_path(path: str) -> None:
     _check(lib.mvg_set_correlation_path(0 if path == "tensor" else 1), "set_correlation_path")
 
 
+def set_tc_weight_lookahead(rows: int) -> None:
+    """Grid rows of tensor-core weights this thread's finds keep in flight
+    ahead of the MMAs (1..64); a launch-shape setting, results do not change."""
+    lib = load()
+    lib.mvg_set_tc_weight_lookahead.argtypes = [C.c_int32]
+    lib.mvg_set_tc_weight_lookahead.restype = C.c_int32
+    _check(lib.mvg_set_tc_weight_lookahead(int(rows)), "set_tc_weight_lookahead")
+
+
 def set_budgets(samples: int = 0, pixels: int = 0, candidates: int = 0) -> None:
     """Extended mode: this thread's model-raster sample, search-image pixel and
     coarse-candidate budgets (0 = the reference's 16 000 000, 32 000 000 and

@@ -110,3 +110,16 @@ def test_noalloc_pyramid_refuses_misaligned_and_host_pointers_without_launching(
     assert f(base, 0, 64, 600000, 64, 0, obase, 64 * 64, C.byref(ow), C.byref(oh), None) == -103
     st = f(base, 1, 64, 64, 128, 1, obase, 64 * 64, C.byref(ow), C.byref(oh), None)
     assert st in (-1, -1000) and lib.mvg_last_error()
+
+
+def test_launch_shape_settings_checked():
+    """The tensor-core weight lookahead is a launch-shape setting: values out
+    of range are refused with InvalidArgument (-1), values in range are taken
+    (no device needed)."""
+    for bad in (0, 65, -3):
+        with pytest.raises(mg.MvError) as e:
+            ncc.set_tc_weight_lookahead(bad)
+        assert e.value.status == -1
+    for good in (1, 8, 24, 64):
+        ncc.set_tc_weight_lookahead(good)
+    ncc.set_tc_weight_lookahead(8)
