@@ -8,12 +8,15 @@ A step is one find on each of `--batch` distinct scenes.
 
 value: images/s with the scenes resident in HBM, through the batched operator
 (mvg_find_ncc_models_batch: 32 finds in flight on the library's host
-threads, their tensor-core launches merged), CUDA events around each step's
-call, L2 flushed between steps.  e2e: the same calls on page-locked host
-images, wall clock around each step (upload, the finds and the result
-read-back inside the timed region).  roofline: the merged tensor-core
-launches of the value pass, all finds' algorithmic multiply-adds over the
-launches' event time; beside it the same kernel launched per find.
+threads, each launching its own kernels; --cohorts k merges their
+tensor-core launches), CUDA events around each step's call, L2 flushed
+between steps.  e2e: the same calls on page-locked host images, wall clock
+around each step (upload, the finds and the result read-back inside the
+timed region).  roofline: the correlation kernel's algorithmic
+multiply-adds over its event time in a profiled pass of the same steps
+(per-find stage events on the find streams), or over the merged launches'
+event time when the value pass merges; beside it the other launch policy
+and the same finds one at a time.
 cpu_baseline: the FP64 oracle restatement of the reference on this host's
 cores (one scene per thread); its matches are the parity check of the value
 pass's poses.
@@ -962,7 +965,10 @@ def main():
     else:
         achieved = achieved_sep
         note = (f"algorithmic correlation FLOPs (2 x MACs) over the stage's event time; peak = {pk['source']} "
-                f"dense bf16 sustained; FP32 CUDA cores")
+                f"dense bf16 sustained; "
+                + ("fp16 operands (exact integer digits), FP32 accumulation in tensor memory; issued/algorithmic "
+                   f"MACs = {prof.get('tensor_issued_macs', 0.0) / max(1.0, d['work']):.2f}"
+                   if rstage == "track_tc" else "FP32 CUDA cores"))
         ms_per_launch = d["ms"] / max(1, d["launches"])
     roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak if achieved else None,
