@@ -530,7 +530,9 @@ std::shared_ptr<const TcPlan> build_tc_plan(const DevLevel& T, size_t nsrc, cons
     max_n = std::max(max_n, pr.n);
   }
   plan->npad = (max_n + 31) / 32 * 32;
-  plan->sets = std::max(1, std::min(4, 512 / kTcBlocksPerSm / plan->npad));
+  // two accumulator regions (the next tile's MMAs run while the epilogue
+  // reads the last one), each sets x npad columns
+  plan->sets = std::max(1, std::min(4, 256 / kTcBlocksPerSm / plan->npad));
   // shared memory: weight ring | two window buffers (rows_slab rows each).
   // The ring holds `lookahead` grid rows of weights (at least two chunks)
   // ahead of the MMAs, for the L2 latency; the window buffers take the rest,

@@ -49,7 +49,8 @@ constexpr int kTcThreads = 320;  // warp 0 MMA, warp 1 weights, warps 2-5 set-up
 constexpr int kTcWindowThreads = 128;
 constexpr int kTcEpilogueThreads = 128;
 constexpr int kTcRows = 128;                  // MMA M
-constexpr uint32_t kTmemCols = 512 / kTcBlocksPerSm;  // accumulator sets x columns per set
+constexpr uint32_t kTmemCols = 512 / kTcBlocksPerSm;  // two accumulator regions
+constexpr uint32_t kTcRegionCols = kTmemCols / 2;      // accumulator sets x columns per set, per region
 constexpr unsigned long long kWaitNs = 1000000000ull;  // an mbarrier wait gives up after one second
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
@@ -162,7 +163,7 @@ struct __align__(16) TcShared {
   uint64_t a_full[2], slab_done[2], drain;
   uint64_t b_full[kTcMaxStages], b_empty[kTcMaxStages];
   uint64_t info_full[2], info_empty[2];  // tile slots
-  uint64_t acc_full, acc_empty;          // the tile's accumulators in tensor memory
+  uint64_t acc_full[2], acc_empty[2];    // accumulator regions in tensor memory (tile s: region s mod 2)
   TcSlot slot[2];
   int job_base[kTcMaxJobs + 1];  // first launch tile of each job
   uint32_t tmem;
@@ -230,7 +231,7 @@ struct RingPos {
 // y mod sets and release the weight buffer; release the window buffer after
 // the slab, and the accumulators to the epilogue after the tile.
 __device__ bool tc_mma_tile(const TcArgs& a, const TcSlot& ts, TcShared& sh, uint8_t* wbase, uint8_t* abase,
-                            uint32_t tmem, RingPos& cm, int& sm) {
+                            uint32_t tmem, uint64_t* acc_full, RingPos& cm, int& sm) {
   const TcGroup& G = ts.grp;
   const TcShape sp(G);
   const int S = a.stages;
@@ -267,7 +268,7 @@ __device__ bool tc_mma_tile(const TcArgs& a, const TcSlot& ts, TcShared& sh, uin
     mma_commit(&sh.slab_done[buf]);
     ++sm;
   }
-  mma_commit(&sh.acc_full);
+  mma_commit(acc_full);
   return true;
 }
 
@@ -494,8 +495,9 @@ __device__ void tc_epilogue(const TcArgs& a, const TcSlot& ts, uint32_t trow, in
 // stride leaves blocks idle at the end).  Warp 0 issues the MMAs, warp 1
 // streams weights, warps 2-5 set up tiles and stage windows, warps 6-9 run
 // the epilogue.  Two tile slots let the set-up, windows and weights of the
-// next tile go ahead while the MMAs of this one run; the MMAs of the next
-// tile start once the epilogue has read the accumulators.  Shared memory:
+// next tile go ahead while the MMAs of this one run, and two accumulator
+// regions in tensor memory (tile s in region s mod 2) let the next tile's
+// MMAs run while the epilogue reads this one.  Shared memory:
 // weight ring (stages x stage_bytes) | two window buffers, the same for
 // every job of the launch.  Every wait is bounded; a role that gives up
 // makes the others leave, the block drains its copies and MMAs and flags
@@ -542,8 +544,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       bar_init(&sh.info_full[b]);
       bar_init(&sh.info_empty[b], 3);  // MMA thread, weight producer, epilogue
     }
-    bar_init(&sh.acc_full);
-    bar_init(&sh.acc_empty);
+    for (int b = 0; b < 2; ++b) {
+      bar_init(&sh.acc_full[b]);
+      bar_init(&sh.acc_empty[b]);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     sh.fail = 0;
     sh.cm = sh.cb = 0;
@@ -569,13 +573,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         const TcSlot& ts = sh.slot[b];
         if (ts.gtile < 0) break;
-        // the previous tile's accumulators have been read
-        if (s > 0 && !bar_wait(&sh.acc_empty, uint32_t((s - 1) & 1), &sh.fail)) {
+        // the region's previous tile (s - 2) has been read by the epilogue
+        if (s >= 2 && !bar_wait(&sh.acc_empty[b], uint32_t(((s >> 1) - 1) & 1), &sh.fail)) {
           tc_fail(sh);
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        if (!tc_mma_tile(Multi ? ts.job : L.single, ts, sh, wbase, abase, tmem, cm, sm)) {
+        if (!tc_mma_tile(Multi ? ts.job : L.single, ts, sh, wbase, abase, tmem + uint32_t(b) * kTcRegionCols,
+                         &sh.acc_full[b], cm, sm)) {
           tc_fail(sh);
           break;
         }
@@ -629,7 +634,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   } else {
     // epilogue warps (named barrier 2)
     const int quarter = warp & 3, et = t - 192;
-    const uint32_t trow = tmem + (uint32_t(quarter * 32) << 16);
     for (int s = 0;; ++s) {
       const int b = s & 1;
       bool ok = bar_wait(&sh.info_full[b], uint32_t((s >> 1) & 1), &sh.fail);
@@ -639,13 +643,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
       const TcSlot& ts = sh.slot[b];
       if (ts.gtile < 0) break;
-      ok = bar_wait(&sh.acc_full, uint32_t(s & 1), &sh.fail);
+      ok = bar_wait(&sh.acc_full[b], uint32_t((s >> 1) & 1), &sh.fail);
       if (!named_and(2, kTcEpilogueThreads, ok)) {
         tc_fail(sh);
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const TcArgs& a = Multi ? ts.job : L.single;
+      const uint32_t trow = tmem + (uint32_t(quarter * 32) << 16) + uint32_t(b) * kTcRegionCols;
       if (ts.grp.rg == 4)
         tc_epilogue<4>(a, ts, trow, quarter, lane);
       else if (ts.grp.rg == 2)
@@ -655,7 +660,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       named_sync(2, kTcEpilogueThreads);
       if (et == 0) {
-        bar_arrive(&sh.acc_empty);
+        bar_arrive(&sh.acc_empty[b]);
         const TcGroup& G = ts.grp;
         atomicAdd(&a.state_rw->tc_macs, (unsigned long long)G.macs * (unsigned long long)ts.cnt);
         atomicAdd(&a.state_rw->tc_issued,
