@@ -30,9 +30,9 @@
 // the level.  Weights (fp16 high and low
 // halves of the scaled weights) stream through a ring of shared-memory
 // buffers with bulk copies (TMA engine).  The block is warp-specialised:
-// four set-up and window-producer warps (two slab buffers), a
-// weight-producer thread, an MMA-issue thread and four epilogue warps, with
-// two tiles in flight; accumulation is FP32 in tensor memory.  The epilogue
+// four window-producer warps (two slab buffers), a weight-producer
+// thread, an MMA-issue thread and four epilogue warps that also set up the
+// tiles, with two tiles in flight; accumulation is FP32 in tensor memory.  The epilogue
 // writes sum w (S - S0) per placement; track_kernel adds the exact integer
 // window moments and applies the reference's selection rule.
 #include <cuda_fp16.h>
@@ -45,7 +45,7 @@
 namespace mvg {
 namespace {
 
-constexpr int kTcThreads = 320;  // warp 0 MMA, warp 1 weights, warps 2-5 set-up and windows, warps 6-9 epilogue
+constexpr int kTcThreads = 320;  // warp 0 MMA, warp 1 weights, warps 2-5 windows, warps 6-9 epilogue and set-up
 constexpr int kTcWindowThreads = 128;
 constexpr int kTcEpilogueThreads = 128;
 constexpr int kTcRows = 128;                  // MMA M
@@ -146,9 +146,9 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 
-// One tile in flight: its set-up, written by the window warps and shared
+// One tile in flight: its set-up, written by the epilogue warps and shared
 // with the other roles (info_full hands it over; info_empty, arrived by the
-// MMA thread, the weight producer and the epilogue, hands the slot back).
+// MMA thread, the weight producer and the window warps, hands the slot back).
 struct __align__(16) TcSlot {
   TcArgs job;    // the tile's job (job tables only)
   TcGroup grp;
@@ -168,7 +168,7 @@ struct __align__(16) TcShared {
   int job_base[kTcMaxJobs + 1];  // first launch tile of each job
   uint32_t tmem;
   int fail;
-  int claim;         // the window warps' next tile (broadcast)
+  int claim;         // the epilogue warps' next tile (broadcast)
   long long cm, cb;  // weight chunks consumed (MMA thread) / loaded (weight producer), at exit
 };
 
@@ -367,8 +367,8 @@ __device__ bool tc_weight_tile(const TcArgs& a, const TcSlot& ts, TcShared& sh, 
   return true;
 }
 
-// Tile set-up (the window warps): the tile's job (job tables), group and
-// candidates into the slot, one candidate per thread.
+// Tile set-up (the epilogue warps, 128 threads): the tile's job (job
+// tables), group and candidates into the slot, one candidate per thread.
 template <bool Multi>
 __device__ void tc_setup(const TcArgs* jobs, const TcShared& sh, TcSlot& ts, int gtile, int ntiles, int pt) {
   if (gtile >= ntiles) {
@@ -383,14 +383,14 @@ __device__ void tc_setup(const TcArgs* jobs, const TcShared& sh, TcSlot& ts, int
   if (Multi) {
     const uint32_t* src = reinterpret_cast<const uint32_t*>(&a);
     uint32_t* dst = reinterpret_cast<uint32_t*>(&ts.job);
-    for (int w = pt; w < int(sizeof(TcArgs) / 4); w += kTcWindowThreads) dst[w] = src[w];
+    for (int w = pt; w < int(sizeof(TcArgs) / 4); w += kTcEpilogueThreads) dst[w] = src[w];
   }
   const int gi = a.tiles->group[tile];
   const TcGroup& gsrc = a.groups[gi];
   {
     const uint32_t* src = reinterpret_cast<const uint32_t*>(&gsrc);
     uint32_t* dst = reinterpret_cast<uint32_t*>(&ts.grp);
-    for (int w = pt; w < int(sizeof(TcGroup) / 4); w += kTcWindowThreads) dst[w] = src[w];
+    for (int w = pt; w < int(sizeof(TcGroup) / 4); w += kTcEpilogueThreads) dst[w] = src[w];
   }
   const int first = a.tiles->first[tile];
   const int cnt = min(kTcCands, a.tiles->last[tile] - first);
@@ -493,8 +493,9 @@ __device__ void tc_epilogue(const TcArgs& a, const TcSlot& ts, uint32_t trow, in
 // those of its jobs in job order; block b takes tile b first, then the next
 // unclaimed tile from a global counter (tiles differ in cost, so a static
 // stride leaves blocks idle at the end).  Warp 0 issues the MMAs, warp 1
-// streams weights, warps 2-5 set up tiles and stage windows, warps 6-9 run
-// the epilogue.  Two tile slots let the set-up, windows and weights of the
+// streams weights, warps 2-5 stage windows, warps 6-9 run the epilogue and
+// set up the tiles (tile s + 2 after the epilogue of tile s, in the slot it
+// frees).  Two tile slots let the set-up, windows and weights of the
 // next tile go ahead while the MMAs of this one run, and two accumulator
 // regions in tensor memory (tile s in region s mod 2) let the next tile's
 // MMAs run while the epilogue reads this one.  Shared memory:
@@ -542,7 +543,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     for (int b = 0; b < 2; ++b) {
       bar_init(&sh.info_full[b]);
-      bar_init(&sh.info_empty[b], 3);  // MMA thread, weight producer, epilogue
+      bar_init(&sh.info_empty[b], 2 + kTcWindowThreads);  // MMA thread, weight producer, window warps
     }
     for (int b = 0; b < 2; ++b) {
       bar_init(&sh.acc_full[b]);
@@ -610,40 +611,43 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     __syncwarp();
   } else if (warp < 6) {
-    // window warps (named barrier 1): claim, set up, stage
+    // window warps: stage the tiles the epilogue warps set up
     const int pt = t - 64;
     int sa = 0;
-    bool ok = true;
     for (int s = 0;; ++s) {
       const int b = s & 1;
-      // the slot's previous tile (s - 2) is done
-      if (ok && s >= 2) ok = bar_wait(&sh.info_empty[b], uint32_t(((s >> 1) - 1) & 1), &sh.fail);
-      if (ok && pt == 0) sh.claim = s == 0 ? int(blockIdx.x) : int(gridDim.x) + atomicAdd(L.next, 1);
-      if (!named_and(1, kTcWindowThreads, ok)) {
-        tc_fail(sh);
-        break;
-      }
-      const int gtile = sh.claim;
-      tc_setup<Multi>(jobs, sh, sh.slot[b], gtile, ntiles, pt);
-      named_sync(1, kTcWindowThreads);
-      if (pt == 0) bar_arrive(&sh.info_full[b]);
-      if (gtile >= ntiles) break;
-      const TcSlot& ts = sh.slot[b];
-      ok = tc_window_tile(Multi ? ts.job : L.single, ts, sh, abase, sa, pt);
-    }
-  } else {
-    // epilogue warps (named barrier 2)
-    const int quarter = warp & 3, et = t - 192;
-    for (int s = 0;; ++s) {
-      const int b = s & 1;
-      bool ok = bar_wait(&sh.info_full[b], uint32_t((s >> 1) & 1), &sh.fail);
-      if (!named_and(2, kTcEpilogueThreads, ok)) {
+      if (!bar_wait(&sh.info_full[b], uint32_t((s >> 1) & 1), &sh.fail)) {
         tc_fail(sh);
         break;
       }
       const TcSlot& ts = sh.slot[b];
       if (ts.gtile < 0) break;
-      ok = bar_wait(&sh.acc_full[b], uint32_t((s >> 1) & 1), &sh.fail);
+      if (!tc_window_tile(Multi ? ts.job : L.single, ts, sh, abase, sa, pt)) {
+        tc_fail(sh);
+        break;
+      }
+      bar_arrive(&sh.info_empty[b]);
+    }
+  } else {
+    // epilogue warps (named barrier 2): the epilogue of tile s, then the
+    // set-up of tile s + 2 in the slot it frees (tiles 0 and 1 first)
+    const int quarter = warp & 3, et = t - 192;
+    auto setup = [&](int sq) {
+      if (et == 0) sh.claim = sq == 0 ? int(blockIdx.x) : int(gridDim.x) + atomicAdd(L.next, 1);
+      named_sync(2, kTcEpilogueThreads);
+      const int gtile = sh.claim;
+      tc_setup<Multi>(jobs, sh, sh.slot[sq & 1], gtile, ntiles, et);
+      named_sync(2, kTcEpilogueThreads);
+      if (et == 0) bar_arrive(&sh.info_full[sq & 1]);
+      return gtile < ntiles;
+    };
+    bool more = setup(0);
+    if (more) more = setup(1);
+    for (int s = 0;; ++s) {
+      const int b = s & 1;
+      const TcSlot& ts = sh.slot[b];
+      if (ts.gtile < 0) break;
+      bool ok = bar_wait(&sh.acc_full[b], uint32_t((s >> 1) & 1), &sh.fail);
       if (!named_and(2, kTcEpilogueThreads, ok)) {
         tc_fail(sh);
         break;
@@ -665,7 +669,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         atomicAdd(&a.state_rw->tc_macs, (unsigned long long)G.macs * (unsigned long long)ts.cnt);
         atomicAdd(&a.state_rw->tc_issued,
                   (unsigned long long)kTcRows * G.n * (G.parts * G.kw + 16) * ((G.kr + G.rg - 1) / G.rg));
-        bar_arrive(&sh.info_empty[b]);
+      }
+      if (more) {
+        // the MMA thread, the weight producer and the window warps are done with tile s
+        ok = bar_wait(&sh.info_empty[b], uint32_t((s >> 1) & 1), &sh.fail);
+        if (!named_and(2, kTcEpilogueThreads, ok)) {
+          tc_fail(sh);
+          break;
+        }
+        more = setup(s + 2);
       }
     }
   }
