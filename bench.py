@@ -501,6 +501,10 @@ def run_config(args) -> None:
         "gpu_launches": int(sum(v["launches"] for v in stages.values()) * args.steps),
         "clocks": clocks.summary(),
         "matches_per_image": [None if isinstance(r, mg.MvError) else len(r[0]) for r in found],
+        # event time per stage, summed over the profiled pass's finds on all
+        # its host threads (finds overlap, so the sum exceeds a step's time)
+        "stages_ms_profiled_pass": {k: round(v["ms"], 1) for k, v in stages.items()},
+        "profiled_finds": finds,
         "pose_error": pose,
     }
     if not args.no_cpu_baseline:

@@ -673,6 +673,8 @@ struct Workspace {
   DevBuf<longlong2> lev_p[kMaxLevels];
   DevBuf<float> planes;
   DevBuf<Cand> cand_a, cand_b, tmp, sorted, accepted;
+  DevBuf<unsigned long long> sort_keys;  // bitonic sort of long lists (budgets above kRankSortMax)
+  DevBuf<int32_t> sort_idx;
   DevBuf<RectAux> aux, accepted_aux;
   DevBuf<int32_t> tested;
   DevBuf<uint8_t> sup;
@@ -1837,6 +1839,18 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     so.out = ws.sorted.p;
     so.state = st;
     so.slot = slot;
+    so.keys = nullptr;
+    so.idx = nullptr;
+    so.npow = 0;
+    if (cap > kRankSortMax) {
+      int np = 4096;
+      while (np < cap) np <<= 1;
+      ws.sort_keys.reserve(size_t(np));
+      ws.sort_idx.reserve(size_t(np));
+      so.keys = ws.sort_keys.p;
+      so.idx = ws.sort_idx.p;
+      so.npow = np;
+    }
     Span sp(kStSort, s);
     check(launch_sort(so, cap, s), "sort");
   }
@@ -1958,26 +1972,32 @@ FindOutput run_find(mvg_ncc_model_s& m, const void* pixels, int type, int64_t W,
     check(launch_select(se, s), "select");
   }
   // A round that accepts nothing (the candidates fail refinement or overlap)
-  // makes the next speculative batch the widest (64): fewer host round trips
-  // while a quota is far from met.  The matches do not depend on the batch:
-  // each candidate's refinement is its own, and the selection takes them in
-  // rank order.
+  // makes the next speculative batch the widest (64) and doubles the rounds
+  // queued per host check (up to 16): fewer host round trips while a quota
+  // is far from met.  The matches do not depend on either: each candidate's
+  // refinement is its own, the selection takes them in rank order, and the
+  // rounds queued past the end of the selection return at once (done).
   int prepared = batch_limit;  // batch bound of the last select launched
   int accepted = 0;
-  for (int round = 0; round < 100000; ++round) {
-    {
-      Span sp(kStRefine, s);
-      check(launch_refine(ra, prepared, s), "refine");
+  int ahead = 1;               // rounds queued per host check
+  for (int round = 0; round < 100000; round += ahead) {
+    for (int k = 0; k < ahead; ++k) {
+      {
+        Span sp(kStRefine, s);
+        check(launch_refine(ra, prepared, s), "refine");
+      }
+      {
+        Span sp(kStSelect, s);
+        check(launch_select(se, s), "select");
+      }
+      prepared = se.batch_limit;
     }
-    {
-      Span sp(kStSelect, s);
-      check(launch_select(se, s), "select");
-    }
-    prepared = se.batch_limit;
     check(cudaMemcpyAsync(ws.h_state, st, sizeof(QueryState), cudaMemcpyDeviceToHost, s), "state");
     check(cudaStreamSynchronize(s), "find");
     if (ws.h_state->done || !ws.h_state->need) break;
-    se.batch_limit = ws.h_state->accepted > accepted ? batch_limit : 64;
+    const bool none = ws.h_state->accepted == accepted;
+    se.batch_limit = none ? 64 : batch_limit;
+    ahead = none ? std::min(16, ahead * 2) : 1;
     accepted = ws.h_state->accepted;
   }
   const QueryState hs = *ws.h_state;

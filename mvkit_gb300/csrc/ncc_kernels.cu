@@ -1343,6 +1343,7 @@ __global__ void __launch_bounds__(256) sort_kernel(SortArgs a) {
   __shared__ int s_finite;
   const int n = live_count(a.state, a.slot);
   if (int(blockIdx.x) * kSortPer >= n) return;
+  if (a.keys && n > kRankSortMax) return;  // the bitonic sort takes it
   const int lane4 = threadIdx.x & 3;
   const int i = blockIdx.x * kSortPer + (threadIdx.x >> 2);
   Cand me{};
@@ -1392,6 +1393,112 @@ __global__ void __launch_bounds__(256) sort_kernel(SortArgs a) {
   if (i < n && lane4 == 0) {
     a.out[rank] = me;
     if (isfinite(me.score)) atomicAdd(&s_finite, 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && s_finite) atomicAdd(&a.state->sorted_count, s_finite);
+}
+
+// Bitonic sort of long candidate lists (more than kRankSortMax): (key,
+// index) pairs, padded to the power of two at or above the live count with
+// entries that order after every candidate; the comparator is the rank
+// sort's order (descending score key, then row, column, angle; the index for
+// exact duplicates).  Stages with k up to 2048 and the j < 2048 steps of
+// longer stages run in shared memory, one 2048-entry segment per block.
+__device__ __forceinline__ bool sort_before(unsigned long long ka, int ia, unsigned long long kb, int ib,
+                                            const Cand* __restrict__ in) {
+  if (ia == INT32_MAX) return false;
+  if (ib == INT32_MAX) return true;
+  if (ka != kb) return ka < kb;
+  const Cand x = in[ia], y = in[ib];
+  if (x.row != y.row) return x.row < y.row;
+  if (x.col != y.col) return x.col < y.col;
+  if (x.angle != y.angle) return x.angle < y.angle;
+  return ia < ib;
+}
+
+__device__ __forceinline__ int bitonic_live(const SortArgs& a) {
+  const int n = live_count(a.state, a.slot);
+  if (n <= kRankSortMax) return 0;
+  int p = 1;
+  while (p < n) p <<= 1;
+  return p;
+}
+
+__global__ void __launch_bounds__(256) bitonic_init_kernel(SortArgs a) {
+  const int np = bitonic_live(a);
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= np) return;
+  const int n = live_count(a.state, a.slot);
+  a.keys[r] = r < n ? desc_key(a.in[r].score) : ~0ULL;
+  a.idx[r] = r < n ? r : INT32_MAX;
+}
+
+// all steps j <= min(k, 2048) / 2 of the stages k0 .. k1 (k0 <= k1 <= 2048:
+// the whole network up to 2048; k0 == k1 > 2048: the shared-memory tail of
+// one stage) on this block's 2048-entry segment
+__global__ void __launch_bounds__(1024) bitonic_block_kernel(SortArgs a, int k0, int k1) {
+  __shared__ unsigned long long s_key[2048];
+  __shared__ int s_idx[2048];
+  const int np = bitonic_live(a);
+  const int base = blockIdx.x * 2048;
+  if (base >= np || k0 > np) return;
+  const int t = threadIdx.x;
+  s_key[t] = a.keys[base + t];
+  s_idx[t] = a.idx[base + t];
+  s_key[t + 1024] = a.keys[base + t + 1024];
+  s_idx[t + 1024] = a.idx[base + t + 1024];
+  __syncthreads();
+  for (int k = k0; k <= k1; k <<= 1) {
+    for (int j = min(k, 2048) >> 1; j > 0; j >>= 1) {
+      const int i = ((t & ~(j - 1)) << 1) | (t & (j - 1)), l = i + j;
+      const bool up = ((base + i) & k) == 0;
+      const unsigned long long ki = s_key[i], kl = s_key[l];
+      const int ii = s_idx[i], il = s_idx[l];
+      if (sort_before(kl, il, ki, ii, a.in) == up) {
+        s_key[i] = kl;
+        s_key[l] = ki;
+        s_idx[i] = il;
+        s_idx[l] = ii;
+      }
+      __syncthreads();
+    }
+  }
+  a.keys[base + t] = s_key[t];
+  a.idx[base + t] = s_idx[t];
+  a.keys[base + t + 1024] = s_key[t + 1024];
+  a.idx[base + t + 1024] = s_idx[t + 1024];
+}
+
+// one step j >= 2048 of stage k, in global memory
+__global__ void __launch_bounds__(256) bitonic_step_kernel(SortArgs a, int k, int j) {
+  const int np = bitonic_live(a);
+  if (k > np) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (np >> 1)) return;
+  const int i = ((t & ~(j - 1)) << 1) | (t & (j - 1)), l = i + j;
+  const bool up = (i & k) == 0;
+  const unsigned long long ki = a.keys[i], kl = a.keys[l];
+  const int ii = a.idx[i], il = a.idx[l];
+  if (sort_before(kl, il, ki, ii, a.in) == up) {
+    a.keys[i] = kl;
+    a.keys[l] = ki;
+    a.idx[i] = il;
+    a.idx[l] = ii;
+  }
+}
+
+__global__ void __launch_bounds__(256) bitonic_gather_kernel(SortArgs a) {
+  __shared__ int s_finite;
+  const int np = bitonic_live(a);
+  if (!np) return;
+  const int n = live_count(a.state, a.slot);
+  if (threadIdx.x == 0) s_finite = 0;
+  __syncthreads();
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n) {
+    const Cand c = a.in[a.idx[r]];
+    a.out[r] = c;
+    if (isfinite(c.score)) atomicAdd(&s_finite, 1);
   }
   __syncthreads();
   if (threadIdx.x == 0 && s_finite) atomicAdd(&a.state->sorted_count, s_finite);
@@ -2052,6 +2159,8 @@ constexpr int kRefineThreads = 512;
 __global__ void __launch_bounds__(kRefineThreads) refine_kernel(RefineArgs a) {
   __shared__ FitShared f;
   const int b = blockIdx.x;
+  // a queued round after the end of the selection has nothing to refine
+  if (a.batch_count < 0 && a.state->done) return;
   if (b >= (a.batch_count >= 0 ? a.batch_count : a.state->batch_count)) return;
   const int i = a.batch[b];
   if (threadIdx.x == 0) {
@@ -2265,6 +2374,18 @@ cudaError_t launch_pairs(const float* v, int w, int h, uint32_t* pairs, cudaStre
 
 cudaError_t launch_sort(const SortArgs& a, int max_candidates, cudaStream_t s) {
   sort_kernel<<<(max_candidates + kSortPer - 1) / kSortPer, 256, 0, s>>>(a);
+  if (a.keys) {
+    // every launch reads the live count and returns when it has no work
+    if (a.npow < max_candidates || a.npow < 4096 || (a.npow & (a.npow - 1))) return cudaErrorInvalidValue;
+    const unsigned segs = unsigned(a.npow / 2048), pairs = unsigned(a.npow / 2 / 256);
+    bitonic_init_kernel<<<unsigned(a.npow / 256), 256, 0, s>>>(a);
+    bitonic_block_kernel<<<segs, 1024, 0, s>>>(a, 2, 2048);
+    for (int k = 4096; k <= a.npow; k <<= 1) {
+      for (int j = k >> 1; j >= 2048; j >>= 1) bitonic_step_kernel<<<pairs, 256, 0, s>>>(a, k, j);
+      bitonic_block_kernel<<<segs, 1024, 0, s>>>(a, k, k);
+    }
+    bitonic_gather_kernel<<<unsigned((max_candidates + 255) / 256), 256, 0, s>>>(a);
+  }
   return cudaGetLastError();
 }
 

@@ -305,11 +305,20 @@ struct Refine4Args {
   double max_shift, max_angle, max_scale;  // step limits per iteration
 };
 
+// Candidate sort.  Lists of up to kRankSortMax candidates are rank-sorted
+// in one launch; longer ones (candidate budgets above it) by a bitonic sort
+// of (key, index) pairs in `keys` / `idx` (npow entries each, npow the power
+// of two at or above the budget; null when the budget is at most
+// kRankSortMax).  Both give the same order.
+constexpr int kRankSortMax = 16384;
 struct SortArgs {
   const Cand* in;
   Cand* out;
   QueryState* state;
   int slot;
+  unsigned long long* keys;
+  int32_t* idx;
+  int npow;
 };
 
 // Level-0 model rectangle about the origin: [left, right] x [top, bottom]

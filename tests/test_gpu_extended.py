@@ -143,3 +143,39 @@ def test_batched_configuration_scaled(mg, orc_ext):
     for i, (g, w) in enumerate(zip(got, want)):
         assert len(w) >= len(batch[i].poses[0])
         assert_same_matches(g[:4], w, f"batch scene {i}")
+
+
+def test_long_candidate_list_sorted(mg, orc_ext):
+    """More than 16 384 full-resolution candidates (the budget_360 scene tiled
+    2 x 2 under extended budgets) take the long-list sort: the sorted list
+    follows the reference's order exactly (score descending, then row,
+    column, angle; matcher.cpp:824-827) on the GPU's own scores, holds no
+    duplicate and the oracle's candidates, and the final matches equal the
+    oracle's."""
+    case = CASES["budget_360"]
+    wl, _ = make_inputs(case)
+    image = np.ascontiguousarray(np.tile(wl.image, (2, 2)))
+    c, f = case["create"], case["find"]
+    ctl = (f["angle_start"], f["angle_extent"], f["min_score"], f["num_matches"], f["max_overlap"], "true",
+           [f["highest"], f["lowest"]])
+    fargs = (f["angle_start"], f["angle_extent"], f["min_score"], f["num_matches"], f["max_overlap"], True,
+             f["highest"], f["lowest"])
+    model = mg.create_ncc_model(wl.template, "auto", c["angle_start"], c["angle_extent"], "auto", "use_polarity")
+    om = orc_ext.create(wl.template, levels=0, angle_start=c["angle_start"], angle_extent=c["angle_extent"])
+    want = orc_ext.find(om, image, *fargs, stage=100, capacity=200_000)
+    want = want[np.isfinite(want[:, 3])]
+    with mg.extended_budgets(**EXT):
+        got = mg.find_ncc_model_stage(image, model, *ctl, stage=100)
+        matches = mg.find_ncc_model(image, model, *ctl)
+    assert len(got) > 16_384, len(got)
+    s = got[:, 3]
+    assert np.all(np.diff(s) <= 0), "sorted by score"
+    for i in np.nonzero(np.diff(s) == 0)[0]:
+        assert tuple(got[i, :3]) < tuple(got[i + 1, :3]), f"tie order at {i}"
+    assert len({tuple(r[:3]) for r in got}) == len(got), "duplicate candidates"
+    ws = {(r[0], r[1], r[2]): r[3] for r in want}
+    common = [r for r in got if (r[0], r[1], r[2]) in ws]
+    assert len(common) >= len(want) - 2 and len(got) <= len(want) + 2, (len(common), len(want), len(got))
+    for r in common:
+        assert abs(r[3] - ws[(r[0], r[1], r[2])]) < 1e-4
+    assert_same_matches(matches, orc_ext.find(om, image, *fargs), "budget_360 tiled 2 x 2")
