@@ -150,7 +150,7 @@ def test_long_candidate_list_sorted(mg, orc_ext):
     2 x 2 under extended budgets) take the long-list sort: the sorted list
     follows the reference's order exactly (score descending, then row,
     column, angle; matcher.cpp:824-827) on the GPU's own scores, holds no
-    duplicate and the oracle's candidates, and the final matches equal the
+    duplicate and the oracle's candidates, and the final matches are the
     oracle's."""
     case = CASES["budget_360"]
     wl, _ = make_inputs(case)
@@ -178,4 +178,11 @@ def test_long_candidate_list_sorted(mg, orc_ext):
     assert len(common) >= len(want) - 2 and len(got) <= len(want) + 2, (len(common), len(want), len(got))
     for r in common:
         assert abs(r[3] - ws[(r[0], r[1], r[2])]) < 1e-4
-    assert_same_matches(matches, orc_ext.find(om, image, *fargs), "budget_360 tiled 2 x 2")
+    # the tiles are copies: their matches tie in score (to ~1e-7, where the
+    # FP32 and FP64 orders of a tie differ), so compare them as a set
+    want_m = oracle_lib.to_halcon(orc_ext.find(om, image, *fargs))
+    got_m = np.stack(matches[:4], axis=1)
+    assert got_m.shape == want_m.shape, (got_m, want_m)
+    key = lambda m: m[np.lexsort((m[:, 1], m[:, 0]))]
+    d = np.abs(key(got_m) - key(want_m))
+    assert d[:, :2].max() <= 0.05 and d[:, 2].max() <= math.radians(0.05) and d[:, 3].max() <= 1e-4, (got_m, want_m)
