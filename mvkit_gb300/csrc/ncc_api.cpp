@@ -917,6 +917,7 @@ class TcBatcher {
   Stats stats() {
     std::lock_guard<std::mutex> lk(m_);
     Stats st;
+    st.ms = folded_ms_;
     for (auto& t : timing_) {
       float ms = 0;
       if (cudaEventSynchronize(t.second) == cudaSuccess && cudaEventElapsedTime(&ms, t.first, t.second) == cudaSuccess)
@@ -932,6 +933,7 @@ class TcBatcher {
     std::lock_guard<std::mutex> lk(m_);
     launches_ = jobs_count_ = 0;
     macs_ = issued_ = 0;
+    folded_ms_ = 0;
     for (auto& t : timing_) {
       cudaEventDestroy(t.first);
       cudaEventDestroy(t.second);
@@ -947,6 +949,21 @@ class TcBatcher {
     cudaEvent_t ready, done;
     const char* error = nullptr;
   };
+
+  // Keeps the timing events bounded: past 1024 launches since the last
+  // reset, the oldest 512 (long complete) are summed and released.
+  void fold_timing_locked() {
+    if (timing_.size() <= 1024) return;
+    for (size_t i = 0; i < 512; ++i) {
+      float ms = 0;
+      if (cudaEventSynchronize(timing_[i].second) == cudaSuccess &&
+          cudaEventElapsedTime(&ms, timing_[i].first, timing_[i].second) == cudaSuccess)
+        folded_ms_ += ms;
+      cudaEventDestroy(timing_[i].first);
+      cudaEventDestroy(timing_[i].second);
+    }
+    timing_.erase(timing_.begin(), timing_.begin() + 512);
+  }
 
   // Launches every pending job, grouped by launch shape (at most kTcMaxJobs
   // a launch), and wakes the waiters.  Done events alternate between two
@@ -998,6 +1015,7 @@ class TcBatcher {
             err = "tensor-core batch: launch";
           cudaEventRecord(t1, stream_);
           timing_.emplace_back(t0, t1);
+          fold_timing_locked();
           ++launches_;
           jobs_count_ += int64_t(jobs.size());
         }
@@ -1025,6 +1043,7 @@ class TcBatcher {
   DevBuf<int> next_;
   cudaEvent_t done_[2 * kDoneSlots] = {};
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> timing_;
+  double folded_ms_ = 0;  // event time of launches whose events were released
   int64_t launches_ = 0, jobs_count_ = 0;
   double macs_ = 0, issued_ = 0;
 };
