@@ -584,6 +584,17 @@ def ncc_score_gradient(image, model: NccModel, poses, stream=None):
     return score, grad
 
 
+def parabola_vertex_offsets(sm, s0, sp):
+    """Vertex positions, in steps and clipped to [-1, 1], of the parabolas
+    through (-1, sm), (0, s0), (1, sp); 0 where a value is not finite or the
+    parabola does not open downwards."""
+    sm, s0, sp = (np.asarray(v, dtype=np.float64) for v in (sm, s0, sp))
+    den = sm - 2 * s0 + sp
+    ok = np.isfinite(sm) & np.isfinite(sp) & np.isfinite(s0) & (den < 0)
+    off = np.where(ok, 0.5 * (sm - sp) / np.where(ok, den, -1.0), 0.0)
+    return np.clip(off, -1.0, 1.0)
+
+
 def ncc_quadratic_peak_fit(image, model: NccModel, poses, steps, stream=None):
     """Quadratic peak fitting of similarity poses (row, column, angle, scale),
     the plain form of sub-sample pose estimation kept beside the Gauss-Newton
@@ -606,11 +617,7 @@ def ncc_quadratic_peak_fit(image, model: NccModel, poses, steps, stream=None):
     sc = sc.reshape(n, 9)
     s0 = sc[:, 0]
     for d in range(4):
-        sm, sp = sc[:, 1 + 2 * d], sc[:, 2 + 2 * d]
-        den = sm - 2 * s0 + sp
-        ok = np.isfinite(sm) & np.isfinite(sp) & np.isfinite(s0) & (den < 0)
-        off = np.where(ok, 0.5 * (sm - sp) / np.where(ok, den, -1.0), 0.0)
-        p[:, d] += np.clip(off, -1.0, 1.0) * steps[d]
+        p[:, d] += parabola_vertex_offsets(sc[:, 1 + 2 * d], s0, sc[:, 2 + 2 * d]) * steps[d]
     score, _ = ncc_score_gradient(image, model, p, stream=stream)
     return p, score
 
